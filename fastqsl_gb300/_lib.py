@@ -1,0 +1,87 @@
+"""ctypes binding of libfastqsl_gb300.so (the C ABI in include/fastqsl_gb300.h).
+
+There is no CPU fallback: if the shared object is missing or no CUDA device
+is visible, every entry point raises.
+"""
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfastqsl_gb300.so")
+
+_lib = None
+_lock = threading.Lock()
+
+c_f32p = ctypes.c_void_p  # device pointers travel as integers
+c_i64 = ctypes.c_int64
+c_int = ctypes.c_int
+c_float = ctypes.c_float
+c_double = ctypes.c_double
+c_vp = ctypes.c_void_p
+
+
+class QslError(RuntimeError):
+    pass
+
+
+class TraceIO(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "inp_x", "inp_y", "inp_z", "start_x", "start_y", "start_z", "flag_start",
+        "end_x", "end_y", "end_z", "flag_end", "B_this_x", "B_this_y", "B_this_z", "B_flag",
+        "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist")]
+
+
+# name -> (restype, argtypes); every pointer is c_void_p
+_P = c_vp
+_SIGS = {
+    "qsl_version": (ctypes.c_char_p, []),
+    "qsl_last_error": (ctypes.c_char_p, []),
+    "qsl_device_sm_count": (c_int, [_P]),
+    "qsl_params_reference_rk4": (None, [_P]),
+    "qsl_params_reference_rkf45": (None, [_P]),
+    "qsl_trace_all_bline": (c_int, [c_int, c_int] + [_P] * 35 + [c_i64, _P]),
+    "qsl_trace_all_bline_rkf45": (c_int, [_P] * 35 + [_P]),
+    "qsl_trace_all_bline_rk4": (c_int, [_P] * 34 + [_P]),
+    "qsl_field_store_bytes": (c_i64, [c_int, c_int, c_int, c_int]),
+    "qsl_field_create": (c_int, [_P, _P, _P, c_int, c_int, c_int, c_int, _P, _P]),
+    "qsl_field_destroy": (c_int, [_P]),
+    "qsl_field_bytes": (c_i64, [_P]),
+    "qsl_field_update": (c_int, [_P, _P, _P, _P, _P]),
+    "qsl_trace": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, _P, c_int, _P, _P, _P]),
+    "qsl_qcalc_plane": (c_int, [_P] * 13 + [c_int, c_int, c_i64, c_double, _P, _P, _P, _P]),
+    "qsl_cook_workspace_bytes": (c_i64, [c_i64]),
+    "qsl_cook_pseudo_line": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 8 + [c_i64, _P]),
+    "qsl_qcut": (c_int, [_P] * 10 + [c_i64, _P, c_i64, c_double, _P, _P, _P]),
+    "qsl_qmerge": (c_int, [_P, _P, _P, c_i64, _P, c_i64, c_int, c_int, _P, _P, _P]),
+}
+
+
+def exported_names():
+    return list(_SIGS)
+
+
+def load(path=None):
+    """Loads the shared object (once) and declares every entry point."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise QslError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                           f"or `python -m fastqsl_gb300._build` (no CPU fallback exists)")
+        lib = ctypes.CDLL(p)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = load().qsl_last_error().decode(errors="replace")
+        raise QslError(f"{what} failed ({rc}): {msg}")
+    return rc

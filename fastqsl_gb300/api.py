@@ -1,0 +1,253 @@
+"""Native Python API over the C ABI: resident field stores, tracing and the
+on-device Q-map pipeline.
+
+Buffers are PyTorch CUDA tensors (or any object exposing
+``__cuda_array_interface__``); every computation runs in the CUDA kernels of
+libfastqsl_gb300.so on the given (default: current) stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .params import TraceParams, absolute_rkf45
+
+LAYOUTS = {"soa": 0, "f4": 1, "h4b": 2}
+SCHEDULES = {"queue": 0, "static": 1}
+
+TRACE_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
+             "B_this_x", "B_this_y", "B_this_z", "B_start_x", "B_start_y", "B_start_z",
+             "B_end_x", "B_end_y", "B_end_z"]
+TRACE_I32 = ["flag_start", "flag_end", "B_flag"]
+
+
+def ptr(a):
+    """Device address of a CUDA tensor / __cuda_array_interface__ array."""
+    if a is None:
+        return None
+    if isinstance(a, torch.Tensor):
+        if not a.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        return a.data_ptr()
+    cai = getattr(a, "__cuda_array_interface__", None)
+    if cai is not None:
+        return int(cai["data"][0])
+    raise TypeError(f"not a device array: {type(a)}")
+
+
+def stream_handle(stream=None):
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, torch.cuda.Stream):
+        return stream.cuda_stream
+    return int(stream)
+
+
+def as_xfast(a, device="cuda"):
+    """A float32 CUDA tensor of shape (nx, ny, nz) with x fastest in memory
+    (strides (1, nx, nx*ny)), copying only when needed."""
+    t = a if isinstance(a, torch.Tensor) else torch.as_tensor(a)
+    if t.dim() != 3:
+        raise ValueError("field arrays must be 3-D (nx, ny, nz)")
+    t = t.to(device=device, dtype=torch.float32)
+    nx, ny, _ = t.shape
+    if t.stride() != (1, nx, nx * ny):
+        t = t.permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    return t
+
+
+class FieldStore:
+    """A field resident on the device in one of the GB300 layouts.
+
+    layout: 'h4b' (fp16 8^3 bricks + per-brick scale), 'f4' (interleaved
+    float4) or 'soa' (the caller's arrays in place)."""
+
+    def __init__(self, Bx, By, Bz, layout="h4b", stream=None):
+        lib = _lib.load()
+        if layout not in LAYOUTS:
+            raise ValueError(f"layout must be one of {list(LAYOUTS)}")
+        self.layout = layout
+        arrs = [as_xfast(b) for b in (Bx, By, Bz)]
+        if len({tuple(a.shape) for a in arrs}) != 1:
+            raise ValueError("Bx, By, Bz must have the same shape")
+        self.shape = tuple(int(s) for s in arrs[0].shape)
+        self._keep = arrs if layout == "soa" else None
+        h = ctypes.c_void_p()
+        _lib.check(lib.qsl_field_create(ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]), *self.shape, LAYOUTS[layout],
+                                        stream_handle(stream), ctypes.byref(h)), "qsl_field_create")
+        self._h = h
+        self.nbytes = int(lib.qsl_field_bytes(h))
+        if layout != "soa" and isinstance(stream, torch.cuda.Stream):
+            # the conversion read the source arrays on `stream`; the caching
+            # allocator may hand their memory to another stream once freed
+            for a in arrs:
+                a.record_stream(stream)
+
+    def update(self, Bx, By, Bz, stream=None):
+        """Refills the store from new arrays of the same shape (x fastest,
+        float32, on the device) without reallocating."""
+        arrs = [as_xfast(b) for b in (Bx, By, Bz)]
+        if tuple(arrs[0].shape) != self.shape:
+            raise ValueError("shape differs from the store's")
+        if self.layout == "soa":
+            self._keep = arrs
+        _lib.check(_lib.load().qsl_field_update(self.handle, ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]),
+                                                stream_handle(stream)), "qsl_field_update")
+
+    @staticmethod
+    def store_bytes(shape, layout):
+        return int(_lib.load().qsl_field_store_bytes(*shape, LAYOUTS[layout]))
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("field store is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _lib.load().qsl_field_destroy(self._h)
+            self._h = None
+            self._keep = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def alloc_trace_outputs(n, device="cuda", twist=False):
+    out = {k: torch.zeros(n, dtype=torch.float32, device=device) for k in TRACE_F32}
+    out.update({k: torch.zeros(n, dtype=torch.int32, device=device) for k in TRACE_I32})
+    out["LineLen"] = torch.zeros(n, dtype=torch.float64, device=device)
+    out["twist"] = torch.zeros(n, dtype=torch.float64, device=device) if twist else None
+    return out
+
+
+def _io(xs, ys, zs, out):
+    io = _lib.TraceIO()
+    io.inp_x, io.inp_y, io.inp_z = ptr(xs), ptr(ys), ptr(zs)
+    for k in TRACE_F32 + TRACE_I32 + ["LineLen"]:
+        setattr(io, k, ptr(out[k]))
+    io.twist = ptr(out.get("twist"))
+    return io
+
+
+def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_len=0.125, tol_coef=1.0,
+          cross_dir=(0.0, 0.0, 1.0), curB=None, schedule="queue", out=None, n=None, n_dev=None, samples=None,
+          queue=None, stream=None):
+    """Traces every seed (xs, ys, zs: float32 CUDA vectors) both ways.
+    Returns the output dict (allocated unless `out` is given).  `n_dev`: a
+    device counter holding the seed count (outputs must then hold the largest
+    count).  `samples`: optional int64 CUDA tensor accumulating the number of
+    trilinear samples taken."""
+    lib = _lib.load()
+    if params is None:
+        params = absolute_rkf45()
+    n = int(xs.shape[0]) if n is None else int(n)
+    if out is None:
+        out = alloc_trace_outputs(n, xs.device, twist=curB is not None)
+    cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
+    cur = [ptr(c) for c in curB] if curB is not None else [None, None, None]
+    if curB is not None and out.get("twist") is None:
+        out["twist"] = torch.zeros(out["LineLen"].shape[0], dtype=torch.float64, device=xs.device)
+    io = _io(xs, ys, zs, out)
+    _lib.check(lib.qsl_trace(field.handle, ctypes.byref(params), ctypes.byref(io), n, ptr(n_dev),
+                             float(s_len), float(tol_coef), cd, *cur, SCHEDULES[schedule], ptr(samples), ptr(queue),
+                             stream_handle(stream)), "qsl_trace")
+    return out
+
+
+class QMapPlan:
+    """Device buffers and launch sequence of the Q pipeline for `nplanes`
+    stacked (n0, n1) seed planes (rows along y, columns along x):
+
+    trace all seeds -> Q on interior pixels (FP64 Jacobian norm and flux
+    ratio) -> compact the B_flag pixels -> trace their 4 pseudo-lines -> Q of
+    those pixels -> merge.  No host synchronisation inside; the pseudo-line
+    trace reads its seed count from the device, so a whole run can be
+    captured in a CUDA graph.  Outputs Q of shape (nplanes, n0-2, n1-2)
+    (float64).  Reference workflow: demo/Q_RKF45CuPy3D.ipynb cell 7 and
+    demo/Q_RKF45CuPy.ipynb cells 7-11."""
+
+    def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True):
+        self.n0, self.n1, self.nplanes = int(n0), int(n1), int(nplanes)
+        if self.n0 < 3 or self.n1 < 3:
+            raise ValueError("planes must be at least 3 x 3 seeds")
+        self.n = self.n0 * self.n1 * self.nplanes
+        self.device = device
+        self.pseudo = pseudo
+        self.main = alloc_trace_outputs(self.n, device)
+        self.Q = torch.empty((self.nplanes, self.n0 - 2, self.n1 - 2), dtype=torch.float64, device=device)
+        self.queue = torch.zeros(2, dtype=torch.int64, device=device)
+        self.samples = torch.zeros(1, dtype=torch.int64, device=device)
+        if pseudo:
+            m = self.nplanes * (self.n0 - 2) * (self.n1 - 2)  # at most every interior pixel
+            self.max_pix = m
+            self.cut = [torch.empty(4 * m, dtype=torch.float32, device=device) for _ in range(3)]
+            self.bz0s = torch.empty(m, dtype=torch.float32, device=device)
+            self.bz0e = torch.empty(m, dtype=torch.float32, device=device)
+            self.pix = torch.empty(m, dtype=torch.int64, device=device)
+            self.count = torch.zeros(2, dtype=torch.int64, device=device)
+            wb = int(_lib.load().qsl_cook_workspace_bytes(self.n))
+            self.work = torch.empty((wb + 7) // 8, dtype=torch.int64, device=device)
+            self.work_bytes = wb
+            self.sub = alloc_trace_outputs(4 * m, device)
+            self.qcut = torch.empty(m, dtype=torch.float64, device=device)
+
+    def run(self, field, xs, ys, zs, params=None, s_len=0.125, tol_coef=1.0, stride=1.0, cross_dir=(0.0, 0.0, 1.0),
+            pseudo_tol_factor=1.0, count_samples=False, stream=None):
+        lib = _lib.load()
+        st = stream_handle(stream)
+        if params is None:
+            params = absolute_rkf45()
+        samples = self.samples if count_samples else None
+        if count_samples:
+            self.samples.zero_()
+        m = self.main
+        trace(field, xs, ys, zs, params, s_len, tol_coef, cross_dir, out=m, n=self.n, samples=samples,
+              queue=self.queue, stream=stream)
+        jac = (1.0 / (2.0 * float(stride))) ** 4.0
+        cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
+        _lib.check(lib.qsl_qcalc_plane(ptr(m["end_x"]), ptr(m["end_y"]), ptr(m["end_z"]), ptr(m["flag_end"]),
+                                       ptr(m["start_x"]), ptr(m["start_y"]), ptr(m["start_z"]), ptr(m["flag_start"]),
+                                       ptr(m["B_start_z"]), ptr(m["B_end_z"]), ptr(m["B_this_x"]),
+                                       ptr(m["B_this_y"]), ptr(m["B_this_z"]), self.n0, self.n1, self.nplanes, jac,
+                                       cd, None, ptr(self.Q), st), "qsl_qcalc_plane")
+        if not self.pseudo:
+            return self.Q
+        _lib.check(lib.qsl_cook_pseudo_line(ptr(m["B_flag"]), ptr(m["start_x"]), ptr(m["start_y"]),
+                                            ptr(m["start_z"]), ptr(m["flag_start"]), ptr(m["B_start_z"]),
+                                            ptr(m["B_end_z"]), self.n, self.n0, self.n1, 1, float(stride),
+                                            ptr(self.cut[0]), ptr(self.cut[1]), ptr(self.cut[2]), ptr(self.bz0s),
+                                            ptr(self.bz0e), ptr(self.pix), ptr(self.count), ptr(self.work),
+                                            self.work_bytes, st), "qsl_cook_pseudo_line")
+        cnt_seeds = self.count[1:2]
+        trace(field, self.cut[0], self.cut[1], self.cut[2], params, s_len, tol_coef * pseudo_tol_factor, cross_dir,
+              out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds, samples=samples, queue=self.queue[1:2],
+              stream=stream)
+        s = self.sub
+        _lib.check(lib.qsl_qcut(ptr(s["start_x"]), ptr(s["start_y"]), ptr(s["start_z"]), ptr(s["flag_start"]),
+                                ptr(s["end_x"]), ptr(s["end_y"]), ptr(s["end_z"]), ptr(s["flag_end"]),
+                                ptr(self.bz0s), ptr(self.bz0e), 0, ptr(self.count[0:1]), self.max_pix, jac, None,
+                                ptr(self.qcut), st), "qsl_qcut")
+        _lib.check(lib.qsl_qmerge(ptr(self.pix), None, ptr(self.qcut), 0, ptr(self.count[0:1]), self.max_pix,
+                                  self.n0, self.n1, None, ptr(self.Q), st), "qsl_qmerge")
+        return self.Q
+
+
+def plane_seed_grid(x0, x1, nx, y0, y1, ny, zs, device="cuda"):
+    """Stacked seed planes: for each z in `zs`, an (ny, nx) grid over
+    [x0, x1] x [y0, y1] (linspace per axis, rows along y).  Returns flattened
+    float32 CUDA vectors (x, y, z)."""
+    xi = torch.linspace(x0, x1, nx, dtype=torch.float32, device=device)
+    yi = torch.linspace(y0, y1, ny, dtype=torch.float32, device=device)
+    zt = torch.as_tensor(zs, dtype=torch.float32, device=device).reshape(-1)
+    npl = zt.shape[0]
+    X = xi.view(1, 1, nx).expand(npl, ny, nx)
+    Y = yi.view(1, ny, 1).expand(npl, ny, nx)
+    Z = zt.view(npl, 1, 1).expand(npl, ny, nx)
+    return X.reshape(-1).contiguous(), Y.reshape(-1).contiguous(), Z.reshape(-1).contiguous()

@@ -1,0 +1,510 @@
+// C ABI of fastqsl_gb300 (declarations and contracts in
+// include/fastqsl_gb300.h).
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <new>
+
+#include "../../include/fastqsl_gb300.h"
+#include "qassembly.h"
+#include "qsl_internal.h"
+
+using namespace qsl;
+
+static thread_local char g_err[512];
+
+static int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? QSL_ERR_NOMEM : QSL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define QSL_CHECK_CUDA(expr, what)                  \
+    do {                                            \
+        cudaError_t e_ = (expr);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+namespace qsl {
+
+int persistent_grid(const void* kernel, int block, size_t smem) {
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, smem) != cudaSuccess) return -1;
+    if (per < 1) per = 1;
+    return sms * per;
+}
+
+}  // namespace qsl
+
+extern "C" {
+
+const char* qsl_last_error(void) { return g_err; }
+
+const char* qsl_version(void) { return "fastqsl_gb300 0.1 (sm_103a)"; }
+
+void qsl_params_reference_rk4(qsl_trace_params* p) {
+    p->integrator = QSL_RK4;
+    p->tol_law = QSL_TOL_REFERENCE;
+    p->tol = 1e-3;
+    p->h_min = 0.1;
+    p->h_max = 100.0;
+    p->reject_factor = 0.618;
+    p->len_ratio = 2.0;
+    p->max_steps = 100000;
+    p->boundary_twist = 1;
+    p->arith = QSL_ARITH_EXACT;
+}
+
+void qsl_params_reference_rkf45(qsl_trace_params* p) {
+    p->integrator = QSL_RKF45;
+    p->tol_law = QSL_TOL_REFERENCE;
+    p->tol = 1e-3;
+    p->h_min = 0.1;
+    p->h_max = 100.0;
+    p->reject_factor = 0.618;
+    p->len_ratio = 3.0;
+    p->max_steps = 500000;
+    p->boundary_twist = 0;
+    p->arith = QSL_ARITH_EXACT;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Field stores
+// ---------------------------------------------------------------------------
+struct qsl_field {
+    int layout;
+    Dims d;
+    const float *bx, *by, *bz;  // SOA only: the caller's arrays (borrowed)
+    float4* f4;
+    uint2* bricks;
+    float* scale;
+    int nbx, nby, nbz;
+    int64_t bytes;
+    int device;
+};
+
+static int64_t layout_bytes(int nx, int ny, int nz, int layout, int* nbx, int* nby, int* nbz) {
+    const int bx = (nx - 1 + BRICK_CELLS - 1) / BRICK_CELLS, by = (ny - 1 + BRICK_CELLS - 1) / BRICK_CELLS,
+              bz = (nz - 1 + BRICK_CELLS - 1) / BRICK_CELLS;
+    if (nbx) *nbx = bx;
+    if (nby) *nby = by;
+    if (nbz) *nbz = bz;
+    const int64_t nodes = (int64_t)nx * ny * nz;
+    switch (layout) {
+        case LAYOUT_SOA: return 0;
+        case LAYOUT_F4: return nodes * (int64_t)sizeof(float4);
+        case LAYOUT_H4B: {
+            const int64_t nb = (int64_t)bx * by * bz;
+            return nb * BRICK_U2 * (int64_t)sizeof(uint2) + nb * (int64_t)sizeof(float);
+        }
+        default: return -1;
+    }
+}
+
+static bool dims_ok(int nx, int ny, int nz) {
+    if (nx < 2 || ny < 2 || nz < 2) return false;
+    // 32-bit cell coordinates and brick indices; 2^40 nodes is far beyond HBM.
+    return (double)nx * ny * nz < 1.1e12;
+}
+
+extern "C" {
+
+int64_t qsl_field_store_bytes(int nx, int ny, int nz, int layout) {
+    if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
+    const int64_t b = layout_bytes(nx, ny, nz, layout, nullptr, nullptr, nullptr);
+    if (b < 0) return fail(QSL_ERR_INVALID, "unknown layout %d", layout);
+    return b;
+}
+
+int qsl_field_create(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz, int layout,
+                     qsl_stream_t stream, qsl_field_t** out) {
+    if (!out) return fail(QSL_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (!Bx || !By || !Bz) return fail(QSL_ERR_INVALID, "null field array");
+    if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
+    int nbx, nby, nbz;
+    const int64_t bytes = layout_bytes(nx, ny, nz, layout, &nbx, &nby, &nbz);
+    if (bytes < 0) return fail(QSL_ERR_INVALID, "unknown layout %d", layout);
+    qsl_field* f = new (std::nothrow) qsl_field();
+    if (!f) return fail(QSL_ERR_NOMEM, "host allocation failed");
+    f->layout = layout;
+    f->d = Dims{nx, ny, nz};
+    f->bytes = bytes;
+    f->nbx = nbx;
+    f->nby = nby;
+    f->nbz = nbz;
+    cudaGetDevice(&f->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (layout == LAYOUT_SOA) {
+        f->bx = Bx;
+        f->by = By;
+        f->bz = Bz;
+    } else if (layout == LAYOUT_F4) {
+        e = cudaMalloc(&f->f4, (size_t)bytes);
+        if (e == cudaSuccess) e = launch_pack_f4(Bx, By, Bz, f->d, f->f4, st);
+    } else {
+        const int64_t nb = (int64_t)nbx * nby * nbz;
+        e = cudaMalloc(&f->bricks, (size_t)(nb * BRICK_U2 * sizeof(uint2)));
+        if (e == cudaSuccess) e = cudaMalloc(&f->scale, (size_t)(nb * sizeof(float)));
+        if (e == cudaSuccess) e = launch_pack_h4b(Bx, By, Bz, f->d, nbx, nby, nbz, f->bricks, f->scale, st);
+    }
+    if (e != cudaSuccess) {
+        cudaFree(f->f4);
+        cudaFree(f->bricks);
+        cudaFree(f->scale);
+        delete f;
+        return cuda_fail(e, "qsl_field_create");
+    }
+    *out = f;
+    return QSL_OK;
+}
+
+int qsl_field_destroy(qsl_field_t* f) {
+    if (!f) return QSL_OK;
+    cudaFree(f->f4);
+    cudaFree(f->bricks);
+    cudaFree(f->scale);
+    delete f;
+    return QSL_OK;
+}
+
+int64_t qsl_field_bytes(const qsl_field_t* f) { return f ? f->bytes : 0; }
+
+int qsl_field_update(qsl_field_t* f, const float* Bx, const float* By, const float* Bz, qsl_stream_t stream) {
+    if (!f || !Bx || !By || !Bz) return fail(QSL_ERR_INVALID, "null argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (f->layout == LAYOUT_SOA) {
+        f->bx = Bx;
+        f->by = By;
+        f->bz = Bz;
+        return QSL_OK;
+    }
+    cudaError_t e = f->layout == LAYOUT_F4
+                        ? launch_pack_f4(Bx, By, Bz, f->d, f->f4, st)
+                        : launch_pack_h4b(Bx, By, Bz, f->d, f->nbx, f->nby, f->nbz, f->bricks, f->scale, st);
+    if (e != cudaSuccess) return cuda_fail(e, "qsl_field_update");
+    return QSL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Tracing
+// ---------------------------------------------------------------------------
+static TraceOut make_out(const qsl_trace_io* io) {
+    TraceOut o;
+    o.start_x = io->start_x; o.start_y = io->start_y; o.start_z = io->start_z; o.flag_start = io->flag_start;
+    o.end_x = io->end_x; o.end_y = io->end_y; o.end_z = io->end_z; o.flag_end = io->flag_end;
+    o.bthis_x = io->B_this_x; o.bthis_y = io->B_this_y; o.bthis_z = io->B_this_z; o.b_flag = io->B_flag;
+    o.bstart_x = io->B_start_x; o.bstart_y = io->B_start_y; o.bstart_z = io->B_start_z;
+    o.bend_x = io->B_end_x; o.bend_y = io->B_end_y; o.bend_z = io->B_end_z;
+    o.line_len = io->LineLen;
+    o.twist = io->twist;
+    return o;
+}
+
+static bool io_ok(const qsl_trace_io* io) {
+    return io && io->inp_x && io->inp_y && io->inp_z && io->start_x && io->start_y && io->start_z &&
+           io->flag_start && io->end_x && io->end_y && io->end_z && io->flag_end && io->B_this_x && io->B_this_y &&
+           io->B_this_z && io->B_flag && io->B_start_x && io->B_start_y && io->B_start_z && io->B_end_x &&
+           io->B_end_y && io->B_end_z && io->LineLen;
+}
+
+static bool params_ok(const qsl_trace_params* p) {
+    return p && (p->integrator == QSL_RK4 || p->integrator == QSL_RKF45) &&
+           (p->tol_law == QSL_TOL_REFERENCE || p->tol_law == QSL_TOL_ABSOLUTE) &&
+           (p->arith == QSL_ARITH_EXACT || p->arith == QSL_ARITH_FAST) && p->max_steps >= 0 &&
+           p->max_steps <= 0x7fffffff && p->reject_factor > 0.0 && p->reject_factor < 1.0 && p->len_ratio >= 0.0;
+}
+
+template <class F>
+static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long long n_host,
+                     unsigned long long* queue_dev, cudaStream_t st) {
+    unsigned long long* q = nullptr;
+    bool own = false;
+    if (schedule == QSL_SCHED_QUEUE) {
+        q = queue_dev;
+        if (!q) {
+            QSL_CHECK_CUDA(cudaMallocAsync((void**)&q, sizeof(unsigned long long), st), "queue allocation");
+            own = true;
+        }
+        cudaError_t e = cudaMemsetAsync(q, 0, sizeof(unsigned long long), st);
+        if (e != cudaSuccess) {
+            if (own) cudaFreeAsync(q, st);
+            return cuda_fail(e, "queue reset");
+        }
+    }
+    J.queue = q;
+    const Schedule sched = schedule == QSL_SCHED_QUEUE ? SCHED_QUEUE : SCHED_STATIC;
+    cudaError_t e;
+    if constexpr (std::is_same<F, FieldSoA>::value) {
+        e = arith == QSL_ARITH_EXACT ? launch_trace_exact(J, twist, sched, n_host, st)
+                                     : launch_trace_fast_soa(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldF4>::value) {
+        e = launch_trace_fast_f4(J, twist, sched, n_host, st);
+    } else {
+        e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
+    }
+    if (own) cudaFreeAsync(q, st);
+    if (e != cudaSuccess) return cuda_fail(e, "trace launch");
+    return QSL_OK;
+}
+
+template <class F>
+static void fill_common(TraceJob<F>& J, const qsl_trace_io* io, const qsl_trace_params* prm,
+                        unsigned long long* samples_dev) {
+    J.shape_dev = nullptr;
+    J.cur = FieldSoA{nullptr, nullptr, nullptr, J.f.d};
+    J.inp_x = io->inp_x;
+    J.inp_y = io->inp_y;
+    J.inp_z = io->inp_z;
+    J.o = make_out(io);
+    J.prm = *prm;
+    J.queue = nullptr;
+    J.samples = samples_dev;
+    memset(&J.s, 0, sizeof(J.s));
+    J.s.n_cap = -1;
+}
+
+extern "C" {
+
+int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n,
+              const unsigned long long* n_dev, float s_len, float tol_coef, const float* cross_dir_h,
+              const float* curBx, const float* curBy, const float* curBz, int schedule,
+              unsigned long long* samples_dev, unsigned long long* queue_dev, qsl_stream_t stream) {
+    if (!field) return fail(QSL_ERR_INVALID, "field is null");
+    if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
+    if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
+    if (n == 0) return QSL_OK;  // also bounds a device count: nothing to write
+    if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
+    if (schedule != QSL_SCHED_QUEUE && schedule != QSL_SCHED_STATIC)
+        return fail(QSL_ERR_INVALID, "bad schedule %d", schedule);
+    if (schedule == QSL_SCHED_STATIC && n_dev) return fail(QSL_ERR_INVALID, "static schedule needs a host count");
+    const bool twist = curBx != nullptr;
+    if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
+    if (field->layout != LAYOUT_SOA && prm->arith == QSL_ARITH_EXACT)
+        return fail(QSL_ERR_INVALID, "exact arithmetic needs the SoA layout");
+    const float cd[3] = {cross_dir_h ? cross_dir_h[0] : 0.f, cross_dir_h ? cross_dir_h[1] : 0.f,
+                         cross_dir_h ? cross_dir_h[2] : 1.f};
+    cudaStream_t st = (cudaStream_t)stream;
+    auto scal = [&](TraceScalars& s) {
+        s.s_len = s_len;
+        s.tol_coef = tol_coef;
+        s.n = n;
+        s.n_dev = n_dev;
+        s.n_cap = n_dev ? n : -1;  // a device count never exceeds the outputs' length n
+        s.cross[0] = cd[0]; s.cross[1] = cd[1]; s.cross[2] = cd[2];
+        s.twist_on = twist ? 1 : 0;
+    };
+    const FieldSoA cur{curBx, curBy, curBz, field->d};
+    if (field->layout == LAYOUT_SOA) {
+        TraceJob<FieldSoA> J;
+        J.f = FieldSoA{field->bx, field->by, field->bz, field->d};
+        fill_common(J, io, prm, samples_dev);
+        J.cur = cur;
+        scal(J.s);
+        return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
+    } else if (field->layout == LAYOUT_F4) {
+        TraceJob<FieldF4> J;
+        J.f = FieldF4{field->f4, field->d};
+        fill_common(J, io, prm, samples_dev);
+        J.cur = cur;
+        scal(J.s);
+        return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
+    } else {
+        TraceJob<FieldH4B> J;
+        J.f = FieldH4B{field->bricks, field->scale, field->d, field->nbx, field->nby};
+        fill_common(J, io, prm, samples_dev);
+        J.cur = cur;
+        scal(J.s);
+        return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
+    }
+}
+
+// Drop-in entry: the reference kernel's argument list (TraceBlineAdaptive.cu:
+// 429-437), scalars by device pointer.  The field is read in place (SoA).
+int qsl_trace_all_bline(int integrator, int arith, const float* Bx, const float* By, const float* Bz,
+                        const int* BshapeN, const float* curB_x, const float* curB_y, const float* curB_z,
+                        double* twist, const bool* curB_flag, const float* inp_x, const float* inp_y,
+                        const float* inp_z, const float* inp_cross_dir, float* start_x, float* start_y,
+                        float* start_z, int* flag_start, float* end_x, float* end_y, float* end_z, int* flag_end,
+                        float* B_this_x, float* B_this_y, float* B_this_z, int* B_flag, float* B_start_x,
+                        float* B_start_y, float* B_start_z, float* B_end_x, float* B_end_y, float* B_end_z,
+                        const float* s_len, const unsigned long long* N, double* LineLen, const float* tol_coef,
+                        int64_t capacity, qsl_stream_t stream) {
+    if (capacity == 0) return QSL_OK;  // nothing can be written
+    if (!Bx || !By || !Bz || !BshapeN || !inp_cross_dir || !s_len || !N)
+        return fail(QSL_ERR_INVALID, "null required pointer");
+    if (integrator == QSL_RKF45 && !tol_coef) return fail(QSL_ERR_INVALID, "RKF45 needs tol_coef");
+    if (arith != QSL_ARITH_EXACT && arith != QSL_ARITH_FAST) return fail(QSL_ERR_INVALID, "bad arith %d", arith);
+    qsl_trace_params prm;
+    if (integrator == QSL_RK4) qsl_params_reference_rk4(&prm);
+    else if (integrator == QSL_RKF45) qsl_params_reference_rkf45(&prm);
+    else return fail(QSL_ERR_INVALID, "bad integrator %d", integrator);
+    prm.arith = arith;
+    qsl_trace_io io{inp_x, inp_y, inp_z, start_x, start_y, start_z, flag_start, end_x, end_y, end_z, flag_end,
+                    B_this_x, B_this_y, B_this_z, B_flag, B_start_x, B_start_y, B_start_z, B_end_x, B_end_y,
+                    B_end_z, LineLen, twist};
+    if (!io_ok(&io)) return fail(QSL_ERR_INVALID, "null pointer in outputs");
+    // the twist code runs only when *curB_flag is true on the device
+    const bool twist_possible = curB_flag && curB_x && curB_y && curB_z && twist;
+    TraceJob<FieldSoA> J;
+    J.f = FieldSoA{Bx, By, Bz, Dims{2, 2, 2}};
+    fill_common(J, &io, &prm, nullptr);
+    J.shape_dev = BshapeN;
+    J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
+    J.s.s_len_dev = s_len;
+    J.s.tol_coef_dev = integrator == QSL_RKF45 ? tol_coef : nullptr;
+    J.s.tol_coef = 1.f;
+    J.s.n_dev = N;
+    J.s.cross_dev = inp_cross_dir;
+    J.s.twist_flag_dev = twist_possible ? curB_flag : nullptr;
+    J.s.twist_on = 0;
+    J.s.n_cap = capacity < 0 ? -1 : capacity;
+    return run_trace(J, arith, twist_possible, QSL_SCHED_QUEUE, 0, nullptr, (cudaStream_t)stream);
+}
+
+int qsl_trace_all_bline_rkf45(const float* Bx, const float* By, const float* Bz, const int* BshapeN,
+                              const float* curB_x, const float* curB_y, const float* curB_z, double* twist,
+                              const bool* curB_flag, const float* inp_x, const float* inp_y, const float* inp_z,
+                              const float* inp_cross_dir, float* start_x, float* start_y, float* start_z,
+                              int* flag_start, float* end_x, float* end_y, float* end_z, int* flag_end,
+                              float* B_this_x, float* B_this_y, float* B_this_z, int* B_flag, float* B_start_x,
+                              float* B_start_y, float* B_start_z, float* B_end_x, float* B_end_y, float* B_end_z,
+                              const float* s_len, const unsigned long long* N, double* LineLen,
+                              const float* tol_coef, qsl_stream_t stream) {
+    return qsl_trace_all_bline(QSL_RKF45, QSL_ARITH_EXACT, Bx, By, Bz, BshapeN, curB_x, curB_y, curB_z, twist,
+                               curB_flag, inp_x, inp_y, inp_z, inp_cross_dir, start_x, start_y, start_z, flag_start,
+                               end_x, end_y, end_z, flag_end, B_this_x, B_this_y, B_this_z, B_flag, B_start_x,
+                               B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len, N, LineLen, tol_coef, -1, stream);
+}
+
+int qsl_trace_all_bline_rk4(const float* Bx, const float* By, const float* Bz, const int* BshapeN,
+                            const float* curB_x, const float* curB_y, const float* curB_z, double* twist,
+                            const bool* curB_flag, const float* inp_x, const float* inp_y, const float* inp_z,
+                            const float* inp_cross_dir, float* start_x, float* start_y, float* start_z,
+                            int* flag_start, float* end_x, float* end_y, float* end_z, int* flag_end,
+                            float* B_this_x, float* B_this_y, float* B_this_z, int* B_flag, float* B_start_x,
+                            float* B_start_y, float* B_start_z, float* B_end_x, float* B_end_y, float* B_end_z,
+                            const float* s_len, const unsigned long long* N, double* LineLen, qsl_stream_t stream) {
+    return qsl_trace_all_bline(QSL_RK4, QSL_ARITH_EXACT, Bx, By, Bz, BshapeN, curB_x, curB_y, curB_z, twist,
+                               curB_flag, inp_x, inp_y, inp_z, inp_cross_dir, start_x, start_y, start_z, flag_start,
+                               end_x, end_y, end_z, flag_end, B_this_x, B_this_y, B_this_z, B_flag, B_start_x,
+                               B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len, N, LineLen, nullptr, -1, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Q assembly
+// ---------------------------------------------------------------------------
+int qsl_qcalc_plane(const float* x_end, const float* y_end, const float* z_end, const int* flag_end,
+                    const float* x_start, const float* y_start, const float* z_start, const int* flag_start,
+                    const float* Bz_in, const float* Bz_out, const float* Bx_0, const float* By_0,
+                    const float* Bz_0, int n0, int n1, int64_t nplanes, double jac_scale,
+                    const float* cross_dir_h, float* Q32, double* Q64, qsl_stream_t stream) {
+    if (!x_end || !y_end || !z_end || !flag_end || !x_start || !y_start || !z_start || !flag_start || !Bz_in ||
+        !Bz_out || !Bx_0 || !By_0 || !Bz_0 || !cross_dir_h)
+        return fail(QSL_ERR_INVALID, "null input");
+    if ((Q32 == nullptr) == (Q64 == nullptr)) return fail(QSL_ERR_INVALID, "exactly one of Q32 / Q64");
+    if (n0 < 3 || n1 < 3 || nplanes < 0) return fail(QSL_ERR_INVALID, "plane must be at least 3 x 3");
+    QPlaneArgs a;
+    a.xe = x_end; a.ye = y_end; a.ze = z_end; a.fe = flag_end;
+    a.xs = x_start; a.ys = y_start; a.zs = z_start; a.fs = flag_start;
+    a.bz_in = Bz_in; a.bz_out = Bz_out; a.bx0 = Bx_0; a.by0 = By_0; a.bz0 = Bz_0;
+    a.cx = cross_dir_h[0]; a.cy = cross_dir_h[1]; a.cz = cross_dir_h[2];
+    a.n0 = n0; a.n1 = n1; a.nplanes = nplanes;
+    a.k32 = (float)jac_scale;
+    a.k64 = jac_scale;
+    a.q32 = Q32;
+    a.q64 = Q64;
+    QSL_CHECK_CUDA(launch_qcalc_plane(a, Q64 != nullptr, (cudaStream_t)stream), "qcalc_plane");
+    return QSL_OK;
+}
+
+int64_t qsl_cook_workspace_bytes(int64_t n) {
+    const long long t = cook_tiles(n);
+    return (int64_t)(t * (sizeof(int) + sizeof(long long)) + 64);
+}
+
+int qsl_cook_pseudo_line(const int* B_flag, const float* x_start, const float* y_start, const float* z_start,
+                         const int* flag_start, const float* Bz_in, const float* Bz_out, int64_t n, int n0, int n1,
+                         int interior_only, float stride, float* cut_x, float* cut_y, float* cut_z,
+                         float* Bz0_start, float* Bz0_end, int64_t* pix, unsigned long long* count_dev,
+                         void* workspace, int64_t workspace_bytes, qsl_stream_t stream) {
+    if (!B_flag || !x_start || !y_start || !z_start || !flag_start || !Bz_in || !Bz_out || !cut_x || !cut_y ||
+        !cut_z || !Bz0_start || !Bz0_end || !count_dev || !workspace)
+        return fail(QSL_ERR_INVALID, "null pointer");
+    if (n < 0) return fail(QSL_ERR_INVALID, "negative n");
+    if (interior_only && (n0 < 1 || n1 < 1 || n % ((int64_t)n0 * n1) != 0))
+        return fail(QSL_ERR_INVALID, "interior_only needs n a multiple of n0*n1");
+    if (workspace_bytes < qsl_cook_workspace_bytes(n)) return fail(QSL_ERR_INVALID, "workspace too small");
+    const long long tiles = cook_tiles(n);
+    long long* tile_off = (long long*)workspace;
+    int* tile_count = (int*)(tile_off + tiles);
+    CookArgs a;
+    a.bflag = B_flag; a.xs = x_start; a.ys = y_start; a.zs = z_start; a.fs = flag_start;
+    a.bz_in = Bz_in; a.bz_out = Bz_out; a.n = n; a.n0 = n0; a.n1 = n1; a.interior_only = interior_only;
+    a.stride = stride; a.tile_off = tile_off;
+    a.cx = cut_x; a.cy = cut_y; a.cz = cut_z; a.bz0s = Bz0_start; a.bz0e = Bz0_end; a.pix = (long long*)pix;
+    QSL_CHECK_CUDA(launch_cook(a, tile_count, tile_off, count_dev, (cudaStream_t)stream), "cook_pseudo_line");
+    return QSL_OK;
+}
+
+int qsl_qcut(const float* start_x, const float* start_y, const float* start_z, const int* flag_start,
+             const float* end_x, const float* end_y, const float* end_z, const int* flag_end,
+             const float* Bz0_start, const float* Bz0_end, int64_t count, const unsigned long long* count_dev,
+             int64_t max_count, double jac_scale, float* Qcut32, double* Qcut64, qsl_stream_t stream) {
+    if (!start_x || !start_y || !start_z || !flag_start || !end_x || !end_y || !end_z || !flag_end ||
+        !Bz0_start || !Bz0_end)
+        return fail(QSL_ERR_INVALID, "null input");
+    if ((Qcut32 == nullptr) == (Qcut64 == nullptr)) return fail(QSL_ERR_INVALID, "exactly one of Qcut32 / Qcut64");
+    QcutArgs a;
+    a.xs = start_x; a.ys = start_y; a.zs = start_z; a.fs = flag_start;
+    a.xe = end_x; a.ye = end_y; a.ze = end_z; a.fe = flag_end;
+    a.bz0s = Bz0_start; a.bz0e = Bz0_end;
+    a.count_dev = count_dev; a.count = count;
+    a.k32 = (float)jac_scale; a.k64 = jac_scale;
+    a.q32 = Qcut32; a.q64 = Qcut64;
+    const long long mc = count_dev ? max_count : count;
+    QSL_CHECK_CUDA(launch_qcut(a, Qcut64 != nullptr, mc, (cudaStream_t)stream), "qcut");
+    return QSL_OK;
+}
+
+int qsl_qmerge(const int64_t* pix, const float* Qcut32, const double* Qcut64, int64_t count,
+               const unsigned long long* count_dev, int64_t max_count, int n0, int n1, float* Qfinal32,
+               double* Qfinal64, qsl_stream_t stream) {
+    if (!pix) return fail(QSL_ERR_INVALID, "null pix");
+    const long long mc = count_dev ? max_count : count;
+    if (Qcut32 && Qfinal32) {
+        QSL_CHECK_CUDA(launch_qmerge_f32((const long long*)pix, Qcut32, count_dev, count, mc, n0, n1, Qfinal32,
+                                         (cudaStream_t)stream), "qmerge");
+    } else if (Qcut64 && Qfinal64) {
+        QSL_CHECK_CUDA(launch_qmerge_f64((const long long*)pix, Qcut64, count_dev, count, mc, n0, n1, Qfinal64,
+                                         (cudaStream_t)stream), "qmerge");
+    } else {
+        return fail(QSL_ERR_INVALID, "Qcut and Qfinal must both be float or both double");
+    }
+    return QSL_OK;
+}
+
+int qsl_device_sm_count(int* sms) {
+    int dev = 0;
+    QSL_CHECK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    QSL_CHECK_CUDA(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
+    return QSL_OK;
+}
+
+}  // extern "C"

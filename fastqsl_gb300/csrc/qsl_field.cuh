@@ -1,0 +1,248 @@
+// Field stores and trilinear sampling for the GB300 tracer.
+//
+// Three layouts of the same (nx, ny, nz) node grid:
+//   FieldSoA  — the caller's three float32 arrays, x fastest (the reference
+//               layout, fastqslpy/cu/TraceBlineAdaptive.cu:36-39); one corner
+//               costs three 4-byte gathers.
+//   FieldF4   — interleaved float4 (Bx, By, Bz, 0) per node; one corner is one
+//               16-byte load.
+//   FieldH4B  — 8x8x8-cell bricks with a one-node apron on the + side (9^3
+//               nodes), each node four fp16 (Bx, By, Bz, 0) scaled by a
+//               per-brick float; one corner is one 8-byte load and a whole
+//               trilinear stencil never leaves its brick.
+//
+// Sampling comes in two arithmetics:
+//   exact — the reference's rounding sequence (weights formed in double and
+//           narrowed, IEEE divide and sqrt).  Only instantiated in translation
+//           units compiled with -fmad=false, so no multiply-add is fused.
+//   fast  — float weights, fused multiply-add, rsqrt normalisation.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qsl {
+
+// ---------------------------------------------------------------------------
+// small vector helpers (own code; semantics of plain per-component float ops)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float3 v3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float norm(float3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ float comp(float3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }
+__device__ __forceinline__ float fcomp(const float* a, int d) { return a[d]; }
+
+struct Dims {
+    int nx, ny, nz;
+    __device__ __forceinline__ int n(int d) const { return d == 0 ? nx : (d == 1 ? ny : nz); }
+};
+
+// ---------------------------------------------------------------------------
+// Field stores.  corners() returns the 8 node vectors of cell (ix, iy, iz) in
+// corner order q = (dx<<2)|(dy<<1)|dz, and the multiplier that turns them into
+// field units (1 except for fp16 bricks).
+// ---------------------------------------------------------------------------
+struct FieldSoA {
+    const float* bx;
+    const float* by;
+    const float* bz;
+    Dims d;
+    __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
+        const int64_t sx = 1, sy = d.nx, sz = (int64_t)d.nx * d.ny;
+        const int64_t base = ix + sy * iy + sz * iz;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int64_t o = base + ((q >> 2) & 1) * sx + ((q >> 1) & 1) * sy + (q & 1) * sz;
+            c[q] = v3(__ldg(bx + o), __ldg(by + o), __ldg(bz + o));
+        }
+        return 1.0f;
+    }
+    __device__ __forceinline__ float scalar(int m, int64_t o) const {
+        return __ldg((m == 0 ? bx : (m == 1 ? by : bz)) + o);
+    }
+};
+
+struct FieldF4 {
+    const float4* b;
+    Dims d;
+    __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
+        const int64_t sy = d.nx, sz = (int64_t)d.nx * d.ny;
+        const int64_t base = ix + sy * iy + sz * iz;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int64_t o = base + ((q >> 2) & 1) + ((q >> 1) & 1) * sy + (q & 1) * sz;
+            const float4 v = __ldg(b + o);
+            c[q] = v3(v.x, v.y, v.z);
+        }
+        return 1.0f;
+    }
+};
+
+// fp16 brick store: brick (bi, bj, bk) holds nodes [8bi, 8bi+8] x [8bj, 8bj+8]
+// x [8bk, 8bk+8] (clamped at the far faces), node (a, b, c) of a brick at
+// uint2 offset a + 9*(b + 9*c); brick stride BRICK_U2 uint2 (5832 B padded to
+// 5888 B, a multiple of 128 B).
+constexpr int BRICK_CELLS = 8;
+constexpr int BRICK_NODES = 9;
+constexpr int BRICK_U2 = 736;  // 9*9*9 = 729 nodes, padded
+struct FieldH4B {
+    const uint2* bricks;
+    const float* scale;  // per brick
+    Dims d;
+    int nbx, nby;        // bricks along x and y
+    __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
+        const int bi = ix >> 3, bj = iy >> 3, bk = iz >> 3;
+        const int64_t brick = bi + (int64_t)nbx * (bj + (int64_t)nby * bk);
+        const uint2* bp = bricks + brick * BRICK_U2;
+        const int a = ix & 7, b = iy & 7, cc = iz & 7;
+        const int base = a + BRICK_NODES * (b + BRICK_NODES * cc);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int o = base + ((q >> 2) & 1) + ((q >> 1) & 1) * BRICK_NODES + (q & 1) * (BRICK_NODES * BRICK_NODES);
+            const uint2 u = __ldg(bp + o);
+            const float2 xy = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+            const float z = __half2float(__ushort_as_half((unsigned short)(u.y & 0xffffu)));
+            c[q] = v3(xy.x, xy.y, z);
+        }
+        return __ldg(scale + brick);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Cell location with the reference's face pinning (Interp3dxyzn,
+// TraceBlineAdaptive.cu:112-131): a coordinate <= 0 uses cell 0 with fraction
+// 0, >= n-1 uses cell n-2 with fraction 1; NaN indexes cell 0.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void locate(float c, int n, int& i, float& r) {
+    r = c - floorf(c);
+    i = __float2int_rd(c);
+    if (c <= 0.f) { r = 0.f; i = 0; }
+    if (c >= (float)(n - 1)) { r = 1.f; i = n - 2; }
+}
+
+// exact: reference rounding of the corner weights (double products narrowed
+// to float; the bare-fraction products rx*ry are float products).
+__device__ __forceinline__ void weights_exact(float rx, float ry, float rz, float w[8]) {
+    const double ox = 1.0 - (double)rx, oy = 1.0 - (double)ry, oz = 1.0 - (double)rz;
+    w[0] = (float)(ox * oy * oz);
+    w[1] = (float)(ox * oy * (double)rz);
+    w[2] = (float)(ox * (double)ry * oz);
+    w[3] = (float)(ox * (double)ry * (double)rz);
+    w[4] = (float)((double)rx * oy * oz);
+    w[5] = (float)((double)rx * oy * (double)rz);
+    const float rxy = rx * ry;
+    w[6] = (float)((double)rxy * oz);
+    w[7] = rxy * rz;
+}
+
+__device__ __forceinline__ void weights_fast(float rx, float ry, float rz, float w[8]) {
+    const float ox = 1.f - rx, oy = 1.f - ry, oz = 1.f - rz;
+    const float a0 = ox * oy, a1 = ox * ry, a2 = rx * oy, a3 = rx * ry;
+    w[0] = a0 * oz; w[1] = a0 * rz; w[2] = a1 * oz; w[3] = a1 * rz;
+    w[4] = a2 * oz; w[5] = a2 * rz; w[6] = a3 * oz; w[7] = a3 * rz;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float3 blend(const float3 c[8], const float w[8]) {
+    float x = c[0].x * w[0], y = c[0].y * w[0], z = c[0].z * w[0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+        if (EXACT) {
+            x = x + c[q].x * w[q];
+            y = y + c[q].y * w[q];
+            z = z + c[q].z * w[q];
+        } else {
+            x = fmaf(c[q].x, w[q], x);
+            y = fmaf(c[q].y, w[q], y);
+            z = fmaf(c[q].z, w[q], z);
+        }
+    }
+    return v3(x, y, z);
+}
+
+// Trilinear B at p; unit = true returns B/|B|.  Reference: Interp3dxyzn,
+// TraceBlineAdaptive.cu:95-201.
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 sample(const F& f, float3 p, bool unit) {
+    int ix, iy, iz;
+    float rx, ry, rz;
+    locate(p.x, f.d.nx, ix, rx);
+    locate(p.y, f.d.ny, iy, ry);
+    locate(p.z, f.d.nz, iz, rz);
+    float w[8];
+    if (EXACT) weights_exact(rx, ry, rz, w);
+    else weights_fast(rx, ry, rz, w);
+    float3 c[8];
+    const float s = f.corners(ix, iy, iz, c);
+    float3 r = blend<EXACT>(c, w);
+    if (unit) {
+        if (EXACT) {
+            const float nb = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+            r = v3(r.x / nb, r.y / nb, r.z / nb);
+        } else {
+            const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+            r = v3(r.x * inv, r.y * inv, r.z * inv);
+        }
+    } else if (s != 1.0f) {
+        r = v3(r.x * s, r.y * s, r.z * s);
+    }
+    return r;
+}
+
+// Position clamped into [1e-4, n-1-1e-4] as the scalar interpolator of the
+// reference does (Interp3d, TraceBlineAdaptive.cu:57-62).
+__device__ __forceinline__ float clamp_inside(float c, int n) {
+    c = (c > 0.f) ? c : (float)0.0001;
+    c = (c < (float)(n - 1)) ? c : (float)((double)((float)n - 1.f) - 0.0001);
+    return c;
+}
+
+// Exact scalar interpolation of one component (Interp3d, :47-93): each term is
+// corner*f1*f2*f3 evaluated left to right, bare float fractions staying float
+// products until a double factor appears, summed in double.
+__device__ __forceinline__ float sample_scalar_exact(const FieldSoA& f, int m, float x, float y, float z) {
+    x = clamp_inside(x, f.d.nx);
+    y = clamp_inside(y, f.d.ny);
+    z = clamp_inside(z, f.d.nz);
+    const float rx = x - floorf(x), ry = y - floorf(y), rz = z - floorf(z);
+    const int ix = __float2int_rd(x), iy = __float2int_rd(y), iz = __float2int_rd(z);
+    const double ox = 1.0 - (double)rx, oy = 1.0 - (double)ry, oz = 1.0 - (double)rz;
+    const int64_t sy = f.d.nx, sz = (int64_t)f.d.nx * f.d.ny;
+    const int64_t b = ix + sy * iy + sz * iz;
+    float a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = f.scalar(m, b + ((q >> 2) & 1) + ((q >> 1) & 1) * sy + (q & 1) * sz);
+    double s = (double)a[0] * ox * oy * oz;
+    s = s + (double)a[1] * ox * oy * (double)rz;
+    s = s + (double)a[2] * ox * (double)ry * oz;
+    s = s + (double)a[3] * ox * (double)ry * (double)rz;
+    s = s + (double)(a[4] * rx) * oy * oz;
+    s = s + (double)(a[5] * rx) * oy * (double)rz;
+    s = s + (double)((a[6] * rx) * ry) * oz;
+    s = s + (double)(((a[7] * rx) * ry) * rz);
+    return (float)s;
+}
+
+// B (all three components) at a clamped position; exact mode evaluates each
+// component like the reference's scalar interpolator, fast mode takes one
+// vector sample at the clamped point.
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 sample_endpoint(const F& f, float3 p);
+
+template <>
+__device__ __forceinline__ float3 sample_endpoint<true, FieldSoA>(const FieldSoA& f, float3 p) {
+    return v3(sample_scalar_exact(f, 0, p.x, p.y, p.z), sample_scalar_exact(f, 1, p.x, p.y, p.z),
+              sample_scalar_exact(f, 2, p.x, p.y, p.z));
+}
+
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 sample_endpoint(const F& f, float3 p) {
+    const float3 q = v3(clamp_inside(p.x, f.d.nx), clamp_inside(p.y, f.d.ny), clamp_inside(p.z, f.d.nz));
+    return sample<false>(f, q, false);
+}
+
+}  // namespace qsl

@@ -1,0 +1,36 @@
+// Internal launch interface between the C ABI (capi.cu) and the kernel
+// translation units.  Not installed; the public surface is
+// include/fastqsl_gb300.h.
+#pragma once
+#include <cuda_runtime.h>
+#include "qsl_trace.cuh"
+
+namespace qsl {
+
+enum Layout { LAYOUT_SOA = 0, LAYOUT_F4 = 1, LAYOUT_H4B = 2 };
+enum Schedule { SCHED_QUEUE = 0, SCHED_STATIC = 1 };
+
+constexpr int kTraceBlock = 128;
+
+// Blocks of `kernel` that fit on one SM at kTraceBlock threads, times the SM
+// count: the persistent grid.
+int persistent_grid(const void* kernel, int block, size_t smem = 0);
+
+// trace_exact.cu (compiled with -fmad=false)
+cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
+                               cudaStream_t st);
+
+// trace_fast.cu
+cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st);
+cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
+                                 cudaStream_t st);
+cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st);
+
+// field_store.cu
+cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);
+cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
+                            uint2* bricks, float* scale, cudaStream_t st);
+
+}  // namespace qsl

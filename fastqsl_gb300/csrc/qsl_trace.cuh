@@ -1,0 +1,408 @@
+// Field-line tracer kernels (RK4 / RKF45), templated on the field store and
+// the arithmetic.  Semantics per seed follow the reference's TraceAllBline
+// (fastqslpy/cu/TraceBlineAdaptive.cu:429-510, fastqslpy/cu/TraceBline.cu:
+// 383-464): forward trace -> end footpoint, backward trace -> start footpoint,
+// B at both footpoints and at the seed, B_flag, line length, optional twist.
+//
+// Scheduling: a persistent grid (a multiple of the SM count) in which every
+// lane owns one line at a time and, the moment its line finishes, takes the
+// next one from a device work counter (one warp-aggregated atomic per refill).
+// Lines whose lengths differ by orders of magnitude (RKF45 near nulls and
+// separators) therefore never hold a warp's other lanes idle.  A static mode
+// (one line per thread, no counter) is the plain baseline.
+#pragma once
+#include "qsl_field.cuh"
+#include "../../include/fastqsl_gb300.h"
+
+namespace qsl {
+
+constexpr double kRefPi = 3.14159265;  // the reference's M_PI (TraceBlineAdaptive.cu:10)
+
+struct TraceOut {
+    float *start_x, *start_y, *start_z;
+    int* flag_start;
+    float *end_x, *end_y, *end_z;
+    int* flag_end;
+    float *bthis_x, *bthis_y, *bthis_z;
+    int* b_flag;
+    float *bstart_x, *bstart_y, *bstart_z;
+    float *bend_x, *bend_y, *bend_z;
+    double* line_len;
+    double* twist;
+};
+
+// Scalars the reference passes as one-element device arrays are read from
+// device memory when the *_dev pointer is set, else taken by value.
+struct TraceScalars {
+    const float* s_len_dev;
+    const float* tol_coef_dev;
+    const unsigned long long* n_dev;
+    const float* cross_dev;
+    const bool* twist_flag_dev;
+    long long n_cap;  // >= 0: lines beyond this index are never touched (array capacity)
+    float s_len;
+    float tol_coef;
+    long long n;
+    float cross[3];
+    int twist_on;
+};
+
+template <class F>
+struct TraceJob {
+    F f;
+    const int* shape_dev;  // when set, the field dims are read from here (nx, ny, nz)
+    FieldSoA cur;  // current density for the twist integral
+    const float *inp_x, *inp_y, *inp_z;
+    TraceOut o;
+    TraceScalars s;
+    qsl_trace_params prm;
+    unsigned long long* queue;    // work counter, zero at launch; null = static
+    unsigned long long* samples;  // optional: total field samples
+};
+
+// Fehlberg 4(5) coefficients, stored to float as the reference does
+// (TraceBlineAdaptive.cu:224-235).
+struct Fehlberg {
+    static constexpr float a21 = (float)(1. / 4.);
+    static constexpr float a31 = (float)(3. / 32.), a32 = (float)(9. / 32.);
+    static constexpr float a41 = (float)(1932. / 2197.), a42 = (float)(-7200. / 2197.), a43 = (float)(7296. / 2197.);
+    static constexpr float a51 = (float)(439. / 216.), a52 = -8.f, a53 = (float)(3680. / 513.),
+                           a54 = (float)(-845. / 4104.);
+    static constexpr float a61 = (float)(-8. / 27.), a62 = 2.f, a63 = (float)(-3544. / 2565.),
+                           a64 = (float)(1859. / 4104.), a65 = (float)(-11. / 40.);
+    static constexpr float b1 = (float)(16. / 135.), b3 = (float)(6656. / 12825.), b4 = (float)(28561. / 56430.),
+                           b5 = (float)(-9. / 50.), b6 = (float)(2. / 55.);
+    static constexpr float e1 = (float)(1. / 360.), e3 = (float)(-128. / 4275.), e4 = (float)(-2197. / 75240.),
+                           e5 = (float)(1. / 50.), e6 = (float)(2. / 55.);
+};
+
+// One Fehlberg step (RKF45, TraceBlineAdaptive.cu:215-254): returns the
+// 5th-order increment (the reference adds it to P0 in one rounding) and the
+// error-estimate norm.
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, float& err, unsigned& ns) {
+    using C = Fehlberg;
+    const float3 k1 = h * sample<EXACT>(f, p, true);
+    const float3 k2 = h * sample<EXACT>(f, p + C::a21 * k1, true);
+    const float3 k3 = h * sample<EXACT>(f, p + (C::a31 * k1 + C::a32 * k2), true);
+    const float3 k4 = h * sample<EXACT>(f, p + ((C::a41 * k1 + C::a42 * k2) + C::a43 * k3), true);
+    const float3 k5 = h * sample<EXACT>(f, p + (((C::a51 * k1 + C::a52 * k2) + C::a53 * k3) + C::a54 * k4), true);
+    const float3 k6 =
+        h * sample<EXACT>(f, p + ((((C::a61 * k1 + C::a62 * k2) + C::a63 * k3) + C::a64 * k4) + C::a65 * k5), true);
+    const float3 e = (((C::e1 * k1 + C::e3 * k3) + C::e4 * k4) + C::e5 * k5) + C::e6 * k6;
+    err = norm(e);
+    ns += 6;
+    return (((C::b1 * k1 + C::b3 * k3) + C::b4 * k4) + C::b5 * k5) + C::b6 * k6;
+}
+
+// Classic RK4 on b (RK4, TraceBlineAdaptive.cu:259-267); returns the
+// increment.  The 1/6 factor is formed as (1./6.)*h in double and narrowed.
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 step_rk4(const F& f, float3 p, float h, unsigned& ns) {
+    const float3 k1 = sample<EXACT>(f, p, true);
+    const float3 k2 = sample<EXACT>(f, p + (h * k1) / 2.f, true);
+    const float3 k3 = sample<EXACT>(f, p + (h * k2) / 2.f, true);
+    const float3 k4 = sample<EXACT>(f, p + h * k3, true);
+    ns += 4;
+    const float c = EXACT ? (float)(1.0 / 6.0 * (double)h) : h * (1.f / 6.f);
+    return c * (((k1 + 2.f * k2) + 2.f * k3) + k4);
+}
+
+// RK4 in the face-normal coordinate, dx/dq = b / b_d over dq = h
+// (RK4_boundary, TraceBlineAdaptive.cu:286-307).
+template <bool EXACT, class F>
+__device__ __noinline__ float3 step_rk4_normal(const F& f, float3 p, float h, int d, unsigned& ns) {
+    float3 b = sample<EXACT>(f, p, true);
+    const float3 k1 = b / comp(b, d);
+    b = sample<EXACT>(f, p + (h * k1) / 2.f, true);
+    const float3 k2 = b / comp(b, d);
+    b = sample<EXACT>(f, p + (h * k2) / 2.f, true);
+    const float3 k3 = b / comp(b, d);
+    b = sample<EXACT>(f, p + h * k3, true);
+    const float3 k4 = b / comp(b, d);
+    ns += 4;
+    const float c = EXACT ? (float)(1.0 / 6.0 * (double)h) : h * (1.f / 6.f);
+    return p + c * (((k1 + 2.f * k2) + 2.f * k3) + k4);
+}
+
+// Boundary classification (checkFlag, TraceBlineAdaptive.cu:309-331).
+__device__ __forceinline__ int box_flag(const Dims& n, float3 p) {
+    const float X = (float)(n.nx - 1), Y = (float)(n.ny - 1), Z = (float)(n.nz - 1);
+    if ((p.x >= 0.f) & (p.y > 0.f) & (p.z >= 0.f) & (p.x <= X) & (p.y <= Y) & (p.z <= Z)) return 0;
+    int f = 42;
+    if ((p.x < 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x < X) & (p.y < Y) & (p.z < Z)) f = 1;
+    if ((p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x >= X) & (p.y < Y) & (p.z < Z)) f = 2;
+    if ((p.x >= 0.f) & (p.y < 0.f) & (p.z >= 0.f) & (p.x < X) & (p.y < Y) & (p.z < Z)) f = 3;
+    if ((p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x < X) & (p.y >= Y) & (p.z < Z)) f = 4;
+    if ((p.x >= 0.f) & (p.y >= 0.f) & (p.z < 0.f) & (p.x < X) & (p.y < Y) & (p.z < Z)) f = 5;
+    if ((p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x < X) & (p.y < Y) & (p.z >= Z)) f = 6;
+    return f;
+}
+
+// Per-lane state of one direction of one line.
+struct Lane {
+    float3 p;      // current point
+    float3 pc;     // Kahan compensation of p (fast arithmetic)
+    float h;       // current step
+    float tol;     // local error tolerance
+    double len;    // accumulated length
+    double tw;     // accumulated twist
+    int steps;     // accepted steps
+    int dir;       // +1 forward, -1 backward
+    long long line;
+    float3 out;    // footpoint of this direction when finished
+    int flag;
+};
+
+template <bool EXACT, class F>
+__device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lane& L, long long line, int dir,
+                                           float s_len, float tol_coef, const float3 nrm, unsigned& ns) {
+    L.line = line;
+    L.dir = dir;
+    L.p = v3(__ldg(J.inp_x + line), __ldg(J.inp_y + line), __ldg(J.inp_z + line));
+    L.pc = v3(0.f, 0.f, 0.f);
+    L.h = s_len;
+    L.len = 0.0;
+    L.tw = 0.0;
+    L.steps = 0;
+    L.flag = 0;
+    L.out = L.p;
+    L.tol = 0.f;
+    if (J.prm.integrator == QSL_RKF45) {
+        // tolerance law (TraceBlineAdaptive.cu:351-359)
+        const float3 b0 = sample<EXACT>(f, L.p, true);
+        ns += 1;
+        const float bn = fabsf(dot(b0, nrm));
+        float tol;
+        if (J.prm.tol_law == QSL_TOL_REFERENCE) {
+            if ((double)bn <= 0.05) tol = (float)(J.prm.tol / 8e3);
+            else tol = (float)(J.prm.tol * (double)powf(bn, 1.5f));
+        } else {
+            tol = (float)J.prm.tol;
+        }
+        L.tol = tol * tol_coef;
+    }
+}
+
+// One trial step of the current direction.  Returns true when the direction
+// is finished (left the box, or stopped by the length / step limit) with
+// L.out, L.flag, L.len, L.tw final.  Reference: TraceBlineAdap,
+// TraceBlineAdaptive.cu:361-421 and TraceBline, TraceBline.cu:320-373.
+template <bool EXACT, bool TWIST, class F>
+__device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane& L, double len_lim, bool tw_on,
+                                          unsigned& ns) {
+    const qsl_trace_params& pr = J.prm;
+    if (!((L.len < len_lim) & (L.steps < pr.max_steps))) {
+        L.out = L.p;
+        L.flag = 0;
+        return true;
+    }
+    const float hd = L.h * (float)L.dir;
+    float3 inc;
+    if (pr.integrator == QSL_RKF45) {
+        float err;
+        inc = step_rkf45<EXACT>(f, L.p, hd, err, ns);
+        float scale;
+        if (EXACT) {
+            scale = powf((float)((double)(L.tol / err) / 11.09), 0.2f);
+            if ((double)scale < 0.618) {
+                L.h = (float)((double)L.h * pr.reject_factor);
+                return false;
+            }
+        } else {
+            scale = powf(L.tol / err * (float)(1.0 / 11.09), 0.2f);
+            if (scale < 0.618f) {
+                L.h = L.h * (float)pr.reject_factor;
+                return false;
+            }
+        }
+        float h = L.h * scale;
+        if ((double)h > pr.h_max) h = (float)pr.h_max;
+        if ((double)h < pr.h_min) h = (float)pr.h_min;
+        L.h = h;
+    } else {
+        inc = step_rk4<EXACT>(f, L.p, hd, ns);
+    }
+    float3 p2;
+    if (EXACT) {
+        p2 = L.p + inc;
+    } else {
+        // Kahan-compensated position update: the rounding lost in p + inc is
+        // carried into the next step, so long lines of short steps do not
+        // drift by accumulated float rounding.
+        const float3 y = inc - L.pc;
+        p2 = L.p + y;
+        L.pc = (p2 - L.p) - y;
+    }
+    const float dl = norm(L.p - p2);
+    L.len = L.len + (double)dl;
+    float td = 0.f;
+    float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
+    if (TWIST && tw_on) {
+        j1 = sample<EXACT>(J.cur, L.p, false);
+        b1 = sample<EXACT>(f, L.p, false);
+        ns += 2;
+        td = dot(j1, b1) / dot(b1, b1);
+        L.tw = L.tw + (double)td / 4.0 / kRefPi * (double)dl;
+    }
+    const int flag = box_flag(f.d, p2);
+    if (flag > 0) {
+        L.len = L.len - (double)dl;
+        if (TWIST && tw_on) L.tw = L.tw - (double)td / 4.0 / kRefPi * (double)dl;
+        if (flag <= 6) {
+            const int d = (flag - 1) / 2;
+            const float q1 = comp(L.p, d), q2 = comp(p2, d);
+            float qmid = q1;
+            if ((double)fabsf(q1 - q2) > 1e-3) {
+                qmid = (flag % 2 == 1) ? 0.f : (float)f.d.n(d);
+                const float3 u1 = sample<EXACT>(f, L.p, true);
+                const float3 u2 = sample<EXACT>(f, p2, true);
+                ns += 2;
+                if (((double)fabsf(comp(u1, d)) < 0.2) | ((double)fabsf(comp(u2, d)) < 0.2)) {
+                    L.out.x = (L.p.x * (q2 - qmid) + p2.x * (qmid - q1)) / (q2 - q1);
+                    L.out.y = (L.p.y * (q2 - qmid) + p2.y * (qmid - q1)) / (q2 - q1);
+                    L.out.z = (L.p.z * (q2 - qmid) + p2.z * (qmid - q1)) / (q2 - q1);
+                } else {
+                    L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d, ns);
+                }
+                L.len = L.len + (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(u1, d)));
+                b1 = u1;
+            } else {
+                L.out = L.p;
+            }
+            if (TWIST && tw_on && pr.boundary_twist) {
+                L.tw = L.tw + (double)(dot(j1, b1) / dot(b1, b1)) / 4.0 / kRefPi * (double)fabsf(qmid - q1) /
+                                  (1e-4 + (double)fabsf(comp(b1, d)));
+            }
+        } else {
+            L.out = p2;
+        }
+        L.flag = flag;
+        L.p = p2;
+        L.steps++;
+        return true;
+    }
+    L.p = p2;
+    L.steps++;
+    return false;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// The tracer kernel.  QUEUE = true: persistent grid with per-lane refill from
+// J.queue; false: line = global thread index + k * total threads.  TWIST
+// compiles the twist integral in; it runs when the runtime flag is set.
+template <bool EXACT, bool TWIST, bool QUEUE, class F>
+__device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
+    F f = J.f;
+    if (J.shape_dev) {
+        f.d.nx = __ldg(J.shape_dev);
+        f.d.ny = __ldg(J.shape_dev + 1);
+        f.d.nz = __ldg(J.shape_dev + 2);
+    }
+    const float s_len = J.s.s_len_dev ? __ldg(J.s.s_len_dev) : J.s.s_len;
+    const float tol_coef = J.s.tol_coef_dev ? __ldg(J.s.tol_coef_dev) : J.s.tol_coef;
+    long long n = J.s.n_dev ? (long long)__ldg(J.s.n_dev) : J.s.n;
+    if (J.s.n_cap >= 0 && n > J.s.n_cap) n = J.s.n_cap;
+    const float3 nrm = J.s.cross_dev ? v3(__ldg(J.s.cross_dev), __ldg(J.s.cross_dev + 1), __ldg(J.s.cross_dev + 2))
+                                     : v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
+    const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
+    const double len_lim = J.prm.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz);
+    unsigned ns = 0;
+    unsigned long long ns_total = 0;
+    const int lane_id = threadIdx.x & 31;
+
+    Lane L;
+    bool active = false;
+    bool drained = false;
+    long long next_static = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // forward-direction results, kept until the line's backward trace ends
+    float3 end_pt = v3(0.f, 0.f, 0.f);
+    double len_fwd = 0.0, tw_fwd = 0.0;
+    int flag_fwd = 0;
+
+    while (true) {
+        // ---- give lanes without a line the next ones ----
+        if (QUEUE) {
+            const bool need = !active && !drained;
+            const unsigned m = __ballot_sync(0xffffffffu, need);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                unsigned long long base = 0;
+                if (lane_id == leader) base = atomicAdd(J.queue, (unsigned long long)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (need) {
+                    const long long line = (long long)base + __popc(m & lanemask_lt());
+                    if (line < n) {
+                        lane_begin<EXACT>(f, J, L, line, +1, s_len, tol_coef, nrm, ns);
+                        active = true;
+                    } else {
+                        drained = true;
+                    }
+                }
+            }
+            if (!__any_sync(0xffffffffu, active)) break;
+            if (!active) continue;
+        } else {
+            if (!active) {
+                if (next_static >= n) break;
+                lane_begin<EXACT>(f, J, L, next_static, +1, s_len, tol_coef, nrm, ns);
+                next_static += stride;
+                active = true;
+            }
+        }
+
+        // ---- advance this lane's line by one trial step ----
+        if (lane_step<EXACT, TWIST>(f, J, L, len_lim, tw_on, ns)) {
+            const long long i = L.line;
+            if (L.dir > 0) {
+                end_pt = L.out;
+                len_fwd = L.len;
+                tw_fwd = L.tw;
+                flag_fwd = L.flag;
+                lane_begin<EXACT>(f, J, L, i, -1, s_len, tol_coef, nrm, ns);
+            } else {
+                const float3 pe = end_pt, ps = L.out;
+                const float3 be = sample_endpoint<EXACT>(f, pe);
+                const float3 bs = sample_endpoint<EXACT>(f, ps);
+                const float3 p0 = v3(__ldg(J.inp_x + i), __ldg(J.inp_y + i), __ldg(J.inp_z + i));
+                const float3 b0 = sample_endpoint<EXACT>(f, p0);
+                ns += 3;
+                const TraceOut& o = J.o;
+                o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
+                o.flag_end[i] = flag_fwd;
+                o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
+                o.start_x[i] = ps.x; o.start_y[i] = ps.y; o.start_z[i] = ps.z;
+                o.flag_start[i] = L.flag;
+                o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
+                o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
+                o.line_len[i] = len_fwd + L.len;
+                if (TWIST && tw_on) o.twist[i] = tw_fwd + L.tw;
+                // B nearly in the seed plane (TraceBlineAdaptive.cu:498-501)
+                const float bn = b0.x * nrm.x + b0.y * nrm.y + b0.z * nrm.z;
+                const float bm = sqrtf(b0.x * b0.x + b0.y * b0.y + b0.z * b0.z);
+                o.b_flag[i] = ((double)fabsf(bn) * 100. < (double)bm) ? 1 : 0;
+                active = false;
+            }
+        }
+        if (ns > (1u << 30)) {
+            ns_total += ns;
+            ns = 0;
+        }
+    }
+    if (J.samples) {
+        ns_total += ns;
+        // one atomic per warp (blocks are whole warps; every lane gets here)
+        __syncwarp();
+        unsigned long long v = ns_total;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane_id == 0) atomicAdd(J.samples, v);
+    }
+}
+
+}  // namespace qsl

@@ -1,0 +1,41 @@
+// Reference-parity tracer kernels.
+//
+// This translation unit is compiled with -fmad=false: no multiply and add are
+// fused, so each float expression rounds exactly where the reference's does
+// when built without contraction (the oracle's rule).  Together with the
+// double-precision corner weights and IEEE divide / sqrt of the exact
+// sampler, the results agree with the reference tracing routine bit for bit
+// except where powf differs by an ulp.
+#include "qsl_internal.h"
+
+namespace qsl {
+
+template <bool TWIST, bool QUEUE>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_exact(const TraceJob<FieldSoA> J) {
+    trace_kernel_body<true, TWIST, QUEUE>(J);
+}
+
+cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
+                               cudaStream_t st) {
+    const void* k;
+    if (sched == SCHED_QUEUE) k = twist ? (const void*)k_trace_exact<true, true> : (const void*)k_trace_exact<false, true>;
+    else k = twist ? (const void*)k_trace_exact<true, false> : (const void*)k_trace_exact<false, false>;
+    int grid;
+    if (sched == SCHED_QUEUE) {
+        grid = persistent_grid(k, kTraceBlock);
+    } else {
+        long long g = (n_host + kTraceBlock - 1) / kTraceBlock;
+        grid = (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
+    }
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    if (sched == SCHED_QUEUE) {
+        if (twist) k_trace_exact<true, true><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_exact<false, true><<<grid, kTraceBlock, 0, st>>>(J);
+    } else {
+        if (twist) k_trace_exact<true, false><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_exact<false, false><<<grid, kTraceBlock, 0, st>>>(J);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace qsl

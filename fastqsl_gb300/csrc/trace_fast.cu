@@ -1,0 +1,48 @@
+// FP32 tracer kernels with fused multiply-add: the plain SoA form (the
+// reference's field layout) and the interleaved-float4 and fp16-brick stores.
+#include "qsl_internal.h"
+
+namespace qsl {
+
+template <bool TWIST, bool QUEUE, class F>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_fast(const TraceJob<F> J) {
+    trace_kernel_body<false, TWIST, QUEUE>(J);
+}
+
+template <class F>
+static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
+    const bool q = sched == SCHED_QUEUE;
+    const void* k = q ? (twist ? (const void*)k_trace_fast<true, true, F> : (const void*)k_trace_fast<false, true, F>)
+                      : (twist ? (const void*)k_trace_fast<true, false, F> : (const void*)k_trace_fast<false, false, F>);
+    int grid;
+    if (q) {
+        grid = persistent_grid(k, kTraceBlock);
+    } else {
+        long long g = (n_host + kTraceBlock - 1) / kTraceBlock;
+        grid = (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
+    }
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    if (q) {
+        if (twist) k_trace_fast<true, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_fast<false, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+    } else {
+        if (twist) k_trace_fast<true, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_fast<false, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st) {
+    return launch_fast(J, twist, sched, n_host, st);
+}
+cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
+                                 cudaStream_t st) {
+    return launch_fast(J, twist, sched, n_host, st);
+}
+cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st) {
+    return launch_fast(J, twist, sched, n_host, st);
+}
+
+}  // namespace qsl

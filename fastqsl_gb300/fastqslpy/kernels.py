@@ -1,0 +1,74 @@
+"""Drop-in for fastqslpy/kernels.py.
+
+``compileTraceBlineAdaptive()`` / ``compileTraceBlineRK4()`` return a callable
+with ``cupy.RawKernel``'s call convention, ``k(grid, block, args)``, taking
+the reference kernel's argument tuple (TraceBlineAdaptive.cu:429-437, 35
+arguments; TraceBline.cu:383-391, 34 arguments; extra trailing arguments are
+ignored as the RK4 kernel ignores the notebooks' trailing tol_coef).  Nothing
+is compiled at run time: the kernels are the prebuilt sm_103a code of
+libfastqsl_gb300.so.  `grid` and `block` are accepted and ignored; the launch
+geometry is a persistent grid sized to the GPU.
+"""
+from .. import _lib
+from ..api import ptr
+
+RK4 = 0
+RKF45 = 1
+_ARITH = {"exact": 0, "fast": 1}
+
+
+def _current_stream(args):
+    for a in args:
+        if hasattr(a, "__cuda_array_interface__") and not hasattr(a, "data_ptr"):
+            try:
+                import cupy  # the caller's arrays are CuPy: use CuPy's current stream
+                return cupy.cuda.get_current_stream().ptr
+            except ImportError:
+                break
+    import torch
+    return torch.cuda.current_stream().cuda_stream
+
+
+# argument positions of the per-seed arrays (inputs and outputs)
+_PER_SEED = [9, 10, 11] + list(range(13, 31)) + [33]
+
+
+def _numel(a):
+    if hasattr(a, "numel"):
+        return int(a.numel())
+    return int(getattr(a, "size", 0))
+
+
+class TraceAllBline:
+    """The reference's TraceAllBline kernel object."""
+
+    def __init__(self, integrator, arith="exact"):
+        if arith not in _ARITH:
+            raise ValueError("arith must be 'exact' or 'fast'")
+        self.integrator = integrator
+        self.arith = arith
+        self.nargs = 35 if integrator == RKF45 else 34
+        _lib.load()
+
+    def __call__(self, grid, block, args, shared_mem=0, stream=None):
+        args = tuple(args)
+        if len(args) < self.nargs:
+            raise TypeError(f"TraceAllBline takes {self.nargs} arguments, got {len(args)}")
+        # the per-seed arrays bound the number of lines the kernel may touch
+        cap = min(_numel(args[i]) for i in _PER_SEED)
+        p = [ptr(a) if _numel(a) else None for a in args[:self.nargs]]
+        if self.integrator == RK4:
+            p.append(None)  # no tol_coef
+        st = stream if stream is not None else _current_stream(args)
+        lib = _lib.load()
+        _lib.check(lib.qsl_trace_all_bline(self.integrator, _ARITH[self.arith], *p, cap, st), "TraceAllBline")
+
+
+def compileTraceBlineAdaptive(arith="exact"):
+    """RKF45 tracer (reference: fastqslpy/kernels.py:10-18)."""
+    return TraceAllBline(RKF45, arith)
+
+
+def compileTraceBlineRK4(arith="exact"):
+    """Fixed-step RK4 tracer (reference: fastqslpy/kernels.py:21-29)."""
+    return TraceAllBline(RK4, arith)

@@ -1,0 +1,243 @@
+/*
+ * fastqsl_gb300 — C ABI of the GB300 (sm_103a) field-line tracer and
+ * squashing-factor (Q) assembly.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless its name ends in _h.
+ *  - Field arrays Bx, By, Bz have shape (nx, ny, nz) with x fastest in memory:
+ *    element (i, j, k) lives at i + nx*(j + ny*k)  (the layout of
+ *    fastqslpy/cu/TraceBlineAdaptive.cu:36-39, get_Idx3d).
+ *  - Every entry point returns 0 on success and a negative qsl_status on
+ *    failure; work is enqueued on `stream` (0 = legacy default stream) and the
+ *    call does not synchronise unless stated.
+ *  - Per-line boundary flags keep the reference meaning
+ *    (TraceBlineAdaptive.cu:309-331): 0 inside / stopped by a limit,
+ *    1..6 left through x-min, x-max, y-min, y-max, z-min, z-max,
+ *    42 edge, corner or non-finite position.
+ */
+#ifndef FASTQSL_GB300_H
+#define FASTQSL_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *qsl_stream_t; /* == cudaStream_t */
+
+enum qsl_status {
+    QSL_OK = 0,
+    QSL_ERR_INVALID = -1,   /* bad argument: null pointer, bad shape, bad enum */
+    QSL_ERR_NOMEM = -2,     /* device allocation failed */
+    QSL_ERR_CUDA = -3,      /* a CUDA call failed; qsl_last_error() has the text */
+    QSL_ERR_TOO_LARGE = -4, /* request exceeds a stated maximum */
+    QSL_ERR_NODEVICE = -5
+};
+
+enum qsl_integrator { QSL_RK4 = 0, QSL_RKF45 = 1 };
+
+enum qsl_tol_law {
+    /* tol*|b0.n|^1.5*tol_coef, or tol/8e3*tol_coef when |b0.n| <= 0.05, with b0
+     * the unit field at the seed and n the seed-plane normal
+     * (TraceBlineAdaptive.cu:354-359) */
+    QSL_TOL_REFERENCE = 0,
+    /* tol*tol_coef */
+    QSL_TOL_ABSOLUTE = 1
+};
+
+/* Arithmetic of the tracing kernels. */
+enum qsl_arith {
+    /* Same operation order and rounding as the reference kernels built without
+     * fused multiply-add: corner weights in FP64, IEEE divide and sqrt. */
+    QSL_ARITH_EXACT = 0,
+    /* FP32 with fused multiply-add, FP32 corner weights and rsqrt
+     * normalisation. */
+    QSL_ARITH_FAST = 1
+};
+
+/* Integrator settings.  qsl_params_reference_rk4/_rkf45 fill the values the
+ * reference hard-wires (TraceBline.cu:10-12, TraceBlineAdaptive.cu:10-13). */
+typedef struct qsl_trace_params {
+    int32_t integrator;      /* qsl_integrator */
+    int32_t tol_law;         /* qsl_tol_law (RKF45 only) */
+    double tol;              /* base local-error tolerance; reference 1e-3 */
+    double h_min;            /* accepted-step lower clamp; reference 0.1 */
+    double h_max;            /* accepted-step upper clamp; reference 100 */
+    double reject_factor;    /* step shrink on rejection; reference 0.618 */
+    double len_ratio;        /* length limit = len_ratio*(nx+ny+nz); ref 3 (RKF45), 2 (RK4) */
+    int64_t max_steps;       /* accepted steps per direction; ref 500000 (RKF45), 100000 (RK4) */
+    int32_t boundary_twist;  /* add the exit-segment twist term (RK4 reference does, TraceBline.cu:362-365) */
+    int32_t arith;           /* qsl_arith */
+} qsl_trace_params;
+
+void qsl_params_reference_rk4(qsl_trace_params *p_h);
+void qsl_params_reference_rkf45(qsl_trace_params *p_h);
+
+/* Text of the last error on the calling host thread. */
+const char *qsl_last_error(void);
+const char *qsl_version(void);
+int qsl_device_sm_count(int *sms_h);
+
+/* ------------------------------------------------------------------------
+ * Drop-in tracing entry points.
+ *
+ * These replace the CUDA kernel the reference compiles at run time and calls
+ * through cupy.RawKernel (fastqslpy/kernels.py:10-29, returning
+ * TraceAllBline):
+ *   qsl_trace_all_bline_rkf45 <- TraceAllBline of
+ *       fastqslpy/cu/TraceBlineAdaptive.cu:429-437 (35 arguments)
+ *   qsl_trace_all_bline_rk4   <- TraceAllBline of
+ *       fastqslpy/cu/TraceBline.cu:383-391 (34 arguments, no tol_coef)
+ * Same argument order and meaning; scalars (BshapeN[3], inp_cross_dir[3],
+ * s_len[1], N[1], tol_coef[1], curB_flag[1]) are device pointers as in the
+ * reference; every array is caller-allocated device memory.  The launch
+ * geometry the reference takes from the caller is chosen here (a persistent
+ * grid sized to the GPU).  Arithmetic is QSL_ARITH_EXACT.  When *curB_flag
+ * is false the curB_* arrays and `twist` are not read or written (they may be
+ * null).  Asynchronous on `stream`.
+ * ------------------------------------------------------------------------ */
+int qsl_trace_all_bline_rkf45(const float *Bx, const float *By, const float *Bz, const int *BshapeN,
+                              const float *curB_x, const float *curB_y, const float *curB_z, double *twist,
+                              const bool *curB_flag, const float *inp_x, const float *inp_y, const float *inp_z,
+                              const float *inp_cross_dir, float *start_x, float *start_y, float *start_z,
+                              int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                              float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag, float *B_start_x,
+                              float *B_start_y, float *B_start_z, float *B_end_x, float *B_end_y, float *B_end_z,
+                              const float *s_len, const unsigned long long *N, double *LineLen,
+                              const float *tol_coef, qsl_stream_t stream);
+
+int qsl_trace_all_bline_rk4(const float *Bx, const float *By, const float *Bz, const int *BshapeN,
+                            const float *curB_x, const float *curB_y, const float *curB_z, double *twist,
+                            const bool *curB_flag, const float *inp_x, const float *inp_y, const float *inp_z,
+                            const float *inp_cross_dir, float *start_x, float *start_y, float *start_z,
+                            int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                            float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag, float *B_start_x,
+                            float *B_start_y, float *B_start_z, float *B_end_x, float *B_end_y, float *B_end_z,
+                            const float *s_len, const unsigned long long *N, double *LineLen, qsl_stream_t stream);
+
+/* The two entries above with the integrator (qsl_integrator) and arithmetic
+ * (qsl_arith) chosen by the caller; tol_coef may be null for QSL_RK4.
+ * capacity >= 0: the number of elements every per-seed array holds; seeds at
+ * or beyond it are never read or written even if *N is larger (0: nothing
+ * is launched and the pointers may be null).  -1: trust *N as the
+ * reference does. */
+int qsl_trace_all_bline(int integrator, int arith, const float *Bx, const float *By, const float *Bz,
+                        const int *BshapeN, const float *curB_x, const float *curB_y, const float *curB_z,
+                        double *twist, const bool *curB_flag, const float *inp_x, const float *inp_y,
+                        const float *inp_z, const float *inp_cross_dir, float *start_x, float *start_y,
+                        float *start_z, int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                        float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag, float *B_start_x,
+                        float *B_start_y, float *B_start_z, float *B_end_x, float *B_end_y, float *B_end_z,
+                        const float *s_len, const unsigned long long *N, double *LineLen, const float *tol_coef,
+                        int64_t capacity, qsl_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Resident field stores (no reference counterpart: the reference keeps the
+ * caller's three arrays).  A store converts the caller's field once into a
+ * GB300 layout and owns that copy; QSL_LAYOUT_SOA borrows the caller's
+ * arrays (they must outlive the store).
+ * ------------------------------------------------------------------------ */
+enum qsl_layout {
+    QSL_LAYOUT_SOA = 0, /* the caller's Bx, By, Bz in place */
+    QSL_LAYOUT_F4 = 1,  /* interleaved float4 per node (16 B/node) */
+    QSL_LAYOUT_H4B = 2  /* fp16 8^3-cell bricks with a +1 apron and a float scale per brick */
+};
+typedef struct qsl_field qsl_field_t;
+
+/* Device bytes a store of this shape and layout owns (0 for SOA). */
+int64_t qsl_field_store_bytes(int nx, int ny, int nz, int layout);
+int qsl_field_create(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz, int layout,
+                     qsl_stream_t stream, qsl_field_t **out_h);
+int qsl_field_destroy(qsl_field_t *field);
+int64_t qsl_field_bytes(const qsl_field_t *field);
+/* Refills a store from new arrays of the same shape (no reallocation). */
+int qsl_field_update(qsl_field_t *field, const float *Bx, const float *By, const float *Bz, qsl_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Native tracing entry (the drop-in entries are thin wrappers of the same
+ * kernels).  Outputs keep the meaning of TraceAllBline's
+ * (TraceBlineAdaptive.cu:429-510).
+ * ------------------------------------------------------------------------ */
+enum qsl_schedule {
+    QSL_SCHED_QUEUE = 0, /* persistent grid, per-lane refill from a device work counter */
+    QSL_SCHED_STATIC = 1 /* one line per thread (needs the host count) */
+};
+
+typedef struct qsl_trace_io {
+    const float *inp_x, *inp_y, *inp_z;
+    float *start_x, *start_y, *start_z;
+    int *flag_start;
+    float *end_x, *end_y, *end_z;
+    int *flag_end;
+    float *B_this_x, *B_this_y, *B_this_z;
+    int *B_flag;
+    float *B_start_x, *B_start_y, *B_start_z;
+    float *B_end_x, *B_end_y, *B_end_z;
+    double *LineLen;
+    double *twist; /* needed when curB is given */
+} qsl_trace_io;
+
+/* Traces n seeds (or *n_dev seeds when n_dev is set; then the outputs must
+ * hold the largest possible count).  cross_dir_h: the seed-plane normal
+ * (host, 3 floats; null = z).  curB*: current density for the twist
+ * integral, or null.  samples_dev (optional) accumulates the number of
+ * trilinear field samples taken.  queue_dev (optional): an 8-byte device
+ * counter used as the work queue; when null one is allocated on `stream`
+ * (stream-ordered) and freed after the launch. */
+int qsl_trace(const qsl_field_t *field, const qsl_trace_params *params_h, const qsl_trace_io *io_h, int64_t n,
+              const unsigned long long *n_dev, float s_len, float tol_coef, const float *cross_dir_h,
+              const float *curBx, const float *curBy, const float *curBz, int schedule,
+              unsigned long long *samples_dev, unsigned long long *queue_dev, qsl_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Q assembly.
+ * ------------------------------------------------------------------------ */
+
+/* Replaces fastqslpy/FastQSL.py:65-117 (QCalcPlane).  Inputs are nplanes
+ * stacked (n0, n1) row-major planes; Q is (nplanes, n0-2, n1-2).
+ * jac_scale = (1/(2*stride_step))^4.  Give exactly one of Q32 (the
+ * reference's FP32 rounding) or Q64 (FP64).  Bz_in / Bz_out are Bz at the
+ * start / end footpoints (the reference uses the z component whatever the
+ * exit face, FastQSL.py:112-113). */
+int qsl_qcalc_plane(const float *x_end, const float *y_end, const float *z_end, const int *flag_end,
+                    const float *x_start, const float *y_start, const float *z_start, const int *flag_start,
+                    const float *Bz_in, const float *Bz_out, const float *Bx_0, const float *By_0,
+                    const float *Bz_0, int n0, int n1, int64_t nplanes, double jac_scale,
+                    const float *cross_dir_h, float *Q32, double *Q64, qsl_stream_t stream);
+
+/* Replaces the seed construction of fastqslpy/FastQSL.py:4-57
+ * (CookPseudoLine): for every pixel with B_flag == 1 (row-major order; only
+ * interior pixels of each (n0, n1) plane when interior_only), four seeds
+ * around its start footpoint, +-stride along the start face's two axes in
+ * the order (+u, +v, -u, -v).  Outputs must hold 4n seeds and n pixels;
+ * count_dev[0] receives the pixel count and count_dev[1] the seed count
+ * (4 per pixel, usable as the n_dev of qsl_trace).  workspace: device scratch of
+ * qsl_cook_workspace_bytes(n) bytes. */
+int64_t qsl_cook_workspace_bytes(int64_t n);
+int qsl_cook_pseudo_line(const int *B_flag, const float *x_start, const float *y_start, const float *z_start,
+                         const int *flag_start, const float *Bz_in, const float *Bz_out, int64_t n, int n0, int n1,
+                         int interior_only, float stride, float *cut_x, float *cut_y, float *cut_z,
+                         float *Bz0_start, float *Bz0_end, int64_t *pix, unsigned long long *count_dev,
+                         void *workspace, int64_t workspace_bytes, qsl_stream_t stream);
+
+/* Replaces demo/Q_RKF45CuPy.ipynb cell 10: Q of each pseudo-line pixel from
+ * its 4 traced pseudo-lines; jac_scale = (1/(2*stride))^4.  The pixel count
+ * is `count`, or *count_dev when set (then max_count bounds the launch). */
+int qsl_qcut(const float *start_x, const float *start_y, const float *start_z, const int *flag_start,
+             const float *end_x, const float *end_y, const float *end_z, const int *flag_end,
+             const float *Bz0_start, const float *Bz0_end, int64_t count, const unsigned long long *count_dev,
+             int64_t max_count, double jac_scale, float *Qcut32, double *Qcut64, qsl_stream_t stream);
+
+/* Replaces demo/Q_RKF45CuPy.ipynb cell 11: Qfinal (nplanes, n0-2, n1-2) gets
+ * Qcut at every compacted interior pixel `pix`. */
+int qsl_qmerge(const int64_t *pix, const float *Qcut32, const double *Qcut64, int64_t count,
+               const unsigned long long *count_dev, int64_t max_count, int n0, int n1, float *Qfinal32,
+               double *Qfinal64, qsl_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

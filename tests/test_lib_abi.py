@@ -1,0 +1,67 @@
+"""The C-ABI library builds, loads without a GPU and exports every entry
+point include/fastqsl_gb300.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fastqsl_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qsl_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from fastqsl_gb300 import _build, _lib
+    _build.build()
+    return _lib.load()
+
+
+def test_header_declares_the_drop_in_entries():
+    names = declared_functions()
+    for n in ["qsl_trace_all_bline_rkf45", "qsl_trace_all_bline_rk4", "qsl_qcalc_plane", "qsl_cook_pseudo_line",
+              "qsl_qcut", "qsl_qmerge", "qsl_trace", "qsl_field_create"]:
+        assert n in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from fastqsl_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\sT\s(qsl_\w+)", out))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    # and the ctypes table covers the same set
+    assert set(_lib.exported_names()) == set(declared_functions())
+
+
+def test_reference_presets_match_python(lib):
+    from fastqsl_gb300 import params as P
+    for cfn, pfn in ((lib.qsl_params_reference_rk4, P.reference_rk4), (lib.qsl_params_reference_rkf45,
+                                                                        P.reference_rkf45)):
+        c = P.TraceParams()
+        cfn(ctypes.byref(c))
+        assert c.as_dict() == pfn().as_dict()
+
+
+def test_params_struct_layout():
+    from fastqsl_gb300 import params as P
+    # int32, int32, 5 doubles, int64, int32, int32
+    assert ctypes.sizeof(P.TraceParams) == 4 + 4 + 5 * 8 + 8 + 4 + 4
+
+
+def test_version_and_errors_without_gpu(lib):
+    assert b"sm_103a" in lib.qsl_version()
+    # argument validation runs before any CUDA call
+    rc = lib.qsl_qcalc_plane(*([None] * 13), 2, 2, 1, 1.0, None, None, None, None)
+    assert rc == -1
+    assert b"null" in lib.qsl_last_error()
+    assert lib.qsl_field_store_bytes(1, 5, 5, 1) == -1
+    assert lib.qsl_field_store_bytes(9, 9, 9, 2) == 5888 + 4
+    assert lib.qsl_field_store_bytes(10, 10, 10, 1) == 16000
