@@ -1,0 +1,379 @@
+"""Benchmark: Q-pixels/s of a full 3-D Q-cube on one GB300.
+
+Workload (one "step"): the 512x512x256 float32 field of 32 sub-surface point
+charges (seeded positions at depth 4-20 cells, strengths +-U(0.2, 2)); Q at
+every interior cell of the central 256x256x128 sub-box, plane by plane with
+z-plane normals (258x258 seeds per plane incl. a one-cell halo for the
+central differences, 128 planes traced in one launch), RKF45 with absolute
+tolerance 1e-4 and steps in [1e-3, 1] cell, pseudo-lines for the pixels
+whose field lies within ~0.6 deg of the plane, FP64 Q assembly.
+
+Forms measured on that workload:
+  value      — fp16 8^3-brick field store + persistent lane-refill tracer
+  plain_fp32 — the plain FP32 kernel: reference SoA field, one line per
+               thread (static grid), no work queue
+Inputs are resident in HBM during the timed region and larger than L2
+(field 805 MB fp32 / 764 MB fp16 bricks; outputs ~0.9 GB), so no L2 flush is
+needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FIELD_SHAPE = (512, 512, 256)
+SUB = dict(x0=128, y0=128, z0=64, nx=256, ny=256, nz=128)
+S_LEN = 0.25
+METRIC = "Q-pixels/s (3-D Q-cube, 512x512x256 field, RKF45 tol 1e-4)"
+NPLANES = [SUB["nz"]]  # --planes: fewer z-planes of the same cube (profiling cases)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4)
+                          if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cube_seeds(device, planes=None):
+    if planes is None and NPLANES[0] != SUB["nz"]:
+        planes = list(range(NPLANES[0]))
+    from fastqsl_gb300 import api
+    s = SUB
+    zs = [float(s["z0"] + k) for k in (range(s["nz"]) if planes is None else planes)]
+    xs, ys, zz = api.plane_seed_grid(s["x0"] - 1.0, s["x0"] + s["nx"], s["nx"] + 2, s["y0"] - 1.0,
+                                     s["y0"] + s["ny"], s["ny"] + 2, zs, device=device)
+    return xs, ys, zz, len(zs)
+
+
+def make_field(device):
+    from fastqsl_gb300 import synthetic as S
+    spec = S.charges32_512(seed=0, shape=FIELD_SHAPE)
+    return S.make_field(spec, device=device, as_numpy=False), spec
+
+
+def run_ours(args, rank, world):
+    import torch
+    from fastqsl_gb300 import api, params as P
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    (bx, by, bz), spec = make_field(dev)
+    prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_FAST)
+    xs, ys, zz, npl = cube_seeds(dev)
+    n0, n1 = SUB["ny"] + 2, SUB["nx"] + 2
+    qpix = SUB["nx"] * SUB["ny"] * npl
+    store = api.FieldStore(bx, by, bz, layout=args.layout)
+    plan = api.QMapPlan(n0, n1, npl, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(count=False, ev=None):
+        return plan.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0, count_samples=count, kernel_events=ev)
+
+    # warm-up
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # samples per step (device counter) for the roofline
+    step(count=True)
+    torch.cuda.synchronize()
+    samples_main = int(plan.samples_main.item())
+    samples_all = int(plan.samples.item())
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    kev = []
+    with ClockSampler(dev.index) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            kev.append(ev)
+            step(ev=ev)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = t0.elapsed_time(t1) / args.steps
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    k_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
+    Q = plan.Q
+
+    res = {"ms": ms, "qpix": qpix, "k_ms": k_ms, "samples_main": samples_main, "samples_all": samples_all,
+           "clocks": clk.summary()}
+    if rank != 0:
+        return res, None
+
+    # ---- plain FP32 kernel (SoA field, static one-line-per-thread grid) ----
+    if not args.skip_plain:
+        soa = api.FieldStore(bx, by, bz, layout="soa")
+        out = plan.main
+        for _ in range(2):
+            api.trace(soa, xs, ys, zz, prm, s_len=S_LEN, schedule="static", out=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        reps = max(1, min(3, args.steps))
+        for _ in range(reps):
+            api.trace(soa, xs, ys, zz, prm, s_len=S_LEN, schedule="static", out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["plain_trace_ms"] = e0.elapsed_time(e1) / reps
+        # the same trace through the plan's kernel configuration for the ratio
+        e0.record(stream)
+        for _ in range(reps):
+            api.trace(store, xs, ys, zz, prm, s_len=S_LEN, schedule=plan.schedule, out=out, order=plan.order,
+                      chunk=plan.chunk, occupancy=plan.occupancy_for(store))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["ours_trace_ms"] = e0.elapsed_time(e1) / reps
+        soa.close()
+
+    # ---- end to end through the public API with host buffers ----
+    if not args.skip_e2e:
+        hb = [torch.empty(b.shape[::-1], dtype=torch.float32).pin_memory() for b in (bx, by, bz)]
+        for h, b in zip(hb, (bx, by, bz)):
+            h.copy_(b.permute(2, 1, 0))
+        dbuf = [torch.empty(b.shape[::-1], dtype=torch.float32, device=dev) for b in (bx, by, bz)]
+        qh = torch.empty(Q.shape, dtype=Q.dtype).pin_memory()
+
+        def e2e_step():
+            for d, h in zip(dbuf, hb):
+                d.copy_(h, non_blocking=True)
+            store.update(*[d.permute(2, 1, 0) for d in dbuf])
+            q = plan.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0)
+            qh.copy_(q, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(1, min(3, args.steps))
+        e0.record(stream)
+        for _ in range(reps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["e2e_ms"] = e0.elapsed_time(e1) / reps
+        res["h2d"] = int(sum(h.numel() * 4 for h in hb))
+        res["d2h"] = int(qh.numel() * qh.element_size())
+
+    # ---- accuracy against the FP64 oracle on a seeded sample of cells ----
+    if not args.skip_accuracy:
+        res["accuracy"] = accuracy_sample(bx, by, bz, Q.cpu().numpy(), prm, args.acc_cells)
+    store.close()
+    return res, Q
+
+
+def accuracy_sample(bx, by, bz, Q, prm, ncells):
+    """|dlog10 Q| of the GPU cube against the FP64 oracle on `ncells` seeded
+    cells: each sampled cell's Q is recomputed from its 5-seed stencil (and
+    its pseudo-lines when flagged) traced in FP64 on the host."""
+    import oracle
+    from fastqsl_gb300 import params as P
+    from oracle import qassembly as QA
+    rng = np.random.default_rng(1234)
+    s = SUB
+    npl = Q.shape[0]
+    ci = rng.integers(0, npl, ncells)
+    cj = rng.integers(0, s["ny"], ncells)
+    ck = rng.integers(0, s["nx"], ncells)
+    B = [b.permute(2, 1, 0).contiguous().cpu().numpy().transpose(2, 1, 0) for b in (bx, by, bz)]
+    prm64 = P.absolute_rkf45(tol=prm.tol, h_min=prm.h_min, h_max=prm.h_max, arith=P.ARITH_EXACT)
+    # 3x3 stencil planes per cell -> reuse the oracle pipeline on tiny planes
+    xs, ys, zs = [], [], []
+    for i, j, k in zip(ci, cj, ck):
+        z = float(s["z0"] + i)
+        x0 = float(s["x0"] + k - 1)
+        y0 = float(s["y0"] + j - 1)
+        for a in range(3):
+            for b in range(3):
+                xs.append(x0 + b)
+                ys.append(y0 + a)
+                zs.append(z)
+    xs, ys, zs = (np.array(v, np.float32) for v in (xs, ys, zs))
+    tr = lambda a, b, c: oracle.trace_all("port64", B[0], B[1], B[2], a, b, c, s_len=S_LEN,  # noqa: E731
+                                          params=prm64)
+    Qr = QA.qmap_pipeline(tr, xs, ys, zs, ncells, 3, 3, 1.0)[:, 0, 0]
+    Qg = Q[ci, cj, ck]
+    both = ~np.isnan(Qr) & ~np.isnan(Qg)
+    d = np.abs(np.log10(Qg[both]) - np.log10(Qr[both]))
+    return {"cells": int(ncells), "nan_agree": float((np.isnan(Qr) == np.isnan(Qg)).mean()),
+            "median_dlog10Q": float(np.median(d)) if d.size else None,
+            "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None}
+
+
+def cpu_baseline(planes, threads=None):
+    """The tracing routine (oracle port of the reference's, OpenMP) plus the
+    Q assembly on `planes` z-planes of the cube, on the host cores."""
+    import torch
+    import oracle
+    from fastqsl_gb300 import params as P
+    from oracle import qassembly as QA
+    (bx, by, bz), _ = make_field("cpu")
+    B = [b.numpy() if isinstance(b, torch.Tensor) else b for b in (bx, by, bz)]
+    B = [np.asfortranarray(b) for b in B]
+    xs, ys, zz, npl = cube_seeds("cpu", planes=planes)
+    xs, ys, zz = xs.numpy(), ys.numpy(), zz.numpy()
+    prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_EXACT)
+    cores = threads or os.cpu_count()
+    tr = lambda a, b, c: oracle.trace_all("port32", B[0], B[1], B[2], a, b, c, s_len=S_LEN, params=prm,  # noqa
+                                          threads=cores)
+    t = time.perf_counter()
+    QA.qmap_pipeline(tr, xs, ys, zz, npl, SUB["ny"] + 2, SUB["nx"] + 2, 1.0, f64=True)
+    dt = time.perf_counter() - t
+    qpix = SUB["nx"] * SUB["ny"] * npl
+    return {"value": qpix / dt, "unit": "Q-pixels/s", "cores": cores, "kind": "port",
+            "sample": f"{npl} of {SUB['nz']} z-planes of the same cube ({qpix} Q-pixels), {dt:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--layout", default="h4b", choices=["h4b", "f4", "soa"])
+    ap.add_argument("--cpu-planes", type=int, default=32)
+    ap.add_argument("--acc-cells", type=int, default=2000)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
+    args = ap.parse_args()
+    NPLANES[0] = max(1, min(SUB["nz"], args.planes))
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        per = []
+        for _ in range(args.warmup):
+            cpu_baseline(list(range(1)), None)
+        for _ in range(args.steps):
+            per.append(cpu_baseline(list(range(args.cpu_planes)), None))
+        v = float(np.mean([p["value"] for p in per]))
+        qpix = SUB["nx"] * SUB["ny"] * SUB["nz"]
+        line = {"metric": METRIC, "value": v, "unit": "Q-pixels/s", "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": qpix / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
+                                                 "sampled_planes_per_step": args.cpu_planes},
+                "cpu_baseline": {**per[-1], "value": v},
+                "e2e": {"value": v, "unit": "Q-pixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res, _ = run_ours(args, rank, world)
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    ms = res["ms"]
+    value = res["qpix"] * world / (ms / 1e3)
+    bytes_per_sample = 48 if args.layout == "h4b" else 96
+    achieved = res["samples_main"] * bytes_per_sample / (res["k_ms"] / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "Q-pixels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (fp16 field storage)" if args.layout == "h4b" else "f32",
+        "data": "synthetic",
+        "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
+                   "field": "x".join(map(str, FIELD_SHAPE)), "qcube": "256x256x128", "layout": args.layout,
+                   "schedule": "static lockstep, 8x8 seed tiles, 8 blocks/SM", "h": [1e-3, 1.0],
+                   "planes": NPLANES[0], "l2": "inputs larger than L2 (no flush)"},
+        "gpu_launches": None,
+        "clocks": res["clocks"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_trace_fast<static, FieldH4B> (main trace)",
+                     "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
+                             f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
+    }
+    # launches per step: main trace, qcalc, flag_count, tile_scan, cook_write,
+    # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
+    line["gpu_launches"] = 8 * args.steps
+    if "plain_trace_ms" in res:
+        line["plain_fp32"] = {"trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
+                              "speedup": res["plain_trace_ms"] / res["ours_trace_ms"]}
+    if "e2e_ms" in res:
+        line["e2e"] = {"value": res["qpix"] / (res["e2e_ms"] / 1e3), "unit": "Q-pixels/s",
+                       "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]}
+    if "accuracy" in res:
+        line["accuracy_vs_fp64"] = res["accuracy"]
+    if not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(list(range(args.cpu_planes)))
+    line["samples_per_step"] = res["samples_all"]
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

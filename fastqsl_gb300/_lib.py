@@ -32,6 +32,11 @@ class TraceIO(ctypes.Structure):
         "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist")]
 
 
+class Sched(ctypes.Structure):
+    _fields_ = [("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32), ("order", ctypes.c_void_p),
+                ("queue", ctypes.c_void_p), ("samples", ctypes.c_void_p), ("occupancy", ctypes.c_int32)]
+
+
 # name -> (restype, argtypes); every pointer is c_void_p
 _P = c_vp
 _SIGS = {
@@ -48,7 +53,7 @@ _SIGS = {
     "qsl_field_destroy": (c_int, [_P]),
     "qsl_field_bytes": (c_i64, [_P]),
     "qsl_field_update": (c_int, [_P, _P, _P, _P, _P]),
-    "qsl_trace": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, _P, c_int, _P, _P, _P]),
+    "qsl_trace": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, _P, _P, _P]),
     "qsl_qcalc_plane": (c_int, [_P] * 13 + [c_int, c_int, c_i64, c_double, _P, _P, _P, _P]),
     "qsl_cook_workspace_bytes": (c_i64, [c_i64]),
     "qsl_cook_pseudo_line": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 8 + [c_i64, _P]),

@@ -138,12 +138,13 @@ def _io(xs, ys, zs, out):
 
 def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_len=0.125, tol_coef=1.0,
           cross_dir=(0.0, 0.0, 1.0), curB=None, schedule="queue", out=None, n=None, n_dev=None, samples=None,
-          queue=None, stream=None):
+          queue=None, order=None, chunk=0, occupancy=0, stream=None):
     """Traces every seed (xs, ys, zs: float32 CUDA vectors) both ways.
     Returns the output dict (allocated unless `out` is given).  `n_dev`: a
     device counter holding the seed count (outputs must then hold the largest
     count).  `samples`: optional int64 CUDA tensor accumulating the number of
-    trilinear samples taken."""
+    trilinear samples taken.  `order`: optional int32 permutation; line k
+    traces seed order[k] (see tile_order).  `chunk`: lines per warp refill."""
     lib = _lib.load()
     if params is None:
         params = absolute_rkf45()
@@ -155,10 +156,26 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
     if curB is not None and out.get("twist") is None:
         out["twist"] = torch.zeros(out["LineLen"].shape[0], dtype=torch.float64, device=xs.device)
     io = _io(xs, ys, zs, out)
+    sc = _lib.Sched(SCHEDULES[schedule], int(chunk), ptr(order), ptr(queue), ptr(samples), int(occupancy))
     _lib.check(lib.qsl_trace(field.handle, ctypes.byref(params), ctypes.byref(io), n, ptr(n_dev),
-                             float(s_len), float(tol_coef), cd, *cur, SCHEDULES[schedule], ptr(samples), ptr(queue),
-                             stream_handle(stream)), "qsl_trace")
+                             float(s_len), float(tol_coef), cd, *cur, ctypes.byref(sc), stream_handle(stream)),
+               "qsl_trace")
     return out
+
+
+def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda"):
+    """A permutation of the seeds of `nplanes` stacked (n0, n1) planes that
+    visits them tile by tile (ty x tx seeds, row-major inside a tile, tiles
+    row-major, planes in turn), as int32 on the device.  Neighbouring seeds
+    start neighbouring field lines, so a warp given consecutive lines of this
+    order gathers from a compact patch of the field."""
+    p = torch.arange(nplanes, device=device, dtype=torch.int64).view(-1, 1, 1)
+    y = torch.arange(n0, device=device, dtype=torch.int64).view(1, -1, 1)
+    x = torch.arange(n1, device=device, dtype=torch.int64).view(1, 1, -1)
+    ntx = (n1 + tx - 1) // tx
+    nty = (n0 + ty - 1) // ty
+    key = (((p * nty + y // ty) * ntx + x // tx) * (ty * tx) + (y % ty) * tx + (x % tx))
+    return torch.argsort(key.reshape(-1)).to(torch.int32)
 
 
 class QMapPlan:
@@ -167,23 +184,36 @@ class QMapPlan:
 
     trace all seeds -> Q on interior pixels (FP64 Jacobian norm and flux
     ratio) -> compact the B_flag pixels -> trace their 4 pseudo-lines -> Q of
-    those pixels -> merge.  No host synchronisation inside; the pseudo-line
+    those pixels -> merge.  The main trace visits the seeds in `tile` order
+    with lanes in lockstep (`schedule`='static'): a warp's lanes start on
+    neighbouring seeds and advance together, so their gathers stay on a
+    compact patch of the field.  No host synchronisation inside; the pseudo-line
     trace reads its seed count from the device, so a whole run can be
     captured in a CUDA graph.  Outputs Q of shape (nplanes, n0-2, n1-2)
     (float64).  Reference workflow: demo/Q_RKF45CuPy3D.ipynb cell 7 and
     demo/Q_RKF45CuPy.ipynb cells 7-11."""
 
-    def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True):
+    # measured best per field layout on GB300 (trace of the 512x512x256 cube):
+    # register budget for 8 resident blocks/SM for the brick and float4
+    # stores, the compiler's choice for SoA
+    DEFAULT_OCCUPANCY = {"h4b": 8, "f4": 8, "soa": 0}
+
+    def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True, tile=(8, 8), chunk=256, schedule="static",
+                 occupancy=None):
         self.n0, self.n1, self.nplanes = int(n0), int(n1), int(nplanes)
         if self.n0 < 3 or self.n1 < 3:
             raise ValueError("planes must be at least 3 x 3 seeds")
         self.n = self.n0 * self.n1 * self.nplanes
         self.device = device
         self.pseudo = pseudo
+        self.schedule = schedule
+        self.chunk = int(chunk)
+        self.occupancy = occupancy  # None: per-layout default at run time
+        self.order = tile_order(self.nplanes, self.n0, self.n1, tile[0], tile[1], device) if tile else None
         self.main = alloc_trace_outputs(self.n, device)
         self.Q = torch.empty((self.nplanes, self.n0 - 2, self.n1 - 2), dtype=torch.float64, device=device)
         self.queue = torch.zeros(2, dtype=torch.int64, device=device)
-        self.samples = torch.zeros(1, dtype=torch.int64, device=device)
+        self.samples_buf = torch.zeros(2, dtype=torch.int64, device=device)  # main, pseudo-line trace
         if pseudo:
             m = self.nplanes * (self.n0 - 2) * (self.n1 - 2)  # at most every interior pixel
             self.max_pix = m
@@ -198,18 +228,38 @@ class QMapPlan:
             self.sub = alloc_trace_outputs(4 * m, device)
             self.qcut = torch.empty(m, dtype=torch.float64, device=device)
 
+    def occupancy_for(self, field):
+        if self.occupancy is not None:
+            return int(self.occupancy)
+        return self.DEFAULT_OCCUPANCY.get(field.layout, 0)
+
+    @property
+    def samples_main(self):
+        return self.samples_buf[0]
+
+    @property
+    def samples(self):
+        return self.samples_buf.sum()
+
     def run(self, field, xs, ys, zs, params=None, s_len=0.125, tol_coef=1.0, stride=1.0, cross_dir=(0.0, 0.0, 1.0),
-            pseudo_tol_factor=1.0, count_samples=False, stream=None):
+            pseudo_tol_factor=1.0, count_samples=False, kernel_events=None, stream=None):
+        """Runs the pipeline; `kernel_events` (start, end) CUDA events are
+        recorded around the main trace launch when given."""
         lib = _lib.load()
         st = stream_handle(stream)
         if params is None:
             params = absolute_rkf45()
-        samples = self.samples if count_samples else None
         if count_samples:
-            self.samples.zero_()
+            self.samples_buf.zero_()
         m = self.main
-        trace(field, xs, ys, zs, params, s_len, tol_coef, cross_dir, out=m, n=self.n, samples=samples,
-              queue=self.queue, stream=stream)
+        ev_stream = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.current_stream()
+        if kernel_events is not None:
+            kernel_events[0].record(ev_stream)
+        trace(field, xs, ys, zs, params, s_len, tol_coef, cross_dir, out=m, n=self.n,
+              samples=self.samples_buf[0:1] if count_samples else None, queue=self.queue, order=self.order,
+              chunk=self.chunk, schedule=self.schedule, occupancy=self.occupancy_for(field), stream=stream)
+        if kernel_events is not None:
+            kernel_events[1].record(ev_stream)
         jac = (1.0 / (2.0 * float(stride))) ** 4.0
         cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
         _lib.check(lib.qsl_qcalc_plane(ptr(m["end_x"]), ptr(m["end_y"]), ptr(m["end_z"]), ptr(m["flag_end"]),
@@ -227,7 +277,8 @@ class QMapPlan:
                                             self.work_bytes, st), "qsl_cook_pseudo_line")
         cnt_seeds = self.count[1:2]
         trace(field, self.cut[0], self.cut[1], self.cut[2], params, s_len, tol_coef * pseudo_tol_factor, cross_dir,
-              out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds, samples=samples, queue=self.queue[1:2],
+              out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds,
+              samples=self.samples_buf[1:2] if count_samples else None, queue=self.queue[1:2],
               stream=stream)
         s = self.sub
         _lib.check(lib.qsl_qcut(ptr(s["start_x"]), ptr(s["start_y"]), ptr(s["start_z"]), ptr(s["flag_start"]),

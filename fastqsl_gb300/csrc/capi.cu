@@ -276,6 +276,9 @@ static void fill_common(TraceJob<F>& J, const qsl_trace_io* io, const qsl_trace_
     J.prm = *prm;
     J.queue = nullptr;
     J.samples = samples_dev;
+    J.order = nullptr;
+    J.chunk = 0;
+    J.occupancy = 0;
     memset(&J.s, 0, sizeof(J.s));
     J.s.n_cap = -1;
 }
@@ -284,8 +287,17 @@ extern "C" {
 
 int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n,
               const unsigned long long* n_dev, float s_len, float tol_coef, const float* cross_dir_h,
-              const float* curBx, const float* curBy, const float* curBz, int schedule,
-              unsigned long long* samples_dev, unsigned long long* queue_dev, qsl_stream_t stream) {
+              const float* curBx, const float* curBy, const float* curBz, const qsl_sched* sched_h,
+              qsl_stream_t stream) {
+    qsl_sched sc{QSL_SCHED_QUEUE, 0, nullptr, nullptr, nullptr, 0};
+    if (sched_h) sc = *sched_h;
+    const int schedule = sc.schedule;
+    unsigned long long* samples_dev = sc.samples;
+    unsigned long long* queue_dev = sc.queue;
+    if (sc.chunk < 0 || sc.chunk > (1 << 20)) return fail(QSL_ERR_INVALID, "chunk out of range");
+    if (sc.occupancy != 0 && sc.occupancy != 8 && sc.occupancy != 10 && sc.occupancy != 12)
+        return fail(QSL_ERR_INVALID, "occupancy must be 0, 8, 10 or 12");
+    if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
     if (!field) return fail(QSL_ERR_INVALID, "field is null");
     if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
     if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
@@ -316,6 +328,9 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         J.f = FieldSoA{field->bx, field->by, field->bz, field->d};
         fill_common(J, io, prm, samples_dev);
         J.cur = cur;
+        J.order = sc.order;
+        J.chunk = sc.chunk;
+        J.occupancy = sc.occupancy;
         scal(J.s);
         return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
     } else if (field->layout == LAYOUT_F4) {
@@ -323,6 +338,9 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         J.f = FieldF4{field->f4, field->d};
         fill_common(J, io, prm, samples_dev);
         J.cur = cur;
+        J.order = sc.order;
+        J.chunk = sc.chunk;
+        J.occupancy = sc.occupancy;
         scal(J.s);
         return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
     } else {
@@ -330,6 +348,9 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         J.f = FieldH4B{field->bricks, field->scale, field->d, field->nbx, field->nby};
         fill_common(J, io, prm, samples_dev);
         J.cur = cur;
+        J.order = sc.order;
+        J.chunk = sc.chunk;
+        J.occupancy = sc.occupancy;
         scal(J.s);
         return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
     }

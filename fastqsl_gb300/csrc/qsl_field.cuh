@@ -124,6 +124,17 @@ __device__ __forceinline__ void locate(float c, int n, int& i, float& r) {
     if (c >= (float)(n - 1)) { r = 1.f; i = n - 2; }
 }
 
+// Fast form of locate(): clamp into [0, n-1] first, then the cell index is
+// min(trunc, n-2) and the fraction the remainder (6 instructions per axis
+// instead of 8).  Identical for finite coordinates; a NaN coordinate lands on
+// cell 0 with fraction 0 (the line's position is NaN anyway and leaves with
+// flag 42 at the boundary test).
+__device__ __forceinline__ void locate_fast(float c, int n, int& i, float& r) {
+    const float cc = fminf(fmaxf(c, 0.f), (float)(n - 1));
+    i = min(__float2int_rz(cc), n - 2);
+    r = cc - (float)i;
+}
+
 // exact: reference rounding of the corner weights (double products narrowed
 // to float; the bare-fraction products rx*ry are float products).
 __device__ __forceinline__ void weights_exact(float rx, float ry, float rz, float w[8]) {
@@ -170,9 +181,15 @@ template <bool EXACT, class F>
 __device__ __forceinline__ float3 sample(const F& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
-    locate(p.x, f.d.nx, ix, rx);
-    locate(p.y, f.d.ny, iy, ry);
-    locate(p.z, f.d.nz, iz, rz);
+    if (EXACT) {
+        locate(p.x, f.d.nx, ix, rx);
+        locate(p.y, f.d.ny, iy, ry);
+        locate(p.z, f.d.nz, iz, rz);
+    } else {
+        locate_fast(p.x, f.d.nx, ix, rx);
+        locate_fast(p.y, f.d.ny, iy, ry);
+        locate_fast(p.z, f.d.nz, iz, rz);
+    }
     float w[8];
     if (EXACT) weights_exact(rx, ry, rz, w);
     else weights_fast(rx, ry, rz, w);

@@ -11,6 +11,7 @@
 // separators) therefore never hold a warp's other lanes idle.  A static mode
 // (one line per thread, no counter) is the plain baseline.
 #pragma once
+#include <type_traits>
 #include "qsl_field.cuh"
 #include "../../include/fastqsl_gb300.h"
 
@@ -58,6 +59,9 @@ struct TraceJob {
     qsl_trace_params prm;
     unsigned long long* queue;    // work counter, zero at launch; null = static
     unsigned long long* samples;  // optional: total field samples
+    const unsigned* order;        // optional: line k traces seed order[k] and writes its outputs there
+    int chunk;                    // lines a warp takes from the queue at a time (QUEUE)
+    int occupancy;                // resident-block variant of the fast kernels (0 = default)
 };
 
 // Fehlberg 4(5) coefficients, stored to float as the reference does
@@ -139,13 +143,24 @@ __device__ __forceinline__ int box_flag(const Dims& n, float3 p) {
     return f;
 }
 
-// Per-lane state of one direction of one line.
+// x^y correctly rounded to float: the double-precision power narrowed once
+// (its error is far below half a float ulp except within ~2^-28 of a float
+// rounding boundary).  The exact kernels use it so that the step controller's
+// decisions do not depend on one library's powf rounding.
+__device__ __forceinline__ float pow_cr(float x, float y) { return (float)pow((double)x, (double)y); }
+
+// Per-lane state of one direction of one line.  The length accumulates in
+// double for exact arithmetic (as the reference does) and in Kahan-
+// compensated float otherwise (FP64 adds are slow on GB300).
+template <bool EXACT>
 struct Lane {
+    typedef typename std::conditional<EXACT, double, float>::type len_t;
     float3 p;      // current point
     float3 pc;     // Kahan compensation of p (fast arithmetic)
     float h;       // current step
     float tol;     // local error tolerance
-    double len;    // accumulated length
+    len_t len;     // accumulated length
+    float lc;      // Kahan compensation of len (fast arithmetic)
     double tw;     // accumulated twist
     int steps;     // accepted steps
     int dir;       // +1 forward, -1 backward
@@ -154,15 +169,28 @@ struct Lane {
     int flag;
 };
 
+template <bool EXACT>
+__device__ __forceinline__ void len_add(Lane<EXACT>& L, double x_exact, float x_fast) {
+    if (EXACT) {
+        L.len = L.len + x_exact;
+    } else {
+        const float y = x_fast - L.lc;
+        const float t = (float)L.len + y;
+        L.lc = (t - (float)L.len) - y;
+        L.len = t;
+    }
+}
+
 template <bool EXACT, class F>
-__device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lane& L, long long line, int dir,
+__device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, long long line, int dir,
                                            float s_len, float tol_coef, const float3 nrm, unsigned& ns) {
     L.line = line;
     L.dir = dir;
     L.p = v3(__ldg(J.inp_x + line), __ldg(J.inp_y + line), __ldg(J.inp_z + line));
     L.pc = v3(0.f, 0.f, 0.f);
     L.h = s_len;
-    L.len = 0.0;
+    L.len = 0;
+    L.lc = 0.f;
     L.tw = 0.0;
     L.steps = 0;
     L.flag = 0;
@@ -176,7 +204,7 @@ __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lan
         float tol;
         if (J.prm.tol_law == QSL_TOL_REFERENCE) {
             if ((double)bn <= 0.05) tol = (float)(J.prm.tol / 8e3);
-            else tol = (float)(J.prm.tol * (double)powf(bn, 1.5f));
+            else tol = (float)(J.prm.tol * (double)(EXACT ? pow_cr(bn, 1.5f) : powf(bn, 1.5f)));
         } else {
             tol = (float)J.prm.tol;
         }
@@ -189,7 +217,8 @@ __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lan
 // L.out, L.flag, L.len, L.tw final.  Reference: TraceBlineAdap,
 // TraceBlineAdaptive.cu:361-421 and TraceBline, TraceBline.cu:320-373.
 template <bool EXACT, bool TWIST, class F>
-__device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane& L, double len_lim, bool tw_on,
+__device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane<EXACT>& L,
+                                          typename Lane<EXACT>::len_t len_lim, bool tw_on,
                                           unsigned& ns) {
     const qsl_trace_params& pr = J.prm;
     if (!((L.len < len_lim) & (L.steps < pr.max_steps))) {
@@ -204,13 +233,15 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         inc = step_rkf45<EXACT>(f, L.p, hd, err, ns);
         float scale;
         if (EXACT) {
-            scale = powf((float)((double)(L.tol / err) / 11.09), 0.2f);
+            scale = pow_cr((float)((double)(L.tol / err) / 11.09), 0.2f);
             if ((double)scale < 0.618) {
                 L.h = (float)((double)L.h * pr.reject_factor);
                 return false;
             }
         } else {
-            scale = powf(L.tol / err * (float)(1.0 / 11.09), 0.2f);
+            // only the next step size depends on this power: hardware
+            // log2 / exp2 are accurate enough
+            scale = exp2f(0.2f * __log2f(L.tol / err * (float)(1.0 / 11.09)));
             if (scale < 0.618f) {
                 L.h = L.h * (float)pr.reject_factor;
                 return false;
@@ -235,7 +266,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         L.pc = (p2 - L.p) - y;
     }
     const float dl = norm(L.p - p2);
-    L.len = L.len + (double)dl;
+    len_add(L, (double)dl, dl);
     float td = 0.f;
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
     if (TWIST && tw_on) {
@@ -245,9 +276,12 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         td = dot(j1, b1) / dot(b1, b1);
         L.tw = L.tw + (double)td / 4.0 / kRefPi * (double)dl;
     }
-    const int flag = box_flag(f.d, p2);
+    // inside test first: the full face classification only runs on exit
+    const bool inside = (p2.x >= 0.f) & (p2.y > 0.f) & (p2.z >= 0.f) & (p2.x <= (float)(f.d.nx - 1)) &
+                        (p2.y <= (float)(f.d.ny - 1)) & (p2.z <= (float)(f.d.nz - 1));
+    const int flag = inside ? 0 : box_flag(f.d, p2);
     if (flag > 0) {
-        L.len = L.len - (double)dl;
+        len_add(L, -(double)dl, -dl);
         if (TWIST && tw_on) L.tw = L.tw - (double)td / 4.0 / kRefPi * (double)dl;
         if (flag <= 6) {
             const int d = (flag - 1) / 2;
@@ -265,7 +299,8 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
                 } else {
                     L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d, ns);
                 }
-                L.len = L.len + (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(u1, d)));
+                len_add(L, (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(u1, d))),
+                        fabsf(qmid - q1) / (1e-4f + fabsf(comp(u1, d))));
                 b1 = u1;
             } else {
                 L.out = L.p;
@@ -293,9 +328,13 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// The tracer kernel.  QUEUE = true: persistent grid with per-lane refill from
-// J.queue; false: line = global thread index + k * total threads.  TWIST
-// compiles the twist integral in; it runs when the runtime flag is set.
+// The tracer kernel.  QUEUE = true: persistent grid; each warp takes chunks
+// of J.chunk consecutive lines from the device counter J.queue and its lanes
+// refill from the warp's current chunk the moment their line ends, so a
+// warp's lanes stay on neighbouring seeds (spatially coherent gathers) while
+// uneven line lengths never idle them.  QUEUE = false: line = global thread
+// index + k * total threads.  Lines are visited in J.order when it is set.
+// TWIST compiles the twist integral in; it runs when the runtime flag is set.
 template <bool EXACT, bool TWIST, bool QUEUE, class F>
 __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     F f = J.f;
@@ -304,6 +343,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
         f.d.ny = __ldg(J.shape_dev + 1);
         f.d.nz = __ldg(J.shape_dev + 2);
     }
+    // a grid needs two nodes per axis for a trilinear cell (uniform exit)
+    if (f.d.nx < 2 || f.d.ny < 2 || f.d.nz < 2) return;
     const float s_len = J.s.s_len_dev ? __ldg(J.s.s_len_dev) : J.s.s_len;
     const float tol_coef = J.s.tol_coef_dev ? __ldg(J.s.tol_coef_dev) : J.s.tol_coef;
     long long n = J.s.n_dev ? (long long)__ldg(J.s.n_dev) : J.s.n;
@@ -311,47 +352,64 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     const float3 nrm = J.s.cross_dev ? v3(__ldg(J.s.cross_dev), __ldg(J.s.cross_dev + 1), __ldg(J.s.cross_dev + 2))
                                      : v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
-    const double len_lim = J.prm.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz);
+    const typename Lane<EXACT>::len_t len_lim =
+        (typename Lane<EXACT>::len_t)(J.prm.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz));
     unsigned ns = 0;
     unsigned long long ns_total = 0;
     const int lane_id = threadIdx.x & 31;
 
-    Lane L;
+    Lane<EXACT> L;
     bool active = false;
     bool drained = false;
+    // warp-uniform chunk window [c_next, c_end) of the work queue
+    long long c_next = 0, c_end = 0;
+    bool q_empty = false;
+    const long long chunk = J.chunk > 0 ? J.chunk : 256;
     long long next_static = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    // forward-direction results, kept until the line's backward trace ends
-    float3 end_pt = v3(0.f, 0.f, 0.f);
-    double len_fwd = 0.0, tw_fwd = 0.0;
-    int flag_fwd = 0;
 
     while (true) {
         // ---- give lanes without a line the next ones ----
         if (QUEUE) {
-            const bool need = !active && !drained;
-            const unsigned m = __ballot_sync(0xffffffffu, need);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                unsigned long long base = 0;
-                if (lane_id == leader) base = atomicAdd(J.queue, (unsigned long long)__popc(m));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (need) {
-                    const long long line = (long long)base + __popc(m & lanemask_lt());
-                    if (line < n) {
-                        lane_begin<EXACT>(f, J, L, line, +1, s_len, tol_coef, nrm, ns);
-                        active = true;
-                    } else {
-                        drained = true;
+            bool need = !active && !drained;
+            unsigned m = __ballot_sync(0xffffffffu, need);
+            while (m) {
+                if (c_next >= c_end) {
+                    if (q_empty) {
+                        drained = drained || need;
+                        break;
                     }
+                    unsigned long long base = 0;
+                    if (lane_id == 0) base = atomicAdd(J.queue, (unsigned long long)chunk);
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if ((long long)base >= n) {
+                        q_empty = true;
+                        drained = drained || need;
+                        break;
+                    }
+                    c_next = (long long)base;
+                    c_end = min((long long)base + chunk, n);
                 }
+                const long long avail = c_end - c_next;
+                const int take = (int)min((long long)__popc(m), avail);
+                const int rank = __popc(m & lanemask_lt());
+                if (need && rank < take) {
+                    const long long line = c_next + rank;
+                    const long long sidx = J.order ? (long long)__ldg(J.order + line) : line;
+                    lane_begin<EXACT>(f, J, L, sidx, +1, s_len, tol_coef, nrm, ns);
+                    active = true;
+                    need = false;
+                }
+                c_next += take;
+                m = __ballot_sync(0xffffffffu, need);
             }
             if (!__any_sync(0xffffffffu, active)) break;
             if (!active) continue;
         } else {
             if (!active) {
                 if (next_static >= n) break;
-                lane_begin<EXACT>(f, J, L, next_static, +1, s_len, tol_coef, nrm, ns);
+                const long long sidx = J.order ? (long long)__ldg(J.order + next_static) : next_static;
+                lane_begin<EXACT>(f, J, L, sidx, +1, s_len, tol_coef, nrm, ns);
                 next_static += stride;
                 active = true;
             }
@@ -360,29 +418,31 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
         // ---- advance this lane's line by one trial step ----
         if (lane_step<EXACT, TWIST>(f, J, L, len_lim, tw_on, ns)) {
             const long long i = L.line;
+            const TraceOut& o = J.o;
             if (L.dir > 0) {
-                end_pt = L.out;
-                len_fwd = L.len;
-                tw_fwd = L.tw;
-                flag_fwd = L.flag;
+                // forward direction done: its outputs go out now, as the
+                // reference writes them (TraceBlineAdaptive.cu:466-474)
+                const float3 pe = L.out;
+                const float3 be = sample_endpoint<EXACT>(f, pe);
+                ns += 1;
+                o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
+                o.flag_end[i] = L.flag;
+                o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
+                o.line_len[i] = (double)L.len;
+                if (TWIST && tw_on) o.twist[i] = L.tw;
                 lane_begin<EXACT>(f, J, L, i, -1, s_len, tol_coef, nrm, ns);
             } else {
-                const float3 pe = end_pt, ps = L.out;
-                const float3 be = sample_endpoint<EXACT>(f, pe);
+                const float3 ps = L.out;
                 const float3 bs = sample_endpoint<EXACT>(f, ps);
                 const float3 p0 = v3(__ldg(J.inp_x + i), __ldg(J.inp_y + i), __ldg(J.inp_z + i));
                 const float3 b0 = sample_endpoint<EXACT>(f, p0);
-                ns += 3;
-                const TraceOut& o = J.o;
-                o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
-                o.flag_end[i] = flag_fwd;
-                o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
+                ns += 2;
                 o.start_x[i] = ps.x; o.start_y[i] = ps.y; o.start_z[i] = ps.z;
                 o.flag_start[i] = L.flag;
                 o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
                 o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
-                o.line_len[i] = len_fwd + L.len;
-                if (TWIST && tw_on) o.twist[i] = tw_fwd + L.tw;
+                o.line_len[i] = o.line_len[i] + (double)L.len;
+                if (TWIST && tw_on) o.twist[i] = o.twist[i] + L.tw;
                 // B nearly in the seed plane (TraceBlineAdaptive.cu:498-501)
                 const float bn = b0.x * nrm.x + b0.y * nrm.y + b0.z * nrm.z;
                 const float bm = sqrtf(b0.x * b0.x + b0.y * b0.y + b0.z * b0.z);

@@ -4,16 +4,22 @@
 
 namespace qsl {
 
-template <bool TWIST, bool QUEUE, class F>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_fast(const TraceJob<F> J) {
+// MINB: minimum resident blocks per SM the register allocation must allow
+// (1 = compiler's choice).  Higher values trade registers (possibly spills)
+// for resident warps; the autotuner measures and picks.
+template <bool TWIST, bool QUEUE, class F, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_fast(const TraceJob<F> J) {
     trace_kernel_body<false, TWIST, QUEUE>(J);
 }
 
-template <class F>
-static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
+template <class F, int MINB>
+static cudaError_t launch_fast_minb(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host,
+                                    cudaStream_t st) {
     const bool q = sched == SCHED_QUEUE;
-    const void* k = q ? (twist ? (const void*)k_trace_fast<true, true, F> : (const void*)k_trace_fast<false, true, F>)
-                      : (twist ? (const void*)k_trace_fast<true, false, F> : (const void*)k_trace_fast<false, false, F>);
+    const void* k = q ? (twist ? (const void*)k_trace_fast<true, true, F, MINB>
+                               : (const void*)k_trace_fast<false, true, F, MINB>)
+                      : (twist ? (const void*)k_trace_fast<true, false, F, MINB>
+                               : (const void*)k_trace_fast<false, false, F, MINB>);
     int grid;
     if (q) {
         grid = persistent_grid(k, kTraceBlock);
@@ -23,13 +29,23 @@ static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched,
     }
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     if (q) {
-        if (twist) k_trace_fast<true, true, F><<<grid, kTraceBlock, 0, st>>>(J);
-        else k_trace_fast<false, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+        if (twist) k_trace_fast<true, true, F, MINB><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_fast<false, true, F, MINB><<<grid, kTraceBlock, 0, st>>>(J);
     } else {
-        if (twist) k_trace_fast<true, false, F><<<grid, kTraceBlock, 0, st>>>(J);
-        else k_trace_fast<false, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+        if (twist) k_trace_fast<true, false, F, MINB><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_fast<false, false, F, MINB><<<grid, kTraceBlock, 0, st>>>(J);
     }
     return cudaGetLastError();
+}
+
+template <class F>
+static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
+    switch (J.occupancy) {
+        case 8: return launch_fast_minb<F, 8>(J, twist, sched, n_host, st);
+        case 10: return launch_fast_minb<F, 10>(J, twist, sched, n_host, st);
+        case 12: return launch_fast_minb<F, 12>(J, twist, sched, n_host, st);
+        default: return launch_fast_minb<F, 1>(J, twist, sched, n_host, st);
+    }
 }
 
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,

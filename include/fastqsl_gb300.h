@@ -180,17 +180,28 @@ typedef struct qsl_trace_io {
     double *twist; /* needed when curB is given */
 } qsl_trace_io;
 
+/* Scheduling of a trace launch (host struct; pointers are device pointers). */
+typedef struct qsl_sched {
+    int32_t schedule;            /* qsl_schedule */
+    int32_t chunk;               /* QUEUE: lines a warp takes per refill (0 = 256) */
+    const uint32_t *order;       /* optional: line k traces seed order[k] and writes its outputs at
+                                    order[k] (a permutation of [0, n)); visiting seeds in compact
+                                    tiles keeps a warp's gathers coherent */
+    unsigned long long *queue;   /* optional 8-byte work counter; when null one is allocated on
+                                    `stream` (stream-ordered) and freed after the launch */
+    unsigned long long *samples; /* optional: accumulates the number of trilinear field samples */
+    int32_t occupancy;           /* fast kernels: register budget for this many resident 128-thread
+                                    blocks per SM (0 = compiler's choice, or 8, 10, 12) */
+} qsl_sched;
+
 /* Traces n seeds (or *n_dev seeds when n_dev is set; then the outputs must
- * hold the largest possible count).  cross_dir_h: the seed-plane normal
+ * hold n, the largest possible count).  cross_dir_h: the seed-plane normal
  * (host, 3 floats; null = z).  curB*: current density for the twist
- * integral, or null.  samples_dev (optional) accumulates the number of
- * trilinear field samples taken.  queue_dev (optional): an 8-byte device
- * counter used as the work queue; when null one is allocated on `stream`
- * (stream-ordered) and freed after the launch. */
+ * integral, or null.  sched_h: null = QUEUE with defaults. */
 int qsl_trace(const qsl_field_t *field, const qsl_trace_params *params_h, const qsl_trace_io *io_h, int64_t n,
               const unsigned long long *n_dev, float s_len, float tol_coef, const float *cross_dir_h,
-              const float *curBx, const float *curBy, const float *curBz, int schedule,
-              unsigned long long *samples_dev, unsigned long long *queue_dev, qsl_stream_t stream);
+              const float *curBx, const float *curBy, const float *curBz, const qsl_sched *sched_h,
+              qsl_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Q assembly.

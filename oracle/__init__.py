@@ -6,6 +6,8 @@ the product path never imports it.
 
 * ``port32`` — C restatement of the reference tracer in reference-parity FP32
   arithmetic (oracle/port/qsl_port.c, ``qo32_*``);
+* ``port32cr`` — the same with a correctly rounded power function, the
+  rounding of the GPU's exact kernels (``qo32cr_*``);
 * ``port64`` — the same algorithm in FP64 (``qo64_*``), the FP64 oracle;
 * ``ref``    — the reference's own kernels compiled for the host
   (oracle/_ref, only where the reference checkout exists);
@@ -28,6 +30,7 @@ _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
 
 _libs = {}
+_PREFIX = {"port32": "qo32_", "port32cr": "qo32cr_", "port64": "qo64_"}
 
 
 def _load(path):
@@ -110,7 +113,7 @@ def trace_all(impl, Bx, By, Bz, xs, ys, zs, cross_dir=(0, 0, 1), s_len=0.125, to
                                 _p(out["LineLen"], _f64p), ctypes.c_float(tol_coef))
     else:
         lib = port_lib()
-        fn = getattr(lib, "qo32_trace_all" if impl == "port32" else "qo64_trace_all")
+        fn = getattr(lib, _PREFIX[impl] + "trace_all")
         if params is None:
             raise ValueError("port oracle needs params")
         samples = ctypes.c_int64(0)
@@ -141,7 +144,7 @@ def scott_all(impl, Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=Non
     twist_on = curB is not None
     cur = [np.asfortranarray(a, dtype=np.float32).ravel(order="F") for a in curB] if twist_on else [None] * 3
     lib = port_lib()
-    fn = getattr(lib, "qo32_scott_all" if impl == "port32" else "qo64_scott_all")
+    fn = getattr(lib, _PREFIX[impl] + "scott_all")
     samples = ctypes.c_int64(0)
     _set_threads(threads)
     rc = fn(*[_p(a, _f32p) for a in flat], _p(shape, _i32p),
@@ -185,7 +188,7 @@ class Probe:
             self.pre = "qref_"
         else:
             self.lib = port_lib()
-            self.pre = "qo32_" if impl == "port32" else "qo64_"
+            self.pre = _PREFIX[impl]
         for nm, rt in (("interp3d", ctypes.c_float), ("rkf45_scott", ctypes.c_float)):
             f = getattr(self.lib, self.pre + nm, None)
             if f is not None:

@@ -1,7 +1,8 @@
 """Builds the CPU oracle (test infrastructure).
 
 * ``oracle/_build/libqsl_oracle.so`` — the C restatement in oracle/port
-  (FP32 reference-parity ``qo32_*`` and FP64 ``qo64_*``), OpenMP-parallel.
+  (FP32 reference-parity ``qo32_*``, the same with a correctly rounded
+  power ``qo32cr_*``, and FP64 ``qo64_*``), OpenMP-parallel.
   Built on every machine (it is the checker on the GPU host as well).
 * ``oracle/_ref/libqslref_{rk4,rkf45,scott}.so`` — the reference's own kernels
   compiled for the host by ``oracle/build_ref.sh``; only where the reference
@@ -38,14 +39,15 @@ def build_port(force=False):
     if not force and _newer(PORT_SO, [src, hdr, __file__]):
         return PORT_SO
     os.makedirs(BUILD, exist_ok=True)
-    o32 = os.path.join(BUILD, "qsl_port32.o")
-    o64 = os.path.join(BUILD, "qsl_port64.o")
-    p1 = subprocess.Popen(["gcc", *_CFLAGS, "-DQO_REAL=float", "-DQO_DOUBLE=0", "-c", src, "-o", o32])
-    p2 = subprocess.Popen(["gcc", *_CFLAGS, "-DQO_REAL=double", "-DQO_DOUBLE=1", "-c", src, "-o", o64])
-    if p1.wait() != 0 or p2.wait() != 0:
+    variants = [("qsl_port32.o", ["-DQO_REAL=float", "-DQO_DOUBLE=0", "-DQO_CRPOW=0"]),
+                ("qsl_port32cr.o", ["-DQO_REAL=float", "-DQO_DOUBLE=0", "-DQO_CRPOW=1"]),
+                ("qsl_port64.o", ["-DQO_REAL=double", "-DQO_DOUBLE=1", "-DQO_CRPOW=0"])]
+    objs = [os.path.join(BUILD, o) for o, _ in variants]
+    procs = [subprocess.Popen(["gcc", *_CFLAGS, *d, "-c", src, "-o", o]) for o, (_, d) in zip(objs, variants)]
+    if any(p.wait() != 0 for p in procs):
         raise RuntimeError("oracle port compile failed")
     tmp = PORT_SO + ".tmp"
-    subprocess.check_call(["gcc", "-shared", "-fopenmp", o32, o64, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", "-shared", "-fopenmp", *objs, "-o", tmp, "-lm"])
     os.replace(tmp, PORT_SO)
     return PORT_SO
 

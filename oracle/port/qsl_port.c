@@ -13,6 +13,8 @@
  *       bit (checked by the tests against oracle/_ref).  With
  *       params->tol_law / h_min / h_max / ... set to non-reference values it
  *       is also the CPU baseline for the benchmark settings.
+ *   QO_REAL=float, QO_CRPOW=1 (prefix qo32cr_): the same with a correctly
+ *       rounded power function, the rounding of the GPU's exact kernels;
  *   QO_REAL=double (prefix qo64_): the FP64 oracle — the same algorithm with
  *       every quantity in double, used to state the error of each GPU form.
  *
@@ -47,6 +49,17 @@ typedef QO_REAL R;
 #define RFLOOR(x) floor(x)
 #define RFABS(x) fabs(x)
 #define RPOW(x, y) pow((x), (y))
+#elif QO_CRPOW
+/* FP32 parity arithmetic with a correctly rounded power (the double-precision
+ * pow narrowed to float), the rounding the GPU's exact kernels use.  glibc's
+ * powf (what the reference's host build calls) misses correct rounding in
+ * ~6e-4 of calls; on the reference's loose tolerance that flips some
+ * accept/reject decisions. */
+#define PFX(n) qo32cr_##n
+#define RSQRT_(x) sqrtf(x)
+#define RFLOOR(x) floorf(x)
+#define RFABS(x) fabsf(x)
+#define RPOW(x, y) ((float)pow((double)(x), (double)(y)))
 #else
 #define PFX(n) qo32_##n
 #define RSQRT_(x) sqrtf(x)

@@ -123,8 +123,12 @@ def test_notebook_workflow_through_dropin(cuda):
     _, Q_final = FastQSL.QMerge(Q, Qcut, arrs[17])
     got = Q_final.cpu().numpy()
     ref = g["Q_final"]
-    nan_same = np.isnan(got) == np.isnan(ref)
-    assert nan_same.mean() >= 0.999
+    flags_same = ((flag_start.cpu().numpy() == g["main_flag_start"]) &
+                  (flag_end.cpu().numpy() == g["main_flag_end"])).mean()
+    assert flags_same >= 0.999, flags_same
+    # one differing flag changes the NaN mask of at most 5 pixels
+    nan_same = (np.isnan(got) == np.isnan(ref)).mean()
+    assert nan_same >= 1.0 - 5.0 * (1.0 - flags_same) - 1e-9, (nan_same, flags_same)
     ok = ~np.isnan(got) & ~np.isnan(ref)
     d = np.abs(np.log10(got[ok]) - np.log10(ref[ok]))
     assert np.median(d) <= 1e-6 and np.quantile(d, 0.99) <= 1e-2, (np.median(d), np.quantile(d, 0.99))
@@ -138,10 +142,8 @@ def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     Bx, By, Bz = S.make_field(spec)
     n0, n1 = 40, 48
     zs = [0.0, 6.0, 13.5]
-    xs, ys, zz = api.plane_seed_grid(4.0, 75.0, n1, 4.0, 67.0, n0, zs)
-    stride = (75.0 - 4.0) / (n1 - 1)
-    stride_y = (67.0 - 4.0) / (n0 - 1)
-    assert abs(stride - stride_y) < 1e-6
+    stride = 1.5
+    xs, ys, zz = api.plane_seed_grid(4.0, 4.0 + stride * (n1 - 1), n1, 4.0, 4.0 + stride * (n0 - 1), n0, zs)
     prm = P.absolute_rkf45()
     fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout=layout)
     plan = api.QMapPlan(n0, n1, len(zs))
