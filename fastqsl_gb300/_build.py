@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NO_FMA = {"trace_exact.cu", "qassembly.cu"}
-SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast.cu", "field_store.cu", "qassembly.cu"]
+SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast.cu", "field_store.cu", "qassembly.cu", "noalloc.cu"]
 
 
 def _deps():

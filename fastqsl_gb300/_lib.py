@@ -57,6 +57,8 @@ _SIGS = {
     "qsl_qcalc_plane": (c_int, [_P] * 13 + [c_int, c_int, c_i64, c_double, _P, _P, _P, _P]),
     "qsl_cook_workspace_bytes": (c_i64, [c_i64]),
     "qsl_cook_pseudo_line": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 8 + [c_i64, _P]),
+    "qsl_cook_noalloc_max_pixels": (c_i64, []),
+    "qsl_cook_pseudo_line_noalloc": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 7 + [_P]),
     "qsl_qcut": (c_int, [_P] * 10 + [c_i64, _P, c_i64, c_double, _P, _P, _P]),
     "qsl_qmerge": (c_int, [_P, _P, _P, c_i64, _P, c_i64, c_int, c_int, _P, _P, _P]),
 }

@@ -36,6 +36,10 @@ static int cuda_fail(cudaError_t e, const char* what) {
 
 namespace qsl {
 
+// Lets other translation units of the library report an error through
+// qsl_last_error().
+int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 int persistent_grid(const void* kernel, int block, size_t smem) {
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;

@@ -234,6 +234,31 @@ int qsl_cook_pseudo_line(const int *B_flag, const float *x_start, const float *y
                          float *Bz0_start, float *Bz0_end, int64_t *pix, unsigned long long *count_dev,
                          void *workspace, int64_t workspace_bytes, qsl_stream_t stream);
 
+/* qsl_cook_pseudo_line without a workspace argument.  This entry has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory: a host application whose allocator has reserved the GPU's
+ * memory for its own pool (nothing is left to cudaMalloc, and the pool is not
+ * exposed to plug-ins), and language bindings that only receive borrowed
+ * device pointers from their host runtime and have no device allocator of
+ * their own.  The compaction scratch (12 bytes per 1024 pixels) is a fixed
+ * array of QSL_NOALLOC_SCRATCH_BYTES inside this library, present on every
+ * GPU that loads the library until the process exits; n is limited to
+ * qsl_cook_noalloc_max_pixels() (about 358 million pixels) and larger
+ * requests return QSL_ERR_TOO_LARGE.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls on a device
+ * share the one array: calls whose work overlaps on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  The
+ * entry allocates nothing: no cudaMalloc, cudaFree or allocating library
+ * routine.  Outputs and count_dev are as for qsl_cook_pseudo_line. */
+#define QSL_NOALLOC_SCRATCH_BYTES (4LL << 20)
+int64_t qsl_cook_noalloc_max_pixels(void);
+int qsl_cook_pseudo_line_noalloc(const int *B_flag, const float *x_start, const float *y_start, const float *z_start,
+                                 const int *flag_start, const float *Bz_in, const float *Bz_out, int64_t n, int n0,
+                                 int n1, int interior_only, float stride, float *cut_x, float *cut_y, float *cut_z,
+                                 float *Bz0_start, float *Bz0_end, int64_t *pix, unsigned long long *count_dev,
+                                 qsl_stream_t stream);
+
 /* Replaces demo/Q_RKF45CuPy.ipynb cell 10: Q of each pseudo-line pixel from
  * its 4 traced pseudo-lines; jac_scale = (1/(2*stride))^4.  The pixel count
  * is `count`, or *count_dev when set (then max_count bounds the launch). */
