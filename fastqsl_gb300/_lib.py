@@ -32,6 +32,13 @@ class TraceIO(ctypes.Structure):
         "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist")]
 
 
+class ScottIO(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "inp_x", "inp_y", "inp_z", "start_x", "start_y", "start_z", "flag_start",
+        "end_x", "end_y", "end_z", "flag_end", "B_this_x", "B_this_y", "B_this_z", "q_0", "q_perp",
+        "LineLen", "twist")]
+
+
 class Sched(ctypes.Structure):
     _fields_ = [("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32), ("order", ctypes.c_void_p),
                 ("queue", ctypes.c_void_p), ("samples", ctypes.c_void_p), ("occupancy", ctypes.c_int32)]
@@ -48,6 +55,9 @@ _SIGS = {
     "qsl_trace_all_bline": (c_int, [c_int, c_int] + [_P] * 35 + [c_i64, _P]),
     "qsl_trace_all_bline_rkf45": (c_int, [_P] * 35 + [_P]),
     "qsl_trace_all_bline_rk4": (c_int, [_P] * 34 + [_P]),
+    "qsl_params_reference_scott": (None, [_P]),
+    "qsl_trace_all_bline_scott": (c_int, [_P] * 30 + [c_i64, _P]),
+    "qsl_trace_scott": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, c_int, _P, _P]),
     "qsl_field_store_bytes": (c_i64, [c_int, c_int, c_int, c_int]),
     "qsl_field_create": (c_int, [_P, _P, _P, c_int, c_int, c_int, c_int, _P, _P]),
     "qsl_field_destroy": (c_int, [_P]),

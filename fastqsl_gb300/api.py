@@ -178,6 +178,48 @@ def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda"):
     return torch.argsort(key.reshape(-1)).to(torch.int32)
 
 
+SCOTT_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "B_this_x", "B_this_y", "B_this_z",
+             "q_0", "q_perp"]
+GRAD_MODES = {"fd": 0, "analytic": 1}
+
+
+def alloc_scott_outputs(n, device="cuda", twist=False):
+    out = {k: torch.zeros(n, dtype=torch.float32, device=device) for k in SCOTT_F32}
+    out["flag_start"] = torch.zeros(n, dtype=torch.int32, device=device)
+    out["flag_end"] = torch.zeros(n, dtype=torch.int32, device=device)
+    out["LineLen"] = torch.zeros(n, dtype=torch.float64, device=device)
+    out["twist"] = torch.zeros(n, dtype=torch.float64, device=device) if twist else None
+    return out
+
+
+def trace_scott(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_len=0.25, tol_coef=1.0,
+                curB=None, grad="analytic", out=None, n=None, n_dev=None, samples=None, order=None, stream=None):
+    """Scott deviation-vector tracer: footpoints, flags, q_0 and q_perp per
+    seed (reference: fastqslpy/cu/TraceBlineScott.cu:334-595).  grad:
+    'fd' (the reference's central differences) or 'analytic' (exact
+    trilinear derivative, fast arithmetic only)."""
+    from .params import reference_scott, ARITH_FAST
+    lib = _lib.load()
+    if params is None:
+        params = reference_scott(arith=ARITH_FAST)
+    n = int(xs.shape[0]) if n is None else int(n)
+    if out is None:
+        out = alloc_scott_outputs(n, xs.device, twist=curB is not None)
+    if curB is not None and out.get("twist") is None:
+        out["twist"] = torch.zeros(out["LineLen"].shape[0], dtype=torch.float64, device=xs.device)
+    io = _lib.ScottIO()
+    io.inp_x, io.inp_y, io.inp_z = ptr(xs), ptr(ys), ptr(zs)
+    for k in SCOTT_F32 + ["flag_start", "flag_end", "LineLen"]:
+        setattr(io, k, ptr(out[k]))
+    io.twist = ptr(out.get("twist"))
+    cur = [ptr(c) for c in curB] if curB is not None else [None, None, None]
+    sc = _lib.Sched(SCHEDULES["static"], 0, ptr(order), None, ptr(samples), 0)
+    _lib.check(lib.qsl_trace_scott(field.handle, ctypes.byref(params), ctypes.byref(io), n, ptr(n_dev),
+                                   float(s_len), float(tol_coef), *cur, GRAD_MODES[grad], ctypes.byref(sc),
+                                   stream_handle(stream)), "qsl_trace_scott")
+    return out
+
+
 class QMapPlan:
     """Device buffers and launch sequence of the Q pipeline for `nplanes`
     stacked (n0, n1) seed planes (rows along y, columns along x):
@@ -277,7 +319,8 @@ class QMapPlan:
                                             self.work_bytes, st), "qsl_cook_pseudo_line")
         cnt_seeds = self.count[1:2]
         trace(field, self.cut[0], self.cut[1], self.cut[2], params, s_len, tol_coef * pseudo_tol_factor, cross_dir,
-              out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds,
+              out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds, schedule="static",
+              occupancy=self.occupancy_for(field),
               samples=self.samples_buf[1:2] if count_samples else None, queue=self.queue[1:2],
               stream=stream)
         s = self.sub

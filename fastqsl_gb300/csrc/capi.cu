@@ -309,7 +309,6 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
     if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
     if (schedule != QSL_SCHED_QUEUE && schedule != QSL_SCHED_STATIC)
         return fail(QSL_ERR_INVALID, "bad schedule %d", schedule);
-    if (schedule == QSL_SCHED_STATIC && n_dev) return fail(QSL_ERR_INVALID, "static schedule needs a host count");
     const bool twist = curBx != nullptr;
     if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
     if (field->layout != LAYOUT_SOA && prm->arith == QSL_ARITH_EXACT)
@@ -432,9 +431,136 @@ int qsl_trace_all_bline_rk4(const float* Bx, const float* By, const float* Bz, c
                                B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len, N, LineLen, nullptr, -1, stream);
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Scott deviation-vector tracer
+// ---------------------------------------------------------------------------
+static bool scott_io_ok(const qsl_scott_io* io) {
+    return io && io->inp_x && io->inp_y && io->inp_z && io->start_x && io->start_y && io->start_z &&
+           io->flag_start && io->end_x && io->end_y && io->end_z && io->flag_end && io->B_this_x && io->B_this_y &&
+           io->B_this_z && io->q_0 && io->q_perp && io->LineLen;
+}
+
+template <class F>
+static void scott_fill(ScottJob<F>& J, const qsl_scott_io* io, const qsl_trace_params* prm) {
+    J.shape_dev = nullptr;
+    J.inp_x = io->inp_x; J.inp_y = io->inp_y; J.inp_z = io->inp_z;
+    ScottOut& o = J.o;
+    o.start_x = io->start_x; o.start_y = io->start_y; o.start_z = io->start_z; o.flag_start = io->flag_start;
+    o.end_x = io->end_x; o.end_y = io->end_y; o.end_z = io->end_z; o.flag_end = io->flag_end;
+    o.bthis_x = io->B_this_x; o.bthis_y = io->B_this_y; o.bthis_z = io->B_this_z;
+    o.q0 = io->q_0; o.qperp = io->q_perp; o.line_len = io->LineLen; o.twist = io->twist;
+    J.prm = *prm;
+    J.order = nullptr;
+    J.samples = nullptr;
+    memset(&J.s, 0, sizeof(J.s));
+    J.s.n_cap = -1;
+}
+
+extern "C" {
+
+int qsl_trace_scott(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_scott_io* io, int64_t n,
+                    const unsigned long long* n_dev, float s_len, float tol_coef, const float* curBx,
+                    const float* curBy, const float* curBz, int grad_mode, const qsl_sched* sched_h,
+                    qsl_stream_t stream) {
+    if (!field) return fail(QSL_ERR_INVALID, "field is null");
+    if (!params_ok(prm) || prm->integrator != QSL_RKF45)
+        return fail(QSL_ERR_INVALID, "bad trace params (the Scott tracer is RKF45)");
+    if (grad_mode != QSL_GRAD_FD && grad_mode != QSL_GRAD_ANALYTIC) return fail(QSL_ERR_INVALID, "bad grad_mode");
+    if (prm->arith == QSL_ARITH_EXACT && (grad_mode != QSL_GRAD_FD || field->layout != LAYOUT_SOA))
+        return fail(QSL_ERR_INVALID, "exact arithmetic needs the SoA layout and QSL_GRAD_FD");
+    if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
+    if (n == 0) return QSL_OK;
+    if (!scott_io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in scott io");
+    const bool twist = curBx != nullptr;
+    if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
+    qsl_sched sc{QSL_SCHED_STATIC, 0, nullptr, nullptr, nullptr, 0};
+    if (sched_h) sc = *sched_h;
+    if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
+    cudaStream_t st = (cudaStream_t)stream;
+    const FieldSoA cur{curBx, curBy, curBz, field->d};
+    cudaError_t e;
+    auto common = [&](auto& J) {
+        scott_fill(J, io, prm);
+        J.cur = cur;
+        J.order = sc.order;
+        J.samples = sc.samples;
+        J.s.s_len = s_len;
+        J.s.tol_coef = tol_coef;
+        J.s.n = n;
+        J.s.n_dev = n_dev;
+        J.s.n_cap = n_dev ? n : -1;
+        J.s.twist_on = twist ? 1 : 0;
+    };
+    if (field->layout == LAYOUT_SOA) {
+        ScottJob<FieldSoA> J;
+        J.f = FieldSoA{field->bx, field->by, field->bz, field->d};
+        common(J);
+        e = prm->arith == QSL_ARITH_EXACT ? launch_scott_exact(J, twist, n, st)
+                                          : launch_scott_fast_soa(J, grad_mode, twist, n, st);
+    } else if (field->layout == LAYOUT_F4) {
+        ScottJob<FieldF4> J;
+        J.f = FieldF4{field->f4, field->d};
+        common(J);
+        e = launch_scott_fast_f4(J, grad_mode, twist, n, st);
+    } else {
+        ScottJob<FieldH4B> J;
+        J.f = FieldH4B{field->bricks, field->scale, field->d, field->nbx, field->nby};
+        common(J);
+        e = launch_scott_fast_h4b(J, grad_mode, twist, n, st);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "scott launch");
+    return QSL_OK;
+}
+
+int qsl_trace_all_bline_scott(const float* Bx, const float* By, const float* Bz, const int* BshapeN,
+                              const float* curB_x, const float* curB_y, const float* curB_z, double* twist,
+                              const bool* curB_flag, const float* inp_x, const float* inp_y, const float* inp_z,
+                              const float* inp_cross_dir, float* start_x, float* start_y, float* start_z,
+                              int* flag_start, float* end_x, float* end_y, float* end_z, int* flag_end,
+                              float* B_this_x, float* B_this_y, float* B_this_z, float* q_0_arr, float* q_perp_arr,
+                              const float* s_len, const unsigned long long* N, double* LineLen,
+                              const float* tol_coef, int64_t capacity, qsl_stream_t stream) {
+    (void)inp_cross_dir;  // read by the reference kernel but unused by its Scott tracer
+    if (capacity == 0) return QSL_OK;
+    if (!Bx || !By || !Bz || !BshapeN || !s_len || !N || !tol_coef)
+        return fail(QSL_ERR_INVALID, "null required pointer");
+    if (capacity < 0) return fail(QSL_ERR_INVALID, "capacity (the per-seed array length) is required");
+    qsl_scott_io io{inp_x, inp_y, inp_z, start_x, start_y, start_z, flag_start, end_x, end_y, end_z, flag_end,
+                    B_this_x, B_this_y, B_this_z, q_0_arr, q_perp_arr, LineLen, twist};
+    if (!scott_io_ok(&io)) return fail(QSL_ERR_INVALID, "null pointer in outputs");
+    qsl_trace_params prm;
+    qsl_params_reference_scott(&prm);
+    const bool twist_possible = curB_flag && curB_x && curB_y && curB_z && twist;
+    ScottJob<FieldSoA> J;
+    J.f = FieldSoA{Bx, By, Bz, Dims{2, 2, 2}};
+    scott_fill(J, &io, &prm);
+    J.shape_dev = BshapeN;
+    J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
+    J.s.s_len_dev = s_len;
+    J.s.tol_coef_dev = tol_coef;
+    J.s.n_dev = N;
+    J.s.n_cap = capacity;
+    J.s.twist_flag_dev = twist_possible ? curB_flag : nullptr;
+    const cudaError_t e = launch_scott_exact(J, twist_possible, capacity, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "scott launch");
+    return QSL_OK;
+}
+
+void qsl_params_reference_scott(qsl_trace_params* p) {
+    qsl_params_reference_rkf45(p);
+    p->tol_law = QSL_TOL_ABSOLUTE;
+    p->len_ratio = 2.0;
+    p->max_steps = 10000;
+}
+
+}  // extern "C"
+
 // ---------------------------------------------------------------------------
 // Q assembly
 // ---------------------------------------------------------------------------
+extern "C" {
 int qsl_qcalc_plane(const float* x_end, const float* y_end, const float* z_end, const int* flag_end,
                     const float* x_start, const float* y_start, const float* z_start, const int* flag_start,
                     const float* Bz_in, const float* Bz_out, const float* Bx_0, const float* By_0,

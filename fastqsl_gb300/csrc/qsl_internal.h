@@ -3,6 +3,7 @@
 // include/fastqsl_gb300.h.
 #pragma once
 #include <cuda_runtime.h>
+#include "qsl_scott.cuh"
 #include "qsl_trace.cuh"
 
 namespace qsl {
@@ -26,6 +27,14 @@ cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Sched
 cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
                                  cudaStream_t st);
 cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st);
+
+// Scott tracer (one line per thread); exact arithmetic uses GRAD_FD
+cudaError_t launch_scott_exact(const ScottJob<FieldSoA>& J, bool twist, long long n_grid, cudaStream_t st);
+cudaError_t launch_scott_fast_soa(const ScottJob<FieldSoA>& J, int grad, bool twist, long long n_grid,
+                                  cudaStream_t st);
+cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid, cudaStream_t st);
+cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool twist, long long n_grid,
                                   cudaStream_t st);
 
 // field_store.cu

@@ -38,4 +38,21 @@ cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule
     return cudaGetLastError();
 }
 
+template <bool TWIST>
+__global__ void __launch_bounds__(kTraceBlock) k_scott_exact(const ScottJob<FieldSoA> J) {
+    scott_kernel_body<true, GRAD_FD, TWIST>(J);
+}
+
+static int grid_for_lines(long long n) {
+    long long g = (n + kTraceBlock - 1) / kTraceBlock;
+    return (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
+}
+
+cudaError_t launch_scott_exact(const ScottJob<FieldSoA>& J, bool twist, long long n_grid, cudaStream_t st) {
+    const int grid = grid_for_lines(n_grid);
+    if (twist) k_scott_exact<true><<<grid, kTraceBlock, 0, st>>>(J);
+    else k_scott_exact<false><<<grid, kTraceBlock, 0, st>>>(J);
+    return cudaGetLastError();
+}
+
 }  // namespace qsl

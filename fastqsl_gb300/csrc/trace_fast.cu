@@ -48,6 +48,37 @@ static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched,
     }
 }
 
+template <int GRAD, bool TWIST, class F>
+__global__ void __launch_bounds__(kTraceBlock) k_scott_fast(const ScottJob<F> J) {
+    scott_kernel_body<false, GRAD, TWIST>(J);
+}
+
+template <class F>
+static cudaError_t launch_scott(const ScottJob<F>& J, int grad, bool twist, long long n_grid, cudaStream_t st) {
+    long long g = (n_grid + kTraceBlock - 1) / kTraceBlock;
+    const int grid = (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
+    if (grad == GRAD_ANALYTIC) {
+        if (twist) k_scott_fast<GRAD_ANALYTIC, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_scott_fast<GRAD_ANALYTIC, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+    } else {
+        if (twist) k_scott_fast<GRAD_FD, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_scott_fast<GRAD_FD, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scott_fast_soa(const ScottJob<FieldSoA>& J, int grad, bool twist, long long n_grid,
+                                  cudaStream_t st) {
+    return launch_scott(J, grad, twist, n_grid, st);
+}
+cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid, cudaStream_t st) {
+    return launch_scott(J, grad, twist, n_grid, st);
+}
+cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool twist, long long n_grid,
+                                  cudaStream_t st) {
+    return launch_scott(J, grad, twist, n_grid, st);
+}
+
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
                                   cudaStream_t st) {
     return launch_fast(J, twist, sched, n_host, st);

@@ -29,7 +29,8 @@ def _current_stream(args):
     return torch.cuda.current_stream().cuda_stream
 
 
-# argument positions of the per-seed arrays (inputs and outputs)
+# argument positions of the per-seed arrays: inp_x/y/z (9-11), start ..
+# B_end_z (13-30), LineLen (33)
 _PER_SEED = [9, 10, 11] + list(range(13, 31)) + [33]
 
 
@@ -62,6 +63,33 @@ class TraceAllBline:
         st = stream if stream is not None else _current_stream(args)
         lib = _lib.load()
         _lib.check(lib.qsl_trace_all_bline(self.integrator, _ARITH[self.arith], *p, cap, st), "TraceAllBline")
+
+
+class TraceAllBlineScott:
+    """The Scott kernel TraceAllBlineScott (TraceBlineScott.cu:521-528, 30
+    arguments), which the reference's Scott notebooks compile themselves;
+    exact arithmetic, central-difference gradient."""
+
+    # inp_x/y/z (9-11), start..q_perp (13-25), LineLen (28)
+    _PER_SEED = [9, 10, 11] + list(range(13, 26)) + [28]
+
+    def __init__(self):
+        _lib.load()
+
+    def __call__(self, grid, block, args, shared_mem=0, stream=None):
+        args = tuple(args)
+        if len(args) < 30:
+            raise TypeError(f"TraceAllBlineScott takes 30 arguments, got {len(args)}")
+        cap = min(_numel(args[i]) for i in self._PER_SEED)
+        p = [ptr(a) if _numel(a) else None for a in args[:30]]
+        st = stream if stream is not None else _current_stream(args)
+        _lib.check(_lib.load().qsl_trace_all_bline_scott(*p, cap, st), "TraceAllBlineScott")
+
+
+def compileTraceBlineScott():
+    """Scott deviation-vector tracer (reference notebooks compile
+    fastqslpy/cu/TraceBlineScott.cu and take TraceAllBlineScott)."""
+    return TraceAllBlineScott()
 
 
 def compileTraceBlineAdaptive(arith="exact"):

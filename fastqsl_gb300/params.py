@@ -58,6 +58,8 @@ def reference_rkf45(arith=ARITH_EXACT) -> TraceParams:
 
 
 def reference_scott(arith=ARITH_EXACT) -> TraceParams:
+    """The Scott tracer's settings; its tolerance is 1e-3*tol_coef (the
+    reference leaves the variable uninitialised, TraceBlineScott.cu:352,378)."""
     return TraceParams(RKF45, TOL_ABSOLUTE, 1e-3, 0.1, 100.0, 0.618, 2.0, 10000, 0, arith)
 
 

@@ -163,7 +163,7 @@ int qsl_field_update(qsl_field_t *field, const float *Bx, const float *By, const
  * ------------------------------------------------------------------------ */
 enum qsl_schedule {
     QSL_SCHED_QUEUE = 0, /* persistent grid, per-lane refill from a device work counter */
-    QSL_SCHED_STATIC = 1 /* one line per thread (needs the host count) */
+    QSL_SCHED_STATIC = 1 /* one line per thread; the grid covers n (with n_dev set, n is the capacity) */
 };
 
 typedef struct qsl_trace_io {
@@ -202,6 +202,54 @@ int qsl_trace(const qsl_field_t *field, const qsl_trace_params *params_h, const 
               const unsigned long long *n_dev, float s_len, float tol_coef, const float *cross_dir_h,
               const float *curBx, const float *curBy, const float *curBz, const qsl_sched *sched_h,
               qsl_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Scott deviation-vector tracer: position plus two deviation vectors along
+ * each line (RKF45 on 9 components), Q from the deviation vectors at both
+ * footpoints (q_0: face-projected, q_perp: perpendicular-projected).
+ * ------------------------------------------------------------------------ */
+enum qsl_grad_mode {
+    QSL_GRAD_FD = 0,       /* grad(B/|B|) by +-1e-3 central differences (reference) */
+    QSL_GRAD_ANALYTIC = 1  /* exact derivative of the trilinear unit field, one cell fetch */
+};
+
+typedef struct qsl_scott_io {
+    const float *inp_x, *inp_y, *inp_z;
+    float *start_x, *start_y, *start_z;
+    int *flag_start;
+    float *end_x, *end_y, *end_z;
+    int *flag_end;
+    float *B_this_x, *B_this_y, *B_this_z;
+    float *q_0, *q_perp;
+    double *LineLen;
+    double *twist; /* needed when curB is given */
+} qsl_scott_io;
+
+/* Reference settings of the Scott tracer (TraceBlineScott.cu:10-14): absolute
+ * tolerance 1e-3*tol_coef (its tolerance variable is never initialised,
+ * :352,378), length limit 2*(nx+ny+nz), 10000 steps over both directions. */
+void qsl_params_reference_scott(qsl_trace_params *p_h);
+
+/* Replaces TraceAllBlineScott (fastqslpy/cu/TraceBlineScott.cu:521-528),
+ * compiled at run time by the reference's Scott notebooks: same 30 arguments
+ * in order, plus capacity (the length of the per-seed arrays; required) and
+ * the stream.  Exact arithmetic, central-difference gradient. */
+int qsl_trace_all_bline_scott(const float *Bx, const float *By, const float *Bz, const int *BshapeN,
+                              const float *curB_x, const float *curB_y, const float *curB_z, double *twist,
+                              const bool *curB_flag, const float *inp_x, const float *inp_y, const float *inp_z,
+                              const float *inp_cross_dir, float *start_x, float *start_y, float *start_z,
+                              int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                              float *B_this_x, float *B_this_y, float *B_this_z, float *q_0_arr, float *q_perp_arr,
+                              const float *s_len, const unsigned long long *N, double *LineLen,
+                              const float *tol_coef, int64_t capacity, qsl_stream_t stream);
+
+/* Native Scott entry: any store, exact (SoA + QSL_GRAD_FD only) or fast
+ * arithmetic, either gradient.  sched_h: order / samples are used (the
+ * schedule is one line per thread). */
+int qsl_trace_scott(const qsl_field_t *field, const qsl_trace_params *params_h, const qsl_scott_io *io_h,
+                    int64_t n, const unsigned long long *n_dev, float s_len, float tol_coef, const float *curBx,
+                    const float *curBy, const float *curBz, int grad_mode, const qsl_sched *sched_h,
+                    qsl_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Q assembly.

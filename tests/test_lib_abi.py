@@ -44,7 +44,8 @@ def test_every_declared_symbol_is_exported(lib):
 def test_reference_presets_match_python(lib):
     from fastqsl_gb300 import params as P
     for cfn, pfn in ((lib.qsl_params_reference_rk4, P.reference_rk4), (lib.qsl_params_reference_rkf45,
-                                                                        P.reference_rkf45)):
+                                                                        P.reference_rkf45),
+                     (lib.qsl_params_reference_scott, P.reference_scott)):
         c = P.TraceParams()
         cfn(ctypes.byref(c))
         assert c.as_dict() == pfn().as_dict()
