@@ -32,6 +32,16 @@ class TraceIO(ctypes.Structure):
         "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist")]
 
 
+class BatchJob(ctypes.Structure):
+    pass  # fields set below (needs TraceParams and TraceIO)
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("jobs_offset", ctypes.c_int64 * 3), ("begin_offset", ctypes.c_int64 * 3),
+                ("total", ctypes.c_int64 * 3), ("njobs", ctypes.c_int32 * 3), ("twist", ctypes.c_int32 * 3),
+                ("table_bytes", ctypes.c_int64), ("lines", ctypes.c_int64)]
+
+
 class ScottIO(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "inp_x", "inp_y", "inp_z", "start_x", "start_y", "start_z", "flag_start",
@@ -43,6 +53,16 @@ class Sched(ctypes.Structure):
     _fields_ = [("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32), ("order", ctypes.c_void_p),
                 ("queue", ctypes.c_void_p), ("samples", ctypes.c_void_p), ("occupancy", ctypes.c_int32)]
 
+
+def _finish_batch_job():
+    from .params import TraceParams
+    BatchJob._fields_ = [("field", ctypes.c_void_p), ("params", TraceParams), ("io", TraceIO),
+                         ("n", ctypes.c_int64), ("s_len", ctypes.c_float), ("tol_coef", ctypes.c_float),
+                         ("cross_dir", ctypes.c_float * 3), ("curB", ctypes.c_void_p * 3),
+                         ("order", ctypes.c_void_p), ("n_dev", ctypes.c_void_p)]
+
+
+_finish_batch_job()
 
 # name -> (restype, argtypes); every pointer is c_void_p
 _P = c_vp
@@ -56,6 +76,12 @@ _SIGS = {
     "qsl_trace_all_bline_rkf45": (c_int, [_P] * 35 + [_P]),
     "qsl_trace_all_bline_rk4": (c_int, [_P] * 34 + [_P]),
     "qsl_params_reference_scott": (None, [_P]),
+    "qsl_batch_pack": (c_int, [_P, c_int, _P, c_i64, _P]),
+    "qsl_batch_run": (c_int, [_P, _P, _P, _P]),
+    "qsl_batch_create": (c_int, [_P, c_int, _P, _P]),
+    "qsl_batch_launch": (c_int, [_P, _P, _P]),
+    "qsl_batch_lines": (c_i64, [_P]),
+    "qsl_batch_destroy": (c_int, [_P]),
     "qsl_trace_all_bline_scott": (c_int, [_P] * 30 + [c_i64, _P]),
     "qsl_trace_scott": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, c_int, _P, _P]),
     "qsl_field_store_bytes": (c_i64, [c_int, c_int, c_int, c_int]),

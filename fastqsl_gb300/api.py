@@ -345,3 +345,147 @@ def plane_seed_grid(x0, x1, nx, y0, y1, ny, zs, device="cuda"):
     Y = yi.view(1, ny, 1).expand(npl, ny, nx)
     Z = zt.view(npl, 1, 1).expand(npl, ny, nx)
     return X.reshape(-1).contiguous(), Y.reshape(-1).contiguous(), Z.reshape(-1).contiguous()
+
+
+class BatchPlan:
+    """Many trace jobs in one launch per field-store type.
+
+    jobs: list of dicts with keys field (FieldStore), xs, ys, zs, params,
+    s_len, tol_coef, cross_dir, out (trace output dict), optional order,
+    n_dev (device seed count; then n = capacity) and n.  The job table is
+    serialised once (qsl_batch_pack) into pinned host memory and copied
+    asynchronously to the device on `stream`; launch() only launches kernels
+    (qsl_batch_run), so it can be captured into a CUDA graph.  Nothing here
+    synchronises the device."""
+
+    def __init__(self, jobs, stream=None, device="cuda"):
+        lib = _lib.load()
+        arr = (_lib.BatchJob * max(1, len(jobs)))()
+        self._keep = []
+        for k, j in enumerate(jobs):
+            b = arr[k]
+            b.field = j["field"].handle
+            b.params = j["params"]
+            b.io = _io(j["xs"], j["ys"], j["zs"], j["out"])
+            b.n = int(j.get("n", j["xs"].shape[0]))
+            b.s_len = float(j.get("s_len", 0.25))
+            b.tol_coef = float(j.get("tol_coef", 1.0))
+            for c in range(3):
+                b.cross_dir[c] = float(j.get("cross_dir", (0.0, 0.0, 1.0))[c])
+            b.order = ptr(j.get("order"))
+            b.n_dev = ptr(j.get("n_dev"))
+            self._keep.append(j)
+        info = _lib.BatchInfo()
+        _lib.check(lib.qsl_batch_pack(arr, len(jobs), None, 0, ctypes.byref(info)), "qsl_batch_pack")
+        nbytes = max(256, int(info.table_bytes))
+        self._host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        _lib.check(lib.qsl_batch_pack(arr, len(jobs), self._host.data_ptr(), nbytes, ctypes.byref(info)),
+                   "qsl_batch_pack")
+        self._dev = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        if stream is not None and isinstance(stream, torch.cuda.Stream):
+            with torch.cuda.stream(stream):
+                self._dev.copy_(self._host, non_blocking=True)
+        else:
+            self._dev.copy_(self._host, non_blocking=True)
+        self.info = info
+        self.lines = int(info.lines)
+
+    def launch(self, samples=None, stream=None):
+        _lib.check(_lib.load().qsl_batch_run(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
+                                             stream_handle(stream)), "qsl_batch_run")
+
+
+class QBatch:
+    """Q maps of many independent jobs (each: a resident field, a stack of
+    (n0, n1) seed planes on arbitrary planes, its own integrator settings)
+    solved together: one batched main-trace launch, per-job Q assembly and
+    pseudo-line compaction, one batched pseudo-line launch, per-job pseudo Q
+    and merge.  All buffers are allocated up front; run() issues only
+    kernels, so it can be captured once into a CUDA graph (capture()) and
+    replayed.  Reference workflow per job: demo/Q_RKF45CuPy.ipynb cells 7-11.
+
+    specs: list of dicts with keys field, xs, ys, zs (flattened stacked
+    planes), n0, n1, nplanes, params, s_len, tol_coef, stride, cross_dir."""
+
+    def __init__(self, specs, device="cuda", tile=(8, 8), stream=None):
+        self.specs = specs
+        lib = _lib.load()
+        self.jobs = []
+        main_jobs, sub_jobs = [], []
+        for sp in specs:
+            n0, n1, npl = int(sp["n0"]), int(sp["n1"]), int(sp.get("nplanes", 1))
+            n = n0 * n1 * npl
+            m = npl * (n0 - 2) * (n1 - 2)
+            J = dict(sp=sp, n0=n0, n1=n1, npl=npl, n=n, m=m)
+            J["main"] = alloc_trace_outputs(n, device)
+            J["order"] = tile_order(npl, n0, n1, tile[0], tile[1], device) if tile else None
+            J["Q"] = torch.empty((npl, n0 - 2, n1 - 2), dtype=torch.float64, device=device)
+            J["cut"] = [torch.empty(4 * m, dtype=torch.float32, device=device) for _ in range(3)]
+            J["bz0s"] = torch.empty(m, dtype=torch.float32, device=device)
+            J["bz0e"] = torch.empty(m, dtype=torch.float32, device=device)
+            J["pix"] = torch.empty(m, dtype=torch.int64, device=device)
+            J["count"] = torch.zeros(2, dtype=torch.int64, device=device)
+            wb = int(lib.qsl_cook_workspace_bytes(n))
+            J["work"] = torch.empty((wb + 7) // 8, dtype=torch.int64, device=device)
+            J["work_bytes"] = wb
+            J["sub"] = alloc_trace_outputs(4 * m, device)
+            J["qcut"] = torch.empty(m, dtype=torch.float64, device=device)
+            common = dict(field=sp["field"], params=sp["params"], s_len=sp.get("s_len", 0.25),
+                          tol_coef=sp.get("tol_coef", 1.0), cross_dir=sp.get("cross_dir", (0.0, 0.0, 1.0)))
+            main_jobs.append(dict(common, xs=sp["xs"], ys=sp["ys"], zs=sp["zs"], out=J["main"], order=J["order"]))
+            sub_jobs.append(dict(common, xs=J["cut"][0], ys=J["cut"][1], zs=J["cut"][2], out=J["sub"],
+                                 n=4 * m, n_dev=J["count"][1:2]))
+            self.jobs.append(J)
+        self.main_batch = BatchPlan(main_jobs, stream=stream)
+        self.sub_batch = BatchPlan(sub_jobs, stream=stream)
+        self.graph = None
+
+    def run(self, stream=None):
+        lib = _lib.load()
+        st = stream_handle(stream)
+        self.main_batch.launch(stream=stream)
+        for J in self.jobs:
+            sp, m = J["sp"], J["main"]
+            jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0
+            cd = (ctypes.c_float * 3)(*[float(c) for c in sp.get("cross_dir", (0.0, 0.0, 1.0))])
+            _lib.check(lib.qsl_qcalc_plane(ptr(m["end_x"]), ptr(m["end_y"]), ptr(m["end_z"]), ptr(m["flag_end"]),
+                                           ptr(m["start_x"]), ptr(m["start_y"]), ptr(m["start_z"]),
+                                           ptr(m["flag_start"]), ptr(m["B_start_z"]), ptr(m["B_end_z"]),
+                                           ptr(m["B_this_x"]), ptr(m["B_this_y"]), ptr(m["B_this_z"]), J["n0"],
+                                           J["n1"], J["npl"], jac, cd, None, ptr(J["Q"]), st), "qcalc_plane")
+            _lib.check(lib.qsl_cook_pseudo_line(ptr(m["B_flag"]), ptr(m["start_x"]), ptr(m["start_y"]),
+                                                ptr(m["start_z"]), ptr(m["flag_start"]), ptr(m["B_start_z"]),
+                                                ptr(m["B_end_z"]), J["n"], J["n0"], J["n1"], 1,
+                                                float(sp.get("stride", 1.0)), ptr(J["cut"][0]), ptr(J["cut"][1]),
+                                                ptr(J["cut"][2]), ptr(J["bz0s"]), ptr(J["bz0e"]), ptr(J["pix"]),
+                                                ptr(J["count"]), ptr(J["work"]), J["work_bytes"], st), "cook")
+        self.sub_batch.launch(stream=stream)
+        for J in self.jobs:
+            sp, s = J["sp"], J["sub"]
+            jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0
+            _lib.check(lib.qsl_qcut(ptr(s["start_x"]), ptr(s["start_y"]), ptr(s["start_z"]), ptr(s["flag_start"]),
+                                    ptr(s["end_x"]), ptr(s["end_y"]), ptr(s["end_z"]), ptr(s["flag_end"]),
+                                    ptr(J["bz0s"]), ptr(J["bz0e"]), 0, ptr(J["count"][0:1]), J["m"], jac, None,
+                                    ptr(J["qcut"]), st), "qcut")
+            _lib.check(lib.qsl_qmerge(ptr(J["pix"]), None, ptr(J["qcut"]), 0, ptr(J["count"][0:1]), J["m"],
+                                      J["n0"], J["n1"], None, ptr(J["Q"]), st), "qmerge")
+        return [J["Q"] for J in self.jobs]
+
+    def capture(self):
+        """Captures run() into a CUDA graph (replay with replay())."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.run(stream=s)  # warm-up outside capture
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+        return [J["Q"] for J in self.jobs]

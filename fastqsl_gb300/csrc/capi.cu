@@ -7,6 +7,7 @@
 
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "../../include/fastqsl_gb300.h"
 #include "qassembly.h"
@@ -429,6 +430,226 @@ int qsl_trace_all_bline_rk4(const float* Bx, const float* By, const float* Bz, c
                                curB_flag, inp_x, inp_y, inp_z, inp_cross_dir, start_x, start_y, start_z, flag_start,
                                end_x, end_y, end_z, flag_end, B_this_x, B_this_y, B_this_z, B_flag, B_start_x,
                                B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len, N, LineLen, nullptr, -1, stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched trace plans
+// ---------------------------------------------------------------------------
+struct qsl_batch {
+    int device;
+    // per store type: job table and warp-aligned line offsets in device memory
+    void* jobs[3];
+    long long* begin[3];
+    int njobs[3];
+    long long total[3];
+    bool twist[3];
+    int64_t lines;
+};
+
+template <class F>
+static TraceJob<F> batch_job_of(const qsl_batch_job& b, const F& f) {
+    TraceJob<F> J;
+    J.f = f;
+    fill_common(J, &b.io, &b.params, nullptr);
+    J.cur = FieldSoA{b.curB[0], b.curB[1], b.curB[2], f.d};
+    J.order = b.order;
+    J.s.s_len = b.s_len;
+    J.s.tol_coef = b.tol_coef;
+    J.s.n = b.n;
+    J.s.n_dev = b.n_dev;
+    J.s.cross[0] = b.cross_dir[0]; J.s.cross[1] = b.cross_dir[1]; J.s.cross[2] = b.cross_dir[2];
+    J.s.twist_on = b.curB[0] ? 1 : 0;
+    return J;
+}
+
+template <class F>
+static int batch_upload(qsl_batch* B, int slot, const std::vector<TraceJob<F>>& js, const std::vector<long long>& beg,
+                        bool twist, cudaStream_t st) {
+    B->njobs[slot] = (int)js.size();
+    B->total[slot] = beg.back();
+    B->twist[slot] = twist;
+    if (js.empty()) return QSL_OK;
+    QSL_CHECK_CUDA(cudaMalloc(&B->jobs[slot], js.size() * sizeof(TraceJob<F>)), "batch job table");
+    QSL_CHECK_CUDA(cudaMalloc((void**)&B->begin[slot], beg.size() * sizeof(long long)), "batch offsets");
+    QSL_CHECK_CUDA(cudaMemcpyAsync(B->jobs[slot], js.data(), js.size() * sizeof(TraceJob<F>),
+                                   cudaMemcpyHostToDevice, st), "batch upload");
+    QSL_CHECK_CUDA(cudaMemcpyAsync(B->begin[slot], beg.data(), beg.size() * sizeof(long long),
+                                   cudaMemcpyHostToDevice, st), "batch upload");
+    // the host vectors die on return: make sure the copies have read them
+    QSL_CHECK_CUDA(cudaStreamSynchronize(st), "batch upload");
+    return QSL_OK;
+}
+
+// Serialised batch table: per store type a TraceJob<F> array and its line
+// offsets, each at a 256-byte aligned offset of one buffer.
+static int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
+
+struct BatchLists {
+    std::vector<TraceJob<FieldSoA>> j0;
+    std::vector<TraceJob<FieldF4>> j1;
+    std::vector<TraceJob<FieldH4B>> j2;
+    std::vector<long long> b[3];
+    bool tw[3] = {false, false, false};
+    int64_t lines = 0;
+};
+
+static int batch_lists(const qsl_batch_job* jobs_h, int njobs, BatchLists& L) {
+    if (njobs < 0 || (njobs > 0 && !jobs_h)) return fail(QSL_ERR_INVALID, "bad job list");
+    for (int k = 0; k < 3; ++k) L.b[k] = std::vector<long long>{0};
+    for (int k = 0; k < njobs; ++k) {
+        const qsl_batch_job& b = jobs_h[k];
+        if (!b.field) return fail(QSL_ERR_INVALID, "job %d: null field", k);
+        if (!params_ok(&b.params) || b.params.arith != QSL_ARITH_FAST)
+            return fail(QSL_ERR_INVALID, "job %d: bad params (batched jobs use fast arithmetic)", k);
+        if (b.n < 0) return fail(QSL_ERR_INVALID, "job %d: negative n", k);
+        if (b.n > 0 && !io_ok(&b.io)) return fail(QSL_ERR_INVALID, "job %d: null pointer in io", k);
+        if (b.curB[0] && (!b.curB[1] || !b.curB[2] || !b.io.twist))
+            return fail(QSL_ERR_INVALID, "job %d: twist needs curB_x/y/z and twist", k);
+        if (b.order && b.n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "job %d: order map limits n", k);
+        const qsl_field* f = b.field;
+        const long long padded = (b.n + 31) / 32 * 32;
+        L.lines += b.n;
+        const int slot = f->layout == LAYOUT_SOA ? 0 : (f->layout == LAYOUT_F4 ? 1 : 2);
+        if (slot == 0) L.j0.push_back(batch_job_of(b, FieldSoA{f->bx, f->by, f->bz, f->d}));
+        else if (slot == 1) L.j1.push_back(batch_job_of(b, FieldF4{f->f4, f->d}));
+        else L.j2.push_back(batch_job_of(b, FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}));
+        L.b[slot].push_back(L.b[slot].back() + padded);
+        L.tw[slot] = L.tw[slot] || b.curB[0];
+    }
+    return QSL_OK;
+}
+
+static void batch_layout(const BatchLists& L, qsl_batch_info* info) {
+    const size_t jsz[3] = {sizeof(TraceJob<FieldSoA>), sizeof(TraceJob<FieldF4>), sizeof(TraceJob<FieldH4B>)};
+    const size_t nj[3] = {L.j0.size(), L.j1.size(), L.j2.size()};
+    int64_t off = 0;
+    for (int k = 0; k < 3; ++k) {
+        info->jobs_offset[k] = off;
+        off = align256(off + (int64_t)(nj[k] * jsz[k]));
+        info->begin_offset[k] = off;
+        off = align256(off + (int64_t)(L.b[k].size() * sizeof(long long)));
+        info->njobs[k] = (int32_t)nj[k];
+        info->twist[k] = L.tw[k] ? 1 : 0;
+        info->total[k] = L.b[k].back();
+    }
+    info->table_bytes = off;
+    info->lines = L.lines;
+}
+
+extern "C" {
+
+int qsl_batch_pack(const qsl_batch_job* jobs_h, int njobs, void* table_h, int64_t table_bytes,
+                   qsl_batch_info* info_h) {
+    if (!info_h) return fail(QSL_ERR_INVALID, "info is null");
+    BatchLists L;
+    int rc = batch_lists(jobs_h, njobs, L);
+    if (rc != QSL_OK) return rc;
+    batch_layout(L, info_h);
+    if (!table_h) return QSL_OK;  // size query
+    if (table_bytes < info_h->table_bytes) return fail(QSL_ERR_INVALID, "table buffer too small");
+    char* t = (char*)table_h;
+    memcpy(t + info_h->jobs_offset[0], L.j0.data(), L.j0.size() * sizeof(TraceJob<FieldSoA>));
+    memcpy(t + info_h->jobs_offset[1], L.j1.data(), L.j1.size() * sizeof(TraceJob<FieldF4>));
+    memcpy(t + info_h->jobs_offset[2], L.j2.data(), L.j2.size() * sizeof(TraceJob<FieldH4B>));
+    for (int k = 0; k < 3; ++k) memcpy(t + info_h->begin_offset[k], L.b[k].data(), L.b[k].size() * sizeof(long long));
+    return QSL_OK;
+}
+
+int qsl_batch_run(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
+                  qsl_stream_t stream) {
+    if (!table_dev || !info_h) return fail(QSL_ERR_INVALID, "null table or info");
+    const char* t = (const char*)table_dev;
+    cudaStream_t st = (cudaStream_t)stream;
+    const qsl_batch_info& I = *info_h;
+    QSL_CHECK_CUDA(launch_trace_batch_soa((const TraceJob<FieldSoA>*)(t + I.jobs_offset[0]),
+                                          (const long long*)(t + I.begin_offset[0]), I.njobs[0], I.total[0],
+                                          I.twist[0] != 0, samples_dev, st), "batch run");
+    QSL_CHECK_CUDA(launch_trace_batch_f4((const TraceJob<FieldF4>*)(t + I.jobs_offset[1]),
+                                         (const long long*)(t + I.begin_offset[1]), I.njobs[1], I.total[1],
+                                         I.twist[1] != 0, samples_dev, st), "batch run");
+    QSL_CHECK_CUDA(launch_trace_batch_h4b((const TraceJob<FieldH4B>*)(t + I.jobs_offset[2]),
+                                          (const long long*)(t + I.begin_offset[2]), I.njobs[2], I.total[2],
+                                          I.twist[2] != 0, samples_dev, st), "batch run");
+    return QSL_OK;
+}
+
+int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream, qsl_batch_t** out) {
+    if (!out) return fail(QSL_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (njobs < 0 || (njobs > 0 && !jobs_h)) return fail(QSL_ERR_INVALID, "bad job list");
+    std::vector<TraceJob<FieldSoA>> js0;
+    std::vector<TraceJob<FieldF4>> js1;
+    std::vector<TraceJob<FieldH4B>> js2;
+    std::vector<long long> b0{0}, b1{0}, b2{0};
+    bool tw[3] = {false, false, false};
+    int64_t lines = 0;
+    for (int k = 0; k < njobs; ++k) {
+        const qsl_batch_job& b = jobs_h[k];
+        if (!b.field) return fail(QSL_ERR_INVALID, "job %d: null field", k);
+        if (!params_ok(&b.params) || b.params.arith != QSL_ARITH_FAST)
+            return fail(QSL_ERR_INVALID, "job %d: bad params (batched jobs use fast arithmetic)", k);
+        if (b.n < 0) return fail(QSL_ERR_INVALID, "job %d: negative n", k);
+        if (b.n > 0 && !io_ok(&b.io)) return fail(QSL_ERR_INVALID, "job %d: null pointer in io", k);
+        if (b.curB[0] && (!b.curB[1] || !b.curB[2] || !b.io.twist))
+            return fail(QSL_ERR_INVALID, "job %d: twist needs curB_x/y/z and twist", k);
+        if (b.order && b.n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "job %d: order map limits n", k);
+        const qsl_field* f = b.field;
+        const long long padded = (b.n + 31) / 32 * 32;
+        lines += b.n;
+        if (f->layout == LAYOUT_SOA) {
+            js0.push_back(batch_job_of(b, FieldSoA{f->bx, f->by, f->bz, f->d}));
+            b0.push_back(b0.back() + padded);
+            tw[0] = tw[0] || b.curB[0];
+        } else if (f->layout == LAYOUT_F4) {
+            js1.push_back(batch_job_of(b, FieldF4{f->f4, f->d}));
+            b1.push_back(b1.back() + padded);
+            tw[1] = tw[1] || b.curB[0];
+        } else {
+            js2.push_back(batch_job_of(b, FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}));
+            b2.push_back(b2.back() + padded);
+            tw[2] = tw[2] || b.curB[0];
+        }
+    }
+    qsl_batch* B = new (std::nothrow) qsl_batch();
+    if (!B) return fail(QSL_ERR_NOMEM, "host allocation failed");
+    cudaGetDevice(&B->device);
+    B->lines = lines;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = batch_upload(B, 0, js0, b0, tw[0], st);
+    if (rc == QSL_OK) rc = batch_upload(B, 1, js1, b1, tw[1], st);
+    if (rc == QSL_OK) rc = batch_upload(B, 2, js2, b2, tw[2], st);
+    if (rc != QSL_OK) {
+        qsl_batch_destroy(B);
+        return rc;
+    }
+    *out = B;
+    return QSL_OK;
+}
+
+int qsl_batch_launch(const qsl_batch_t* B, unsigned long long* samples_dev, qsl_stream_t stream) {
+    if (!B) return fail(QSL_ERR_INVALID, "batch is null");
+    cudaStream_t st = (cudaStream_t)stream;
+    QSL_CHECK_CUDA(launch_trace_batch_soa((const TraceJob<FieldSoA>*)B->jobs[0], B->begin[0], B->njobs[0],
+                                          B->total[0], B->twist[0], samples_dev, st), "batch launch");
+    QSL_CHECK_CUDA(launch_trace_batch_f4((const TraceJob<FieldF4>*)B->jobs[1], B->begin[1], B->njobs[1],
+                                         B->total[1], B->twist[1], samples_dev, st), "batch launch");
+    QSL_CHECK_CUDA(launch_trace_batch_h4b((const TraceJob<FieldH4B>*)B->jobs[2], B->begin[2], B->njobs[2],
+                                          B->total[2], B->twist[2], samples_dev, st), "batch launch");
+    return QSL_OK;
+}
+
+int64_t qsl_batch_lines(const qsl_batch_t* B) { return B ? B->lines : 0; }
+
+int qsl_batch_destroy(qsl_batch_t* B) {
+    if (!B) return QSL_OK;
+    for (int k = 0; k < 3; ++k) {
+        cudaFree(B->jobs[k]);
+        cudaFree(B->begin[k]);
+    }
+    delete B;
+    return QSL_OK;
 }
 
 }  // extern "C"

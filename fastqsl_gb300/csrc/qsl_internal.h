@@ -3,6 +3,7 @@
 // include/fastqsl_gb300.h.
 #pragma once
 #include <cuda_runtime.h>
+#include "qsl_batch.cuh"
 #include "qsl_scott.cuh"
 #include "qsl_trace.cuh"
 
@@ -36,6 +37,14 @@ cudaError_t launch_scott_fast_soa(const ScottJob<FieldSoA>& J, int grad, bool tw
 cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid, cudaStream_t st);
 cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool twist, long long n_grid,
                                   cudaStream_t st);
+
+// Batched trace over a job table in device memory (trace_fast.cu)
+cudaError_t launch_trace_batch_soa(const TraceJob<FieldSoA>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st);
+cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs, long long total,
+                                  bool twist, unsigned long long* samples, cudaStream_t st);
+cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st);
 
 // field_store.cu
 cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);

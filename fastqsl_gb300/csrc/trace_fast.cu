@@ -79,6 +79,39 @@ cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool tw
     return launch_scott(J, grad, twist, n_grid, st);
 }
 
+// Batched trace: one line per thread, 8 resident blocks/SM (the register
+// budget measured best for the lockstep tracer).
+template <bool TWIST, class F>
+__global__ void __launch_bounds__(kTraceBlock, 8) k_trace_batch(const TraceJob<F>* __restrict__ jobs,
+                                                                 const long long* __restrict__ begin, int njobs,
+                                                                 unsigned long long* samples) {
+    batch_kernel_body<TWIST>(jobs, begin, njobs, samples);
+}
+
+template <class F>
+static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin, int njobs, long long total,
+                                bool twist, unsigned long long* samples, cudaStream_t st) {
+    if (njobs <= 0 || total <= 0) return cudaSuccess;
+    long long g = (total + kTraceBlock - 1) / kTraceBlock;
+    const int grid = (int)(g > (1 << 30) ? (1 << 30) : g);
+    if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
+    else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_batch_soa(const TraceJob<FieldSoA>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
+}
+cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs, long long total,
+                                  bool twist, unsigned long long* samples, cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
+}
+cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
+}
+
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
                                   cudaStream_t st) {
     return launch_fast(J, twist, sched, n_host, st);

@@ -196,3 +196,28 @@ def field_fingerprint(bx, by, bz) -> str:
             a = a.detach().cpu().numpy()
         h.update(np.ascontiguousarray(np.asarray(a).transpose(2, 1, 0)).tobytes())
     return h.hexdigest()[:16]
+
+
+def cutting_plane(shape, normal, n0, n1, spacing=None, center=None):
+    """Seeds on an arbitrarily oriented plane through `center` (default: box
+    centre) with unit normal `normal`: an (n0, n1) grid along two in-plane
+    axes u (columns) and v (rows), spacing chosen so the grid stays inside the
+    box unless given.  Returns float32 (x, y, z) of the flattened grid, the
+    normal (float32) and the spacing (the Q stride)."""
+    nx, ny, nz = shape
+    n = np.asarray(normal, np.float64)
+    n = n / np.linalg.norm(n)
+    e = np.eye(3)[int(np.argmin(np.abs(n)))]
+    u = np.cross(n, e)
+    u /= np.linalg.norm(u)
+    v = np.cross(n, u)
+    c = np.array([(nx - 1) / 2.0, (ny - 1) / 2.0, (nz - 1) / 2.0]) if center is None else np.asarray(center, float)
+    if spacing is None:
+        half = 0.45 * min(nx - 1, ny - 1, nz - 1)  # corners of the grid stay inside the box
+        spacing = 2 * half / (max(n0, n1) - 1) / np.sqrt(2.0)
+    a = (np.arange(n1) - (n1 - 1) / 2.0) * spacing
+    b = (np.arange(n0) - (n0 - 1) / 2.0) * spacing
+    B, A = np.meshgrid(b, a, indexing="ij")
+    pts = c[None, None, :] + A[..., None] * u[None, None, :] + B[..., None] * v[None, None, :]
+    pts = pts.reshape(-1, 3).astype(np.float32)
+    return pts[:, 0].copy(), pts[:, 1].copy(), pts[:, 2].copy(), n.astype(np.float32), float(spacing)

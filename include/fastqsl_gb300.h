@@ -204,6 +204,50 @@ int qsl_trace(const qsl_field_t *field, const qsl_trace_params *params_h, const 
               qsl_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Batched trace plans (no reference counterpart: the reference launches one
+ * kernel per seed set).  Many jobs — different fields (any store), seed
+ * sets, RK4/RKF45 settings — traced by one launch per store type, each job's
+ * lines in their own warp-aligned range.  qsl_batch_create uploads the job
+ * table once (synchronises `stream`); qsl_batch_launch only launches kernels,
+ * so it can be replayed or captured into a CUDA graph.  Jobs use fast
+ * arithmetic; outputs as qsl_trace.
+ * ------------------------------------------------------------------------ */
+typedef struct qsl_batch_job {
+    const qsl_field_t *field;
+    qsl_trace_params params;  /* arith must be QSL_ARITH_FAST */
+    qsl_trace_io io;
+    int64_t n;
+    float s_len;
+    float tol_coef;
+    float cross_dir[3];
+    const float *curB[3];     /* twist current density, or nulls */
+    const uint32_t *order;    /* optional seed visiting order (tile order) */
+    const unsigned long long *n_dev; /* optional: seed count on the device (<= n, which sizes the range) */
+} qsl_batch_job;
+typedef struct qsl_batch qsl_batch_t;
+
+/* Stateless form for callers that manage their own memory (a serving loop
+ * must not synchronise): qsl_batch_pack serialises the job table into a host
+ * buffer (table_h null: only fills info, including table_bytes); the caller
+ * copies those bytes to device memory (256-byte aligned) by any means and
+ * qsl_batch_run launches from it.  The table holds device addresses of the
+ * jobs' fields and buffers, which must stay valid until the run completes. */
+typedef struct qsl_batch_info {
+    int64_t jobs_offset[3], begin_offset[3], total[3];
+    int32_t njobs[3], twist[3];
+    int64_t table_bytes, lines;
+} qsl_batch_info;
+int qsl_batch_pack(const qsl_batch_job *jobs_h, int njobs, void *table_h, int64_t table_bytes,
+                   qsl_batch_info *info_h);
+int qsl_batch_run(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
+                  qsl_stream_t stream);
+
+int qsl_batch_create(const qsl_batch_job *jobs_h, int njobs, qsl_stream_t stream, qsl_batch_t **out_h);
+int qsl_batch_launch(const qsl_batch_t *batch, unsigned long long *samples_dev, qsl_stream_t stream);
+int64_t qsl_batch_lines(const qsl_batch_t *batch);
+int qsl_batch_destroy(qsl_batch_t *batch);
+
+/* ------------------------------------------------------------------------
  * Scott deviation-vector tracer: position plus two deviation vectors along
  * each line (RKF45 on 9 components), Q from the deviation vectors at both
  * footpoints (q_0: face-projected, q_perp: perpendicular-projected).
