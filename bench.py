@@ -288,6 +288,64 @@ def cpu_baseline(planes, threads=None):
             "sample": f"{npl} of {SUB['nz']} z-planes of the same cube ({qpix} Q-pixels), {dt:.1f} s"}
 
 
+def batched_graph(device, n_fields=64, seed=11, reps=3):
+    """64 independent fields (4-32 charges; 64^3, 128^3, 192x192x128 or 256^3;
+    fp16 bricks or float32 SoA), each with an arbitrarily oriented cutting
+    plane of 10^3-10^6 seeds (log-uniform), RK4 or RKF45; the whole Q pipeline
+    of all 64 captured once into a CUDA graph and replayed."""
+    import torch
+    from fastqsl_gb300 import api, params as P, synthetic as S
+    rng = np.random.default_rng(seed)
+    sizes = [(64, 64, 64), (128, 128, 128), (192, 192, 128), (256, 256, 256)]
+    specs, stores = [], []
+    for k in range(n_fields):
+        shape = sizes[int(rng.integers(len(sizes)))]
+        spec = S.charges_random(seed * 100 + k, shape, int(rng.integers(4, 33)))
+        B = S.make_field(spec, device=device, as_numpy=False)
+        fs = api.FieldStore(*B, layout="h4b" if rng.random() < 0.5 else "soa")
+        stores.append(fs)
+        total = float(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
+        n0 = max(3, int(np.sqrt(total)))
+        n1 = max(3, int(total / n0))
+        xs, ys, zs, nrm, stride = S.cutting_plane(shape, rng.normal(size=3), n0, n1)
+        rkf = rng.random() < 0.5
+        prm = P.absolute_rkf45(tol=1e-4) if rkf else P.fixed_rk4(arith=P.ARITH_FAST)
+        prm.max_steps = 20000 if not rkf else prm.max_steps
+        t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+        specs.append(dict(field=fs, xs=t(xs), ys=t(ys), zs=t(zs), n0=n0, n1=n1, nplanes=1, params=prm,
+                          s_len=0.25 if rkf else 0.1, stride=stride, cross_dir=tuple(float(c) for c in nrm)))
+    qb = api.QBatch(specs, device=device)
+    qb.capture()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        qb.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    qpix = sum((sp["n0"] - 2) * (sp["n1"] - 2) for sp in specs)
+    lines = sum(sp["n0"] * sp["n1"] for sp in specs)
+    out = {"fields": n_fields, "seeds": int(lines), "q_pixels": int(qpix), "graph_ms": ms,
+           "qpixels_per_s": qpix / (ms / 1e3)}
+    for fs in stores:
+        fs.close()
+    return out
+
+
+def serving_sweep(device, count=48):
+    """8 resident 384x384x256 fields; Poisson streams of Q-map requests
+    (10^4-4x10^6 seeds, tol 1e-3/1e-4/1e-5) at fractions of the saturated
+    rate; p50/p99 latency against each request's isolated solve."""
+    from fastqsl_gb300 import serving
+    fields = serving.make_fields(n_fields=8, shape=(384, 384, 256), device=device)
+    srv = serving.QServer(fields, hbm_budget=48 << 30, streams=3, max_batch=16)
+    out = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8))
+    for fs in fields.values():
+        fs.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -301,6 +359,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     args = ap.parse_args()
     NPLANES[0] = max(1, min(SUB["nz"], args.planes))
@@ -369,6 +429,12 @@ def main():
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]}
     if "accuracy" in res:
         line["accuracy_vs_fp64"] = res["accuracy"]
+    if not args.skip_batched:
+        import torch
+        line["batched_graph"] = batched_graph(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
+    if not args.skip_serving:
+        import torch
+        line["serving"] = serving_sweep(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(list(range(args.cpu_planes)))
     line["samples_per_step"] = res["samples_all"]

@@ -1,0 +1,326 @@
+"""Resident-field Q-map serving with continuous batching.
+
+Fields stay on the device (FieldStore).  Requests name a field, a stack of
+seed planes (an arbitrarily oriented plane, or several parallel ones = a
+sub-box) and an RKF45 tolerance.  The scheduler loop:
+
+* completes finished batches (a CUDA event per batch; results were copied to
+  pinned host memory on the batch's stream) and returns their memory to the
+  HBM budget;
+* admits waiting requests in arrival order while their device memory fits in
+  what the budget has left, up to `max_batch` per batch;
+* launches every newly admitted group as one batch (QBatch: one main-trace
+  launch and one pseudo-line launch for all of them) on the next of several
+  CUDA streams, so a batch starts while earlier ones are still on the GPU and
+  their work overlaps on the device.
+
+Nothing in the loop synchronises the device: allocations come from the
+caching allocator on the batch's stream, the job table is copied
+asynchronously from pinned memory, completion is polled.  A request's result
+does not depend on what it was batched with (each line is traced by one
+thread with its job's settings; tests check alone == in the mix bit for bit).
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+import torch
+
+from . import api
+from .params import absolute_rkf45
+
+
+@dataclass
+class QRequest:
+    """A Q-map request: nplanes parallel (n0, n1) seed planes on `field`,
+    plane k offset by k*spacing along `normal` from `center`."""
+    rid: int
+    field: str
+    n0: int
+    n1: int
+    nplanes: int = 1
+    center: tuple = (0.0, 0.0, 0.0)
+    normal: tuple = (0.0, 0.0, 1.0)
+    spacing: float = 1.0
+    tol: float = 1e-4
+    arrival: float = 0.0          # seconds after the stream starts (run_stream)
+    # filled by the server
+    t_submit: float = 0.0
+    t_admit: float = 0.0
+    t_done: float = 0.0
+    result: np.ndarray | None = None
+    meta: dict = dc_field(default_factory=dict)
+
+    @property
+    def seeds(self):
+        return self.n0 * self.n1 * self.nplanes
+
+    @property
+    def qpixels(self):
+        return self.nplanes * (self.n0 - 2) * (self.n1 - 2)
+
+    @property
+    def latency(self):
+        return self.t_done - self.t_submit
+
+
+def request_bytes(req: QRequest) -> int:
+    """Device bytes a request holds while in flight (QBatch buffers: main
+    trace outputs, order, seeds, the pseudo-line buffers sized for every
+    interior pixel, Q and the compaction workspace)."""
+    n, m = req.seeds, req.qpixels
+    return int(n * (72 + 8 + 4 + 12 + 4) + m * (4 * (72 + 8 + 12) + 8 + 8 + 8 + 8) + (n // 1024 + 1) * 12 + 4096)
+
+
+def plane_axes(normal):
+    n = np.asarray(normal, np.float64)
+    n = n / np.linalg.norm(n)
+    e = np.eye(3)[int(np.argmin(np.abs(n)))]
+    u = np.cross(n, e)
+    u /= np.linalg.norm(u)
+    v = np.cross(n, u)
+    return n, u, v
+
+
+def seeds_on_device(req: QRequest, device):
+    """Seeds of the request's planes, built on the device (no host copy):
+    plane k, row i, column j at center + (j - (n1-1)/2) s u + (i - (n0-1)/2) s v
+    + k s n."""
+    n, u, v = plane_axes(req.normal)
+    s = float(req.spacing)
+    c = torch.tensor(req.center, dtype=torch.float64, device=device)
+    j = (torch.arange(req.n1, dtype=torch.float64, device=device) - (req.n1 - 1) / 2.0) * s
+    i = (torch.arange(req.n0, dtype=torch.float64, device=device) - (req.n0 - 1) / 2.0) * s
+    k = torch.arange(req.nplanes, dtype=torch.float64, device=device) * s
+    U = torch.tensor(u, dtype=torch.float64, device=device)
+    V = torch.tensor(v, dtype=torch.float64, device=device)
+    N = torch.tensor(n, dtype=torch.float64, device=device)
+    pts = (c.view(1, 1, 1, 3) + k.view(-1, 1, 1, 1) * N + i.view(1, -1, 1, 1) * V + j.view(1, 1, -1, 1) * U)
+    pts = pts.reshape(-1, 3).to(torch.float32)
+    return pts[:, 0].contiguous(), pts[:, 1].contiguous(), pts[:, 2].contiguous(), tuple(float(x) for x in n)
+
+
+class _Flight:
+    """One launched batch: its requests, buffers, pinned results, event."""
+
+    def __init__(self, reqs, qb, hosts, event, nbytes):
+        self.reqs, self.qb, self.hosts, self.event, self.nbytes = reqs, qb, hosts, event, nbytes
+
+
+class QServer:
+    """Continuous-batching Q-map server over resident fields.
+
+    fields: {name: FieldStore}.  hbm_budget: bytes the in-flight requests may
+    hold; a request larger than the whole budget is rejected at submit.
+    streams: CUDA streams batches rotate over (overlap on the device).
+    max_batch: requests per batch."""
+
+    def __init__(self, fields, hbm_budget=16 << 30, streams=3, max_batch=16, s_len=0.25, h_min=1e-3, h_max=1.0,
+                 tile=(8, 8), device="cuda"):
+        self.fields = dict(fields)
+        self.budget = int(hbm_budget)
+        self.used = 0
+        self.device = torch.device(device)
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, streams))]
+        self._next_stream = 0
+        self.max_batch = int(max_batch)
+        self.s_len, self.h_min, self.h_max = s_len, h_min, h_max
+        self.tile = tile
+        self.pending = collections.deque()
+        self.flights = []
+        self.done = []
+        self.batches = 0
+
+    # ---- request intake ----
+    def submit(self, req: QRequest, now=None):
+        if req.field not in self.fields:
+            raise KeyError(f"unknown field {req.field!r}")
+        if req.n0 < 3 or req.n1 < 3:
+            raise ValueError("a request needs at least 3 x 3 seeds per plane")
+        nb = request_bytes(req)
+        if nb > self.budget:
+            raise MemoryError(f"request {req.rid} needs {nb} B, more than the HBM budget {self.budget} B")
+        req.meta["bytes"] = nb
+        req.t_submit = time.perf_counter() if now is None else now
+        self.pending.append(req)
+
+    # ---- one scheduler turn ----
+    def step(self):
+        """Retires finished batches, then admits and launches waiting requests.
+        Returns True if anything happened."""
+        progressed = self._retire()
+        group, nbytes = [], 0
+        while self.pending and len(group) < self.max_batch:
+            r = self.pending[0]
+            if self.used + nbytes + r.meta["bytes"] > self.budget:
+                break
+            self.pending.popleft()
+            group.append(r)
+            nbytes += r.meta["bytes"]
+        if group:
+            self._launch(group, nbytes)
+            progressed = True
+        return progressed
+
+    def _retire(self):
+        progressed = False
+        keep = []
+        for fl in self.flights:
+            if fl.event.query():
+                t = time.perf_counter()
+                for r, h in zip(fl.reqs, fl.hosts):
+                    r.t_done = t
+                    r.result = h.numpy()
+                    self.done.append(r)
+                self.used -= fl.nbytes
+                progressed = True
+            else:
+                keep.append(fl)
+        self.flights = keep
+        return progressed
+
+    def _launch(self, group, nbytes):
+        st = self.streams[self._next_stream]
+        self._next_stream = (self._next_stream + 1) % len(self.streams)
+        t = time.perf_counter()
+        with torch.cuda.stream(st):
+            specs = []
+            for r in group:
+                r.t_admit = t
+                xs, ys, zs, nrm = seeds_on_device(r, self.device)
+                prm = absolute_rkf45(tol=r.tol, h_min=self.h_min, h_max=self.h_max)
+                specs.append(dict(field=self.fields[r.field], xs=xs, ys=ys, zs=zs, n0=r.n0, n1=r.n1,
+                                  nplanes=r.nplanes, params=prm, s_len=self.s_len, stride=r.spacing, cross_dir=nrm))
+            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st)
+            qs = qb.run(stream=st)
+            hosts = []
+            for q in qs:
+                h = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
+                h.copy_(q, non_blocking=True)
+                hosts.append(h)
+            ev = torch.cuda.Event()
+            ev.record(st)
+        self.used += nbytes
+        self.batches += 1
+        self.flights.append(_Flight(group, qb, hosts, ev, nbytes))
+
+    def idle(self):
+        return not self.pending and not self.flights
+
+    def drain(self, poll=2e-4):
+        while not self.idle():
+            if not self.step():
+                time.sleep(poll)
+
+    # ---- a timed stream of requests ----
+    def run_stream(self, requests, poll=2e-4):
+        """Submits each request at its `arrival` time (seconds from now),
+        serving continuously; returns the requests in completion order."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        t0 = time.perf_counter()
+        k = 0
+        self.done = []
+        while k < len(reqs) or not self.idle():
+            now = time.perf_counter()
+            while k < len(reqs) and t0 + reqs[k].arrival <= now:
+                self.submit(reqs[k], now=t0 + reqs[k].arrival)
+                k += 1
+            if not self.step():
+                nxt = t0 + reqs[k].arrival - time.perf_counter() if k < len(reqs) else poll
+                time.sleep(max(0.0, min(poll, nxt)))
+        return list(self.done)
+
+
+def solve_alone(server: QServer, req: QRequest):
+    """The isolated solve: the request alone on an otherwise idle server;
+    returns (latency in s, Q)."""
+    assert server.idle()
+    r = QRequest(**{k: getattr(req, k) for k in ("rid", "field", "n0", "n1", "nplanes", "center", "normal",
+                                                     "spacing", "tol")})
+    server.submit(r)
+    server.drain()
+    server.done = [d for d in server.done if d is not r]
+    return r.latency, r.result
+
+
+def latency_stats(done, isolated=None):
+    """p50/p99 latency (s), throughput (Q-pixels/s over the busy span) and,
+    given {rid: isolated latency}, p50/p99 of latency / isolated."""
+    lat = np.array([r.latency for r in done])
+    span = max(r.t_done for r in done) - min(r.t_submit for r in done)
+    out = {"requests": len(done), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+           "qpixels_per_s": float(sum(r.qpixels for r in done) / span)}
+    if isolated:
+        ratio = np.array([r.latency / isolated[r.rid] for r in done])
+        out["p50_over_isolated"] = float(np.percentile(ratio, 50))
+        out["p99_over_isolated"] = float(np.percentile(ratio, 99))
+    return out
+
+
+# --------------------------------------------------------------------------
+# The serving-stream workload: resident fields and seeded request streams
+# --------------------------------------------------------------------------
+
+def make_fields(n_fields=8, shape=(384, 384, 256), layout="h4b", seed=0, device="cuda"):
+    """`n_fields` resident stores of point-charge + twisted-tube fields with
+    seeded parameters (synthetic.charges_tube)."""
+    from . import synthetic as S
+    stores = {}
+    for k in range(n_fields):
+        spec = S.charges_tube(seed * 1000 + k, shape, n_charges=8)
+        B = S.make_field(spec, device=device, as_numpy=False)
+        stores[f"f{k}"] = api.FieldStore(*B, layout=layout)
+        del B
+    return stores
+
+
+def make_requests(fields_shape, names, count, rate, seed=0, seeds_range=(1e4, 4e6), tols=(1e-3, 1e-4, 1e-5),
+                  subbox_prob=0.3):
+    """`count` requests with Poisson arrivals at `rate` per second (rate
+    None: all at t = 0): log-uniform seed counts, a random field, a random
+    plane (or, with probability subbox_prob, a stack of 2-8 planes), a random
+    tolerance.  The grid spacing keeps every seed inside the box."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.random.default_rng(seed + 1)  # own stream: same requests at every rate
+    nx, ny, nz = fields_shape
+    t = 0.0
+    out = []
+    for k in range(count):
+        if rate:
+            t += arrivals.exponential(1.0 / rate)
+        total = float(np.exp(rng.uniform(np.log(seeds_range[0]), np.log(seeds_range[1]))))
+        npl = int(rng.integers(2, 9)) if rng.random() < subbox_prob else 1
+        side = max(3, int(round(np.sqrt(total / npl))))
+        n0 = max(3, int(round(side * rng.uniform(0.7, 1.3))))
+        n1 = max(3, int(round(total / npl / n0)))
+        normal = rng.normal(size=3)
+        normal /= np.linalg.norm(normal)
+        reach = 0.42 * min(nx - 1, ny - 1, nz - 1)
+        spacing = min(1.0, reach / (0.5 * np.hypot(n0, n1) + npl))
+        center = (0.5 * (nx - 1) + rng.uniform(-0.05, 0.05) * nx, 0.5 * (ny - 1) + rng.uniform(-0.05, 0.05) * ny,
+                  0.5 * (nz - 1) + rng.uniform(-0.05, 0.05) * nz)
+        out.append(QRequest(rid=k, field=names[int(rng.integers(len(names)))], n0=n0, n1=n1, nplanes=npl,
+                            center=center, normal=tuple(normal), spacing=float(spacing),
+                            tol=float(tols[int(rng.integers(len(tols)))]), arrival=t))
+    return out
+
+
+def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6)):
+    """Isolated solve of every request, the saturated throughput (all
+    requests at once), then Poisson streams at fractions of the saturated
+    request rate.  Returns a dict of latency_stats per point."""
+    names = sorted(server.fields)
+    burst = make_requests(fields_shape, names, count, None, seed=seed, seeds_range=seeds_range)
+    iso = {r.rid: solve_alone(server, r)[0] for r in burst}
+    done = server.run_stream(burst)
+    sat = latency_stats(done, iso)
+    span = max(r.t_done for r in done) - min(r.t_submit for r in done)
+    sat_rate = count / span
+    res = {"saturated": sat, "isolated_p50_s": float(np.median(list(iso.values())))}
+    for f in fractions:
+        reqs = make_requests(fields_shape, names, count, f * sat_rate, seed=seed, seeds_range=seeds_range)
+        res[f"rate_{f:.2f}"] = dict(latency_stats(server.run_stream(reqs), iso), offered_req_per_s=f * sat_rate)
+    return res
