@@ -122,6 +122,8 @@ def run_ours(args, rank, world):
     qpix = SUB["nx"] * SUB["ny"] * npl
     store = api.FieldStore(bx, by, bz, layout=args.layout)
     plan = api.QMapPlan(n0, n1, npl, device=dev)
+    from fastqsl_gb300 import autotune
+    tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=8)
     stream = torch.cuda.current_stream()
 
     def step(count=False, ev=None):
@@ -162,7 +164,8 @@ def run_ours(args, rank, world):
     Q = plan.Q
 
     res = {"ms": ms, "qpix": qpix, "k_ms": k_ms, "samples_main": samples_main, "samples_all": samples_all,
-           "clocks": clk.summary()}
+           "clocks": clk.summary(), "autotune": {"tile": list(tuned["tile"]), "occupancy": tuned["occupancy"],
+                                                 "sample_ms": tuned["table"]}}
     if rank != 0:
         return res, None
 
@@ -421,6 +424,9 @@ def main():
     # launches per step: main trace, qcalc, flag_count, tile_scan, cook_write,
     # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
     line["gpu_launches"] = 8 * args.steps
+    line["config"]["autotune"] = res["autotune"]
+    line["config"]["schedule"] = (f"static lockstep, {res['autotune']['tile'][0]}x{res['autotune']['tile'][1]} "
+                                  f"seed tiles, occupancy {res['autotune']['occupancy']} (autotuned)")
     if "plain_trace_ms" in res:
         line["plain_fp32"] = {"trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
                               "speedup": res["plain_trace_ms"] / res["ours_trace_ms"]}

@@ -300,8 +300,8 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
     unsigned long long* samples_dev = sc.samples;
     unsigned long long* queue_dev = sc.queue;
     if (sc.chunk < 0 || sc.chunk > (1 << 20)) return fail(QSL_ERR_INVALID, "chunk out of range");
-    if (sc.occupancy != 0 && sc.occupancy != 8 && sc.occupancy != 10 && sc.occupancy != 12)
-        return fail(QSL_ERR_INVALID, "occupancy must be 0, 8, 10 or 12");
+    if (sc.occupancy != 0 && (sc.occupancy < 8 || sc.occupancy > 12 || sc.occupancy == 11))
+        return fail(QSL_ERR_INVALID, "occupancy must be 0, 8, 9, 10 or 12");
     if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
     if (!field) return fail(QSL_ERR_INVALID, "field is null");
     if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");

@@ -42,6 +42,7 @@ template <class F>
 static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
     switch (J.occupancy) {
         case 8: return launch_fast_minb<F, 8>(J, twist, sched, n_host, st);
+        case 9: return launch_fast_minb<F, 9>(J, twist, sched, n_host, st);
         case 10: return launch_fast_minb<F, 10>(J, twist, sched, n_host, st);
         case 12: return launch_fast_minb<F, 12>(J, twist, sched, n_host, st);
         default: return launch_fast_minb<F, 1>(J, twist, sched, n_host, st);

@@ -7,12 +7,15 @@ sub-box) and an RKF45 tolerance.  The scheduler loop:
 * completes finished batches (a CUDA event per batch; results were copied to
   pinned host memory on the batch's stream) and returns their memory to the
   HBM budget;
-* admits waiting requests in arrival order while their device memory fits in
-  what the budget has left, up to `max_batch` per batch;
+* sorts requests into size classes; per class, admits waiting requests in
+  arrival order while their device memory fits in what the budget has left,
+  up to the class's batch size and in-flight limit;
 * launches every newly admitted group as one batch (QBatch: one main-trace
-  launch and one pseudo-line launch for all of them) on the next of several
+  launch and one pseudo-line launch for all of them) on one of the class's
   CUDA streams, so a batch starts while earlier ones are still on the GPU and
-  their work overlaps on the device.
+  their work overlaps on the device.  Smaller classes run on higher-priority
+  streams: their blocks are dispatched ahead of a large batch's remaining
+  blocks, so a small request does not wait for a large one to finish.
 
 Nothing in the loop synchronises the device: allocations come from the
 caching allocator on the batch's stream, the job table is copied
@@ -118,18 +121,29 @@ class QServer:
     streams: CUDA streams batches rotate over (overlap on the device).
     max_batch: requests per batch."""
 
-    def __init__(self, fields, hbm_budget=16 << 30, streams=3, max_batch=16, s_len=0.25, h_min=1e-3, h_max=1.0,
-                 tile=(8, 8), device="cuda"):
+    # size classes: (upper bound on seeds, requests per batch, batches in flight)
+    CLASSES = ((1.5e5, 32, 2), (1.2e6, 8, 2), (float("inf"), 2, 2))
+
+    def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
+                 tile=(8, 8), device="cuda", classes=None):
         self.fields = dict(fields)
         self.budget = int(hbm_budget)
         self.used = 0
         self.device = torch.device(device)
-        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, streams))]
-        self._next_stream = 0
-        self.max_batch = int(max_batch)
+        self.classes = classes or self.CLASSES
+        if max_batch is not None:
+            self.classes = tuple((ub, min(int(max_batch), mb), fl) for ub, mb, fl in self.classes)
+        # smaller requests get higher stream priority: the block scheduler
+        # dispatches their blocks ahead of a large batch's remaining ones
+        lo, hi = torch.cuda.Stream.priority_range() if hasattr(torch.cuda.Stream, "priority_range") else (0, -1)
+        prios = [max(hi, lo - (len(self.classes) - 1 - c)) for c in range(len(self.classes))]
+        prios = [hi if c == 0 else lo for c in range(len(self.classes))] if len(set(prios)) < 2 else prios
+        self.streams = [[torch.cuda.Stream(device=self.device, priority=prios[c]) for _ in range(max(1, streams))]
+                        for c in range(len(self.classes))]
+        self._next_stream = [0] * len(self.classes)
         self.s_len, self.h_min, self.h_max = s_len, h_min, h_max
         self.tile = tile
-        self.pending = collections.deque()
+        self.pending = [collections.deque() for _ in self.classes]
         self.flights = []
         self.done = []
         self.batches = 0
@@ -144,25 +158,32 @@ class QServer:
         if nb > self.budget:
             raise MemoryError(f"request {req.rid} needs {nb} B, more than the HBM budget {self.budget} B")
         req.meta["bytes"] = nb
+        req.meta["class"] = next(c for c, (ub, _, _) in enumerate(self.classes) if req.seeds <= ub)
         req.t_submit = time.perf_counter() if now is None else now
-        self.pending.append(req)
+        self.pending[req.meta["class"]].append(req)
 
     # ---- one scheduler turn ----
     def step(self):
-        """Retires finished batches, then admits and launches waiting requests.
-        Returns True if anything happened."""
+        """Retires finished batches, then, per size class, admits waiting
+        requests (arrival order, within the HBM budget and the class's batch
+        size and in-flight limits) and launches them as one batch on that
+        class's streams.  Returns True if anything happened."""
         progressed = self._retire()
-        group, nbytes = [], 0
-        while self.pending and len(group) < self.max_batch:
-            r = self.pending[0]
-            if self.used + nbytes + r.meta["bytes"] > self.budget:
-                break
-            self.pending.popleft()
-            group.append(r)
-            nbytes += r.meta["bytes"]
-        if group:
-            self._launch(group, nbytes)
-            progressed = True
+        for c, (_, max_batch, max_flights) in enumerate(self.classes):
+            q = self.pending[c]
+            if not q or sum(1 for fl in self.flights if fl.cls == c) >= max_flights:
+                continue
+            group, nbytes = [], 0
+            while q and len(group) < max_batch:
+                r = q[0]
+                if self.used + nbytes + r.meta["bytes"] > self.budget:
+                    break
+                q.popleft()
+                group.append(r)
+                nbytes += r.meta["bytes"]
+            if group:
+                self._launch(group, nbytes, c)
+                progressed = True
         return progressed
 
     def _retire(self):
@@ -182,9 +203,9 @@ class QServer:
         self.flights = keep
         return progressed
 
-    def _launch(self, group, nbytes):
-        st = self.streams[self._next_stream]
-        self._next_stream = (self._next_stream + 1) % len(self.streams)
+    def _launch(self, group, nbytes, cls):
+        st = self.streams[cls][self._next_stream[cls]]
+        self._next_stream[cls] = (self._next_stream[cls] + 1) % len(self.streams[cls])
         t = time.perf_counter()
         with torch.cuda.stream(st):
             specs = []
@@ -205,10 +226,12 @@ class QServer:
             ev.record(st)
         self.used += nbytes
         self.batches += 1
-        self.flights.append(_Flight(group, qb, hosts, ev, nbytes))
+        fl = _Flight(group, qb, hosts, ev, nbytes)
+        fl.cls = cls
+        self.flights.append(fl)
 
     def idle(self):
-        return not self.pending and not self.flights
+        return not any(self.pending) and not self.flights
 
     def drain(self, poll=2e-4):
         while not self.idle():

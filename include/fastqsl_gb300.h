@@ -191,7 +191,7 @@ typedef struct qsl_sched {
                                     `stream` (stream-ordered) and freed after the launch */
     unsigned long long *samples; /* optional: accumulates the number of trilinear field samples */
     int32_t occupancy;           /* fast kernels: register budget for this many resident 128-thread
-                                    blocks per SM (0 = compiler's choice, or 8, 10, 12) */
+                                    blocks per SM (0 = compiler's choice, or 8, 9, 10, 12) */
 } qsl_sched;
 
 /* Traces n seeds (or *n_dev seeds when n_dev is set; then the outputs must

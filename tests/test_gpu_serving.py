@@ -7,7 +7,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-def _server(budget=8 << 30, streams=3, max_batch=8):
+def _server(budget=8 << 30, streams=2, max_batch=8):
     from fastqsl_gb300 import serving
     fields = serving.make_fields(n_fields=3, shape=(48, 44, 40), seed=3)
     return serving.QServer(fields, hbm_budget=budget, streams=streams, max_batch=max_batch), (48, 44, 40)
