@@ -123,7 +123,10 @@ def run_ours(args, rank, world):
     store = api.FieldStore(bx, by, bz, layout=args.layout)
     plan = api.QMapPlan(n0, n1, npl, device=dev)
     from fastqsl_gb300 import autotune
-    tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=8)
+    if args.no_autotune:
+        tuned = {"tile": (8, 8), "occupancy": plan.occupancy_for(store), "table": {}}
+    else:
+        tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=8)
     stream = torch.cuda.current_stream()
 
     def step(count=False, ev=None):
@@ -363,6 +366,7 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch configuration (profiling)")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     args = ap.parse_args()

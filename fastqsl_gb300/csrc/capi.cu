@@ -1,5 +1,6 @@
 // C ABI of fastqsl_gb300 (declarations and contracts in
 // include/fastqsl_gb300.h).
+#include <climits>
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -279,6 +280,10 @@ static void fill_common(TraceJob<F>& J, const qsl_trace_io* io, const qsl_trace_
     J.inp_z = io->inp_z;
     J.o = make_out(io);
     J.prm = *prm;
+    J.lim.h_min = (float)prm->h_min;
+    J.lim.h_max = (float)prm->h_max;
+    J.lim.reject = (float)prm->reject_factor;
+    J.lim.max_steps = prm->max_steps > INT_MAX ? INT_MAX : (prm->max_steps < 0 ? 0 : (int)prm->max_steps);
     J.queue = nullptr;
     J.samples = samples_dev;
     J.order = nullptr;

@@ -48,6 +48,17 @@ struct TraceScalars {
     int twist_on;
 };
 
+// Step-size limits of the adaptive controller narrowed to float once on the
+// host.  For a float h and a double bound H, `h > H` and `h > (float)H` clamp
+// h to the same value (the only float between H and its rounding is the
+// rounding itself), so the fast kernels compare in float and keep the FP64
+// pipe off the per-step path.  max_steps is clamped to the int range of the
+// lane's step counter.
+struct StepLimits {
+    float h_min, h_max, reject;
+    int max_steps;
+};
+
 template <class F>
 struct TraceJob {
     F f;
@@ -57,6 +68,7 @@ struct TraceJob {
     TraceOut o;
     TraceScalars s;
     qsl_trace_params prm;
+    StepLimits lim;               // prm's controller limits in float (fast arithmetic)
     unsigned long long* queue;    // work counter, zero at launch; null = static
     unsigned long long* samples;  // optional: total field samples
     const unsigned* order;        // optional: line k traces seed order[k] and writes its outputs there
@@ -221,7 +233,8 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
                                           typename Lane<EXACT>::len_t len_lim, bool tw_on,
                                           unsigned& ns) {
     const qsl_trace_params& pr = J.prm;
-    if (!((L.len < len_lim) & (L.steps < pr.max_steps))) {
+    const bool more_steps = EXACT ? ((long long)L.steps < pr.max_steps) : (L.steps < J.lim.max_steps);
+    if (!((L.len < len_lim) & more_steps)) {
         L.out = L.p;
         L.flag = 0;
         return true;
@@ -243,13 +256,18 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
             // log2 / exp2 are accurate enough
             scale = exp2f(0.2f * __log2f(L.tol / err * (float)(1.0 / 11.09)));
             if (scale < 0.618f) {
-                L.h = L.h * (float)pr.reject_factor;
+                L.h = L.h * J.lim.reject;
                 return false;
             }
         }
         float h = L.h * scale;
-        if ((double)h > pr.h_max) h = (float)pr.h_max;
-        if ((double)h < pr.h_min) h = (float)pr.h_min;
+        if (EXACT) {
+            if ((double)h > pr.h_max) h = (float)pr.h_max;
+            if ((double)h < pr.h_min) h = (float)pr.h_min;
+        } else {
+            if (h > J.lim.h_max) h = J.lim.h_max;  // a NaN step stays NaN, as above
+            if (h < J.lim.h_min) h = J.lim.h_min;
+        }
         L.h = h;
     } else {
         inc = step_rk4<EXACT>(f, L.p, hd, ns);
