@@ -210,6 +210,91 @@ __device__ __forceinline__ float3 sample(const F& f, float3 p, bool unit) {
     return r;
 }
 
+// ---------------------------------------------------------------------------
+// Fast sampling of the fp16 brick store without fp16->fp32 conversions.
+//
+// The x-lerp of each corner pair reads the fp16 components directly with the
+// mixed-precision multiply-add (fma.rn.f32.f16: the f16 x f16 product is exact
+// and the sum is rounded once to f32); the y and z lerps run on packed f32
+// pairs (fma.rn.f32x2) for (Bx, By) and scalar f32 for Bz.  The x fraction
+// is rounded to a multiple of 2^-11, on which both r and 1 - r are exact in
+// fp16, so the x weights sum to exactly 1 and the result is the trilinear
+// value at a point within 2^-12 cell of p along x (the fp16 node values
+// themselves carry a relative rounding of up to 2^-12).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void xlerp_h4(uint2 lo, uint2 hi, unsigned w, float& x, float& y, float& z) {
+    asm("{\n\t"
+        ".reg .f16 a0, a1, a2, a3, b0, b1, b2, b3, wo, wr;\n\t"
+        ".reg .f32 t;\n\t"
+        "mov.b32 {a0, a1}, %3;\n\t"
+        "mov.b32 {a2, a3}, %4;\n\t"
+        "mov.b32 {b0, b1}, %5;\n\t"
+        "mov.b32 {b2, b3}, %6;\n\t"
+        "mov.b32 {wo, wr}, %7;\n\t"
+        "fma.rn.f32.f16 t, a0, wo, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %0, b0, wr, t;\n\t"
+        "fma.rn.f32.f16 t, a1, wo, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %1, b1, wr, t;\n\t"
+        "fma.rn.f32.f16 t, a2, wo, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %2, b2, wr, t;\n\t"
+        "}"
+        : "=f"(x), "=f"(y), "=f"(z)
+        : "r"(lo.x), "r"(lo.y), "r"(hi.x), "r"(hi.y), "r"(w));
+}
+
+// (a.x + r (b.x - a.x), a.y + r (b.y - a.y)) on the packed f32 pipe.
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float r) {
+    float2 d;
+    asm("{\n\t"
+        ".reg .b64 ra, rb, rr, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rr, {%6, %6};\n\t"
+        "sub.rn.f32x2 rd, rb, ra;\n\t"
+        "fma.rn.f32x2 rd, rd, rr, ra;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t"
+        "}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(r));
+    return d;
+}
+
+template <>
+__device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, float3 p, bool unit) {
+    int ix, iy, iz;
+    float rx, ry, rz;
+    locate_fast(p.x, f.d.nx, ix, rx);
+    locate_fast(p.y, f.d.ny, iy, ry);
+    locate_fast(p.z, f.d.nz, iz, rz);
+    const float rq = rintf(rx * 2048.f) * (1.f / 2048.f);
+    const __half2 wh = __floats2half2_rn(1.f - rq, rq);  // exact: both on the 2^-11 grid
+    const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
+    const int bi = ix >> 3, bj = iy >> 3, bk = iz >> 3;
+    const int64_t brick = bi + (int64_t)f.nbx * (bj + (int64_t)f.nby * bk);
+    const uint2* bp = f.bricks + brick * BRICK_U2 + ((ix & 7) + BRICK_NODES * ((iy & 7) + BRICK_NODES * (iz & 7)));
+    uint2 u[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        u[q] = __ldg(bp + ((q >> 2) & 1) + ((q >> 1) & 1) * BRICK_NODES + (q & 1) * (BRICK_NODES * BRICK_NODES));
+    // e[(dy << 1) | dz]: x-lerped corner pairs
+    float2 exy[4];
+    float ez[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) xlerp_h4(u[q], u[q + 4], w, exy[q].x, exy[q].y, ez[q]);
+    const float2 g0 = lerp2(exy[0], exy[2], ry), g1 = lerp2(exy[1], exy[3], ry);
+    const float gz0 = fmaf(ry, ez[2] - ez[0], ez[0]), gz1 = fmaf(ry, ez[3] - ez[1], ez[1]);
+    const float2 rxy = lerp2(g0, g1, rz);
+    float3 r = v3(rxy.x, rxy.y, fmaf(rz, gz1 - gz0, gz0));
+    if (unit) {
+        const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+        r = v3(r.x * inv, r.y * inv, r.z * inv);
+    } else {
+        const float s = __ldg(f.scale + brick);
+        r = v3(r.x * s, r.y * s, r.z * s);
+    }
+    return r;
+}
+
 // Position clamped into [1e-4, n-1-1e-4] as the scalar interpolator of the
 // reference does (Interp3d, TraceBlineAdaptive.cu:57-62).
 __device__ __forceinline__ float clamp_inside(float c, int n) {
