@@ -242,21 +242,9 @@ __device__ __forceinline__ void xlerp_h4(uint2 lo, uint2 hi, unsigned w, float& 
         : "r"(lo.x), "r"(lo.y), "r"(hi.x), "r"(hi.y), "r"(w));
 }
 
-// (a.x + r (b.x - a.x), a.y + r (b.y - a.y)) on the packed f32 pipe.
-__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float r) {
-    float2 d;
-    asm("{\n\t"
-        ".reg .b64 ra, rb, rr, rd;\n\t"
-        "mov.b64 ra, {%2, %3};\n\t"
-        "mov.b64 rb, {%4, %5};\n\t"
-        "mov.b64 rr, {%6, %6};\n\t"
-        "sub.rn.f32x2 rd, rb, ra;\n\t"
-        "fma.rn.f32x2 rd, rd, rr, ra;\n\t"
-        "mov.b64 {%0, %1}, rd;\n\t"
-        "}"
-        : "=f"(d.x), "=f"(d.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(r));
-    return d;
+// o a + r b (o = 1 - r) for an (x, y) pair on the packed f32 pipe.
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float o, float r) {
+    return __ffma2_rn(b, make_float2(r, r), __fmul2_rn(a, make_float2(o, o)));
 }
 
 template <>
@@ -269,9 +257,11 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
     const float rq = rintf(rx * 2048.f) * (1.f / 2048.f);
     const __half2 wh = __floats2half2_rn(1.f - rq, rq);  // exact: both on the 2^-11 grid
     const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
-    const int bi = ix >> 3, bj = iy >> 3, bk = iz >> 3;
-    const int64_t brick = bi + (int64_t)f.nbx * (bj + (int64_t)f.nby * bk);
-    const uint2* bp = f.bricks + brick * BRICK_U2 + ((ix & 7) + BRICK_NODES * ((iy & 7) + BRICK_NODES * (iz & 7)));
+    // brick indices fit 32 bits (field stores hold < 1.1e12 nodes, so fewer
+    // than 2.2e9 bricks)
+    const unsigned brick = (unsigned)(ix >> 3) + (unsigned)f.nbx * ((unsigned)(iy >> 3) + (unsigned)f.nby * (unsigned)(iz >> 3));
+    const unsigned node = (unsigned)((ix & 7) + BRICK_NODES * ((iy & 7) + BRICK_NODES * (iz & 7)));
+    const uint2* bp = f.bricks + ((unsigned long long)brick * BRICK_U2 + node);
     uint2 u[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
@@ -281,10 +271,11 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
     float ez[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) xlerp_h4(u[q], u[q + 4], w, exy[q].x, exy[q].y, ez[q]);
-    const float2 g0 = lerp2(exy[0], exy[2], ry), g1 = lerp2(exy[1], exy[3], ry);
-    const float gz0 = fmaf(ry, ez[2] - ez[0], ez[0]), gz1 = fmaf(ry, ez[3] - ez[1], ez[1]);
-    const float2 rxy = lerp2(g0, g1, rz);
-    float3 r = v3(rxy.x, rxy.y, fmaf(rz, gz1 - gz0, gz0));
+    const float oy = 1.f - ry, oz = 1.f - rz;
+    const float2 g0 = lerp2(exy[0], exy[2], oy, ry), g1 = lerp2(exy[1], exy[3], oy, ry);
+    const float gz0 = fmaf(ez[2], ry, ez[0] * oy), gz1 = fmaf(ez[3], ry, ez[1] * oy);
+    const float2 rxy = lerp2(g0, g1, oz, rz);
+    float3 r = v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
     if (unit) {
         const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
         r = v3(r.x * inv, r.y * inv, r.z * inv);

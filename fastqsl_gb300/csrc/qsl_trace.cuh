@@ -95,8 +95,46 @@ struct Fehlberg {
 // One Fehlberg step (RKF45, TraceBlineAdaptive.cu:215-254): returns the
 // 5th-order increment (the reference adds it to P0 in one rounding) and the
 // error-estimate norm.
+// Vector as an (x, y) pair for the packed f32x2 pipe plus a scalar z.
+struct PV {
+    float2 xy;
+    float z;
+};
+__device__ __forceinline__ PV pv(float3 a) { return {make_float2(a.x, a.y), a.z}; }
+__device__ __forceinline__ float3 f3(PV a) { return v3(a.xy.x, a.xy.y, a.z); }
+// a*x + y
+__device__ __forceinline__ PV axpy(float a, PV x, PV y) {
+    return {__ffma2_rn(make_float2(a, a), x.xy, y.xy), fmaf(a, x.z, y.z)};
+}
+__device__ __forceinline__ PV scal(float a, PV x) { return {__fmul2_rn(make_float2(a, a), x.xy), a * x.z}; }
+
+// Fast-arithmetic Fehlberg step: the same stages on the unit field b with
+// the step folded in once per stage (p + h * sum a_ij b_j), combinations on
+// packed (x, y) pairs.  Differs from the reference's rounding sequence only
+// in rounding.
+template <class F>
+__device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h, float& err, unsigned& ns) {
+    using C = Fehlberg;
+    const PV P = pv(p);
+    const PV b1 = pv(sample<false>(f, p, true));
+    const PV b2 = pv(sample<false>(f, f3(axpy(h * C::a21, b1, P)), true));
+    PV c = axpy(C::a32, b2, scal(C::a31, b1));
+    const PV b3 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
+    c = axpy(C::a43, b3, axpy(C::a42, b2, scal(C::a41, b1)));
+    const PV b4 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
+    c = axpy(C::a54, b4, axpy(C::a53, b3, axpy(C::a52, b2, scal(C::a51, b1))));
+    const PV b5 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
+    c = axpy(C::a65, b5, axpy(C::a64, b4, axpy(C::a63, b3, axpy(C::a62, b2, scal(C::a61, b1)))));
+    const PV b6 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
+    const PV e = axpy(C::e6, b6, axpy(C::e5, b5, axpy(C::e4, b4, axpy(C::e3, b3, scal(C::e1, b1)))));
+    err = fabsf(h) * norm(f3(e));
+    ns += 6;
+    return f3(scal(h, axpy(C::b6, b6, axpy(C::b5, b5, axpy(C::b4, b4, axpy(C::b3, b3, scal(C::b1, b1)))))));
+}
+
 template <bool EXACT, class F>
 __device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, float& err, unsigned& ns) {
+    if (!EXACT) return step_rkf45_fast(f, p, h, err, ns);
     using C = Fehlberg;
     const float3 k1 = h * sample<EXACT>(f, p, true);
     const float3 k2 = h * sample<EXACT>(f, p + C::a21 * k1, true);
