@@ -36,6 +36,7 @@ SUB = dict(x0=128, y0=128, z0=64, nx=256, ny=256, nz=128)
 S_LEN = 0.25
 METRIC = "Q-pixels/s (3-D Q-cube, 512x512x256 field, RKF45 tol 1e-4)"
 NPLANES = [SUB["nz"]]  # --planes: fewer z-planes of the same cube (profiling cases)
+PLANE0 = [0]  # --plane-offset: first of those planes
 
 
 def peaks():
@@ -95,13 +96,16 @@ class ClockSampler:
 
 def cube_seeds(device, planes=None):
     if planes is None and NPLANES[0] != SUB["nz"]:
-        planes = list(range(NPLANES[0]))
+        planes = list(range(PLANE0[0], PLANE0[0] + NPLANES[0]))
     from fastqsl_gb300 import api
     s = SUB
     zs = [float(s["z0"] + k) for k in (range(s["nz"]) if planes is None else planes)]
     xs, ys, zz = api.plane_seed_grid(s["x0"] - 1.0, s["x0"] + s["nx"], s["nx"] + 2, s["y0"] - 1.0,
                                      s["y0"] + s["ny"], s["ny"] + 2, zs, device=device)
     return xs, ys, zz, len(zs)
+
+
+STORE_TYPES = {"h8c": "FieldH8C", "h4b": "FieldH4B", "f4": "FieldF4", "soa": "FieldSoA"}
 
 
 def make_field(device):
@@ -358,7 +362,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--layout", default="h4b", choices=["h4b", "f4", "soa"])
+    ap.add_argument("--layout", default="h4b", choices=["h8c", "h4b", "f4", "soa"])
     ap.add_argument("--cpu-planes", type=int, default=32)
     ap.add_argument("--acc-cells", type=int, default=2000)
     ap.add_argument("--skip-plain", action="store_true")
@@ -369,8 +373,10 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration (profiling)")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
+    ap.add_argument("--plane-offset", type=int, default=0, help="first z-plane with --planes")
     args = ap.parse_args()
     NPLANES[0] = max(1, min(SUB["nz"], args.planes))
+    PLANE0[0] = max(0, min(SUB["nz"] - NPLANES[0], args.plane_offset))
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -406,12 +412,13 @@ def main():
     peak, peak_kind = peaks()
     ms = res["ms"]
     value = res["qpix"] * world / (ms / 1e3)
-    bytes_per_sample = 48 if args.layout == "h4b" else 96
+    fp16 = args.layout in ("h4b", "h8c")
+    bytes_per_sample = 48 if fp16 else 96
     achieved = res["samples_main"] * bytes_per_sample / (res["k_ms"] / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "Q-pixels/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (fp16 field storage)" if args.layout == "h4b" else "f32",
+        "vs_baseline": None, "dtype": "f32 (fp16 field storage)" if fp16 else "f32",
         "data": "synthetic",
         "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
                    "field": "x".join(map(str, FIELD_SHAPE)), "qcube": "256x256x128", "layout": args.layout,
@@ -421,7 +428,7 @@ def main():
         "clocks": res["clocks"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_trace_fast<static, FieldH4B> (main trace)",
+                     "kernel": f"k_trace_fast<static, {STORE_TYPES[args.layout]}> (main trace)",
                      "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
                              f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
     }
@@ -430,7 +437,8 @@ def main():
     line["gpu_launches"] = 8 * args.steps
     line["config"]["autotune"] = res["autotune"]
     line["config"]["schedule"] = (f"static lockstep, {res['autotune']['tile'][0]}x{res['autotune']['tile'][1]} "
-                                  f"seed tiles, occupancy {res['autotune']['occupancy']} (autotuned)")
+                                  f"seed tiles, occupancy {res['autotune']['occupancy']} "
+                                  f"({'default' if args.no_autotune else 'autotuned'})")
     if "plain_trace_ms" in res:
         line["plain_fp32"] = {"trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
                               "speedup": res["plain_trace_ms"] / res["ours_trace_ms"]}

@@ -20,7 +20,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 NO_FMA = {"trace_exact.cu", "qassembly.cu"}
-SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast.cu", "field_store.cu", "qassembly.cu", "noalloc.cu"]
+SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast_soa.cu", "trace_fast_f4.cu", "trace_fast_h4b.cu",
+           "trace_fast_h8c.cu", "field_store.cu", "qassembly.cu", "noalloc.cu"]
 
 
 def _deps():

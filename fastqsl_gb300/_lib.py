@@ -37,8 +37,8 @@ class BatchJob(ctypes.Structure):
 
 
 class BatchInfo(ctypes.Structure):
-    _fields_ = [("jobs_offset", ctypes.c_int64 * 3), ("begin_offset", ctypes.c_int64 * 3),
-                ("total", ctypes.c_int64 * 3), ("njobs", ctypes.c_int32 * 3), ("twist", ctypes.c_int32 * 3),
+    _fields_ = [("jobs_offset", ctypes.c_int64 * 4), ("begin_offset", ctypes.c_int64 * 4),
+                ("total", ctypes.c_int64 * 4), ("njobs", ctypes.c_int32 * 4), ("twist", ctypes.c_int32 * 4),
                 ("table_bytes", ctypes.c_int64), ("lines", ctypes.c_int64)]
 
 

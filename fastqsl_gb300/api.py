@@ -14,7 +14,7 @@ import torch
 from . import _lib
 from .params import TraceParams, absolute_rkf45
 
-LAYOUTS = {"soa": 0, "f4": 1, "h4b": 2}
+LAYOUTS = {"soa": 0, "f4": 1, "h4b": 2, "h8c": 3}
 SCHEDULES = {"queue": 0, "static": 1}
 
 TRACE_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
@@ -61,8 +61,10 @@ def as_xfast(a, device="cuda"):
 class FieldStore:
     """A field resident on the device in one of the GB300 layouts.
 
-    layout: 'h4b' (fp16 8^3 bricks + per-brick scale), 'f4' (interleaved
-    float4) or 'soa' (the caller's arrays in place)."""
+    layout: 'h8c' (fp16 cell records: each cell's 8 corners in 64 B, the
+    fastest store, ~64 B per cell), 'h4b' (fp16 8^3 bricks + per-brick scale,
+    ~11 B per node), 'f4' (interleaved float4) or 'soa' (the caller's arrays
+    in place)."""
 
     def __init__(self, Bx, By, Bz, layout="h4b", stream=None):
         lib = _lib.load()
@@ -238,7 +240,7 @@ class QMapPlan:
     # measured best per field layout on GB300 (trace of the 512x512x256 cube):
     # register budget for 8 resident blocks/SM for the brick and float4
     # stores, the compiler's choice for SoA
-    DEFAULT_OCCUPANCY = {"h4b": 8, "f4": 8, "soa": 0}
+    DEFAULT_OCCUPANCY = {"h8c": 8, "h4b": 8, "f4": 8, "soa": 0}
 
     def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True, tile=(8, 8), chunk=256, schedule="static",
                  occupancy=None):

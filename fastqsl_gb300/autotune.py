@@ -7,7 +7,7 @@ planes) for each candidate
 * seed tile — which seeds a warp's 32 lanes trace together (8x8 tiles give a
   warp a 8x4 patch; 16x16 a 16x2 strip; 4x8 a 4x8 patch),
 * resident-block budget — registers per thread sized for 0 (compiler's
-  choice), 8, 9, 10 or 12 blocks of 128 threads per SM,
+  choice), 6, 7, 8, 9 or 10 blocks of 128 threads per SM,
 
 and keeps the fastest.  Results are cached per (device, store layout, field
 shape, integrator, plane shape).
@@ -19,7 +19,7 @@ import torch
 from . import api
 
 TILES = ((8, 8), (4, 8), (16, 16))
-OCCUPANCIES = (0, 8, 9, 10)
+OCCUPANCIES = (0, 6, 7, 8, 9, 10)
 
 _cache: dict = {}
 

@@ -97,6 +97,7 @@ struct qsl_field {
     float4* f4;
     uint2* bricks;
     float* scale;
+    uint4* cells;  // H8C records
     int nbx, nby, nbz;
     int64_t bytes;
     int device;
@@ -116,6 +117,7 @@ static int64_t layout_bytes(int nx, int ny, int nz, int layout, int* nbx, int* n
             const int64_t nb = (int64_t)bx * by * bz;
             return nb * BRICK_U2 * (int64_t)sizeof(uint2) + nb * (int64_t)sizeof(float);
         }
+        case LAYOUT_H8C: return (int64_t)bx * by * bz * 512 * CELL_RECORD_U4 * (int64_t)sizeof(uint4);
         default: return -1;
     }
 }
@@ -162,16 +164,20 @@ int qsl_field_create(const float* Bx, const float* By, const float* Bz, int nx, 
     } else if (layout == LAYOUT_F4) {
         e = cudaMalloc(&f->f4, (size_t)bytes);
         if (e == cudaSuccess) e = launch_pack_f4(Bx, By, Bz, f->d, f->f4, st);
-    } else {
+    } else if (layout == LAYOUT_H4B) {
         const int64_t nb = (int64_t)nbx * nby * nbz;
         e = cudaMalloc(&f->bricks, (size_t)(nb * BRICK_U2 * sizeof(uint2)));
         if (e == cudaSuccess) e = cudaMalloc(&f->scale, (size_t)(nb * sizeof(float)));
         if (e == cudaSuccess) e = launch_pack_h4b(Bx, By, Bz, f->d, nbx, nby, nbz, f->bricks, f->scale, st);
+    } else {
+        e = cudaMalloc(&f->cells, (size_t)bytes);
+        if (e == cudaSuccess) e = launch_pack_h8c(Bx, By, Bz, f->d, nbx, nby, nbz, f->cells, st);
     }
     if (e != cudaSuccess) {
         cudaFree(f->f4);
         cudaFree(f->bricks);
         cudaFree(f->scale);
+        cudaFree(f->cells);
         delete f;
         return cuda_fail(e, "qsl_field_create");
     }
@@ -184,6 +190,7 @@ int qsl_field_destroy(qsl_field_t* f) {
     cudaFree(f->f4);
     cudaFree(f->bricks);
     cudaFree(f->scale);
+    cudaFree(f->cells);
     delete f;
     return QSL_OK;
 }
@@ -199,14 +206,21 @@ int qsl_field_update(qsl_field_t* f, const float* Bx, const float* By, const flo
         f->bz = Bz;
         return QSL_OK;
     }
-    cudaError_t e = f->layout == LAYOUT_F4
-                        ? launch_pack_f4(Bx, By, Bz, f->d, f->f4, st)
-                        : launch_pack_h4b(Bx, By, Bz, f->d, f->nbx, f->nby, f->nbz, f->bricks, f->scale, st);
+    cudaError_t e = f->layout == LAYOUT_F4    ? launch_pack_f4(Bx, By, Bz, f->d, f->f4, st)
+                    : f->layout == LAYOUT_H4B ? launch_pack_h4b(Bx, By, Bz, f->d, f->nbx, f->nby, f->nbz, f->bricks,
+                                                                f->scale, st)
+                                              : launch_pack_h8c(Bx, By, Bz, f->d, f->nbx, f->nby, f->nbz, f->cells, st);
     if (e != cudaSuccess) return cuda_fail(e, "qsl_field_update");
     return QSL_OK;
 }
 
 }  // extern "C"
+
+// device views of a store
+static FieldSoA soa_of(const qsl_field* f) { return FieldSoA{f->bx, f->by, f->bz, f->d}; }
+static FieldF4 f4_of(const qsl_field* f) { return FieldF4{f->f4, f->d}; }
+static FieldH4B h4b_of(const qsl_field* f) { return FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}; }
+static FieldH8C h8c_of(const qsl_field* f) { return FieldH8C{f->cells, f->d, f->nbx, f->nby}; }
 
 // ---------------------------------------------------------------------------
 // Tracing
@@ -262,8 +276,10 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
                                      : launch_trace_fast_soa(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldF4>::value) {
         e = launch_trace_fast_f4(J, twist, sched, n_host, st);
-    } else {
+    } else if constexpr (std::is_same<F, FieldH4B>::value) {
         e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
+    } else {
+        e = launch_trace_fast_h8c(J, twist, sched, n_host, st);
     }
     if (own) cudaFreeAsync(q, st);
     if (e != cudaSuccess) return cuda_fail(e, "trace launch");
@@ -305,8 +321,8 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
     unsigned long long* samples_dev = sc.samples;
     unsigned long long* queue_dev = sc.queue;
     if (sc.chunk < 0 || sc.chunk > (1 << 20)) return fail(QSL_ERR_INVALID, "chunk out of range");
-    if (sc.occupancy != 0 && (sc.occupancy < 8 || sc.occupancy > 12 || sc.occupancy == 11))
-        return fail(QSL_ERR_INVALID, "occupancy must be 0, 8, 9, 10 or 12");
+    if (sc.occupancy != 0 && (sc.occupancy < 6 || sc.occupancy > 10))
+        return fail(QSL_ERR_INVALID, "occupancy must be 0, 6, 7, 8, 9 or 10");
     if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
     if (!field) return fail(QSL_ERR_INVALID, "field is null");
     if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
@@ -332,9 +348,9 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         s.twist_on = twist ? 1 : 0;
     };
     const FieldSoA cur{curBx, curBy, curBz, field->d};
-    if (field->layout == LAYOUT_SOA) {
-        TraceJob<FieldSoA> J;
-        J.f = FieldSoA{field->bx, field->by, field->bz, field->d};
+    auto go = [&](auto store) {
+        TraceJob<decltype(store)> J;
+        J.f = store;
         fill_common(J, io, prm, samples_dev);
         J.cur = cur;
         J.order = sc.order;
@@ -342,26 +358,12 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         J.occupancy = sc.occupancy;
         scal(J.s);
         return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
-    } else if (field->layout == LAYOUT_F4) {
-        TraceJob<FieldF4> J;
-        J.f = FieldF4{field->f4, field->d};
-        fill_common(J, io, prm, samples_dev);
-        J.cur = cur;
-        J.order = sc.order;
-        J.chunk = sc.chunk;
-        J.occupancy = sc.occupancy;
-        scal(J.s);
-        return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
-    } else {
-        TraceJob<FieldH4B> J;
-        J.f = FieldH4B{field->bricks, field->scale, field->d, field->nbx, field->nby};
-        fill_common(J, io, prm, samples_dev);
-        J.cur = cur;
-        J.order = sc.order;
-        J.chunk = sc.chunk;
-        J.occupancy = sc.occupancy;
-        scal(J.s);
-        return run_trace(J, prm->arith, twist, schedule, n, queue_dev, st);
+    };
+    switch (field->layout) {
+        case LAYOUT_SOA: return go(soa_of(field));
+        case LAYOUT_F4: return go(f4_of(field));
+        case LAYOUT_H4B: return go(h4b_of(field));
+        default: return go(h8c_of(field));
     }
 }
 
@@ -442,14 +444,16 @@ int qsl_trace_all_bline_rk4(const float* Bx, const float* By, const float* Bz, c
 // ---------------------------------------------------------------------------
 // Batched trace plans
 // ---------------------------------------------------------------------------
+// Jobs are grouped by store type (slot = the layout code); each slot is one
+// launch over its job table.
 struct qsl_batch {
     int device;
     // per store type: job table and warp-aligned line offsets in device memory
-    void* jobs[3];
-    long long* begin[3];
-    int njobs[3];
-    long long total[3];
-    bool twist[3];
+    void* jobs[kStoreTypes];
+    long long* begin[kStoreTypes];
+    int njobs[kStoreTypes];
+    long long total[kStoreTypes];
+    bool twist[kStoreTypes];
     int64_t lines;
 };
 
@@ -469,40 +473,29 @@ static TraceJob<F> batch_job_of(const qsl_batch_job& b, const F& f) {
     return J;
 }
 
-template <class F>
-static int batch_upload(qsl_batch* B, int slot, const std::vector<TraceJob<F>>& js, const std::vector<long long>& beg,
-                        bool twist, cudaStream_t st) {
-    B->njobs[slot] = (int)js.size();
-    B->total[slot] = beg.back();
-    B->twist[slot] = twist;
-    if (js.empty()) return QSL_OK;
-    QSL_CHECK_CUDA(cudaMalloc(&B->jobs[slot], js.size() * sizeof(TraceJob<F>)), "batch job table");
-    QSL_CHECK_CUDA(cudaMalloc((void**)&B->begin[slot], beg.size() * sizeof(long long)), "batch offsets");
-    QSL_CHECK_CUDA(cudaMemcpyAsync(B->jobs[slot], js.data(), js.size() * sizeof(TraceJob<F>),
-                                   cudaMemcpyHostToDevice, st), "batch upload");
-    QSL_CHECK_CUDA(cudaMemcpyAsync(B->begin[slot], beg.data(), beg.size() * sizeof(long long),
-                                   cudaMemcpyHostToDevice, st), "batch upload");
-    // the host vectors die on return: make sure the copies have read them
-    QSL_CHECK_CUDA(cudaStreamSynchronize(st), "batch upload");
-    return QSL_OK;
-}
-
-// Serialised batch table: per store type a TraceJob<F> array and its line
-// offsets, each at a 256-byte aligned offset of one buffer.
 static int64_t align256(int64_t x) { return (x + 255) / 256 * 256; }
 
+// Per store type: the job list (TraceJob<F> of that store, as bytes) and the
+// line offsets.
 struct BatchLists {
-    std::vector<TraceJob<FieldSoA>> j0;
-    std::vector<TraceJob<FieldF4>> j1;
-    std::vector<TraceJob<FieldH4B>> j2;
-    std::vector<long long> b[3];
-    bool tw[3] = {false, false, false};
+    std::vector<char> j[kStoreTypes];
+    size_t jsz[kStoreTypes] = {sizeof(TraceJob<FieldSoA>), sizeof(TraceJob<FieldF4>), sizeof(TraceJob<FieldH4B>),
+                               sizeof(TraceJob<FieldH8C>)};
+    std::vector<long long> b[kStoreTypes];
+    bool tw[kStoreTypes] = {false, false, false, false};
     int64_t lines = 0;
+    size_t count(int k) const { return j[k].size() / jsz[k]; }
 };
+
+template <class F>
+static void push_job(std::vector<char>& v, const TraceJob<F>& J) {
+    const char* p = reinterpret_cast<const char*>(&J);
+    v.insert(v.end(), p, p + sizeof(J));
+}
 
 static int batch_lists(const qsl_batch_job* jobs_h, int njobs, BatchLists& L) {
     if (njobs < 0 || (njobs > 0 && !jobs_h)) return fail(QSL_ERR_INVALID, "bad job list");
-    for (int k = 0; k < 3; ++k) L.b[k] = std::vector<long long>{0};
+    for (int k = 0; k < kStoreTypes; ++k) L.b[k] = std::vector<long long>{0};
     for (int k = 0; k < njobs; ++k) {
         const qsl_batch_job& b = jobs_h[k];
         if (!b.field) return fail(QSL_ERR_INVALID, "job %d: null field", k);
@@ -516,31 +509,52 @@ static int batch_lists(const qsl_batch_job* jobs_h, int njobs, BatchLists& L) {
         const qsl_field* f = b.field;
         const long long padded = (b.n + 31) / 32 * 32;
         L.lines += b.n;
-        const int slot = f->layout == LAYOUT_SOA ? 0 : (f->layout == LAYOUT_F4 ? 1 : 2);
-        if (slot == 0) L.j0.push_back(batch_job_of(b, FieldSoA{f->bx, f->by, f->bz, f->d}));
-        else if (slot == 1) L.j1.push_back(batch_job_of(b, FieldF4{f->f4, f->d}));
-        else L.j2.push_back(batch_job_of(b, FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}));
+        const int slot = f->layout;
+        switch (slot) {
+            case LAYOUT_SOA: push_job(L.j[slot], batch_job_of(b, soa_of(f))); break;
+            case LAYOUT_F4: push_job(L.j[slot], batch_job_of(b, f4_of(f))); break;
+            case LAYOUT_H4B: push_job(L.j[slot], batch_job_of(b, h4b_of(f))); break;
+            default: push_job(L.j[slot], batch_job_of(b, h8c_of(f))); break;
+        }
         L.b[slot].push_back(L.b[slot].back() + padded);
         L.tw[slot] = L.tw[slot] || b.curB[0];
     }
     return QSL_OK;
 }
 
+// Serialised batch table: per store type a TraceJob<F> array and its line
+// offsets, each at a 256-byte aligned offset of one buffer.
 static void batch_layout(const BatchLists& L, qsl_batch_info* info) {
-    const size_t jsz[3] = {sizeof(TraceJob<FieldSoA>), sizeof(TraceJob<FieldF4>), sizeof(TraceJob<FieldH4B>)};
-    const size_t nj[3] = {L.j0.size(), L.j1.size(), L.j2.size()};
     int64_t off = 0;
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < kStoreTypes; ++k) {
         info->jobs_offset[k] = off;
-        off = align256(off + (int64_t)(nj[k] * jsz[k]));
+        off = align256(off + (int64_t)L.j[k].size());
         info->begin_offset[k] = off;
         off = align256(off + (int64_t)(L.b[k].size() * sizeof(long long)));
-        info->njobs[k] = (int32_t)nj[k];
+        info->njobs[k] = (int32_t)L.count(k);
         info->twist[k] = L.tw[k] ? 1 : 0;
         info->total[k] = L.b[k].back();
     }
     info->table_bytes = off;
     info->lines = L.lines;
+}
+
+// One launch per store type with jobs (a type without jobs launches nothing).
+static cudaError_t launch_slots(void* const jobs[], long long* const begin[], const int njobs[],
+                                const long long total[], const bool twist[], unsigned long long* samples,
+                                cudaStream_t st) {
+    cudaError_t e = launch_trace_batch_soa((const TraceJob<FieldSoA>*)jobs[0], begin[0], njobs[0], total[0], twist[0],
+                                           samples, st);
+    if (e == cudaSuccess)
+        e = launch_trace_batch_f4((const TraceJob<FieldF4>*)jobs[1], begin[1], njobs[1], total[1], twist[1], samples,
+                                  st);
+    if (e == cudaSuccess)
+        e = launch_trace_batch_h4b((const TraceJob<FieldH4B>*)jobs[2], begin[2], njobs[2], total[2], twist[2],
+                                   samples, st);
+    if (e == cudaSuccess)
+        e = launch_trace_batch_h8c((const TraceJob<FieldH8C>*)jobs[3], begin[3], njobs[3], total[3], twist[3],
+                                   samples, st);
+    return e;
 }
 
 extern "C" {
@@ -555,79 +569,64 @@ int qsl_batch_pack(const qsl_batch_job* jobs_h, int njobs, void* table_h, int64_
     if (!table_h) return QSL_OK;  // size query
     if (table_bytes < info_h->table_bytes) return fail(QSL_ERR_INVALID, "table buffer too small");
     char* t = (char*)table_h;
-    memcpy(t + info_h->jobs_offset[0], L.j0.data(), L.j0.size() * sizeof(TraceJob<FieldSoA>));
-    memcpy(t + info_h->jobs_offset[1], L.j1.data(), L.j1.size() * sizeof(TraceJob<FieldF4>));
-    memcpy(t + info_h->jobs_offset[2], L.j2.data(), L.j2.size() * sizeof(TraceJob<FieldH4B>));
-    for (int k = 0; k < 3; ++k) memcpy(t + info_h->begin_offset[k], L.b[k].data(), L.b[k].size() * sizeof(long long));
+    for (int k = 0; k < kStoreTypes; ++k) {
+        if (!L.j[k].empty()) memcpy(t + info_h->jobs_offset[k], L.j[k].data(), L.j[k].size());
+        memcpy(t + info_h->begin_offset[k], L.b[k].data(), L.b[k].size() * sizeof(long long));
+    }
     return QSL_OK;
 }
 
 int qsl_batch_run(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
                   qsl_stream_t stream) {
     if (!table_dev || !info_h) return fail(QSL_ERR_INVALID, "null table or info");
-    const char* t = (const char*)table_dev;
-    cudaStream_t st = (cudaStream_t)stream;
+    char* t = (char*)table_dev;
     const qsl_batch_info& I = *info_h;
-    QSL_CHECK_CUDA(launch_trace_batch_soa((const TraceJob<FieldSoA>*)(t + I.jobs_offset[0]),
-                                          (const long long*)(t + I.begin_offset[0]), I.njobs[0], I.total[0],
-                                          I.twist[0] != 0, samples_dev, st), "batch run");
-    QSL_CHECK_CUDA(launch_trace_batch_f4((const TraceJob<FieldF4>*)(t + I.jobs_offset[1]),
-                                         (const long long*)(t + I.begin_offset[1]), I.njobs[1], I.total[1],
-                                         I.twist[1] != 0, samples_dev, st), "batch run");
-    QSL_CHECK_CUDA(launch_trace_batch_h4b((const TraceJob<FieldH4B>*)(t + I.jobs_offset[2]),
-                                          (const long long*)(t + I.begin_offset[2]), I.njobs[2], I.total[2],
-                                          I.twist[2] != 0, samples_dev, st), "batch run");
+    void* jobs[kStoreTypes];
+    long long* begin[kStoreTypes];
+    int nj[kStoreTypes];
+    long long total[kStoreTypes];
+    bool tw[kStoreTypes];
+    for (int k = 0; k < kStoreTypes; ++k) {
+        jobs[k] = t + I.jobs_offset[k];
+        begin[k] = (long long*)(t + I.begin_offset[k]);
+        nj[k] = I.njobs[k];
+        total[k] = I.total[k];
+        tw[k] = I.twist[k] != 0;
+    }
+    QSL_CHECK_CUDA(launch_slots(jobs, begin, nj, total, tw, samples_dev, (cudaStream_t)stream), "batch run");
     return QSL_OK;
 }
 
 int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream, qsl_batch_t** out) {
     if (!out) return fail(QSL_ERR_INVALID, "out is null");
     *out = nullptr;
-    if (njobs < 0 || (njobs > 0 && !jobs_h)) return fail(QSL_ERR_INVALID, "bad job list");
-    std::vector<TraceJob<FieldSoA>> js0;
-    std::vector<TraceJob<FieldF4>> js1;
-    std::vector<TraceJob<FieldH4B>> js2;
-    std::vector<long long> b0{0}, b1{0}, b2{0};
-    bool tw[3] = {false, false, false};
-    int64_t lines = 0;
-    for (int k = 0; k < njobs; ++k) {
-        const qsl_batch_job& b = jobs_h[k];
-        if (!b.field) return fail(QSL_ERR_INVALID, "job %d: null field", k);
-        if (!params_ok(&b.params) || b.params.arith != QSL_ARITH_FAST)
-            return fail(QSL_ERR_INVALID, "job %d: bad params (batched jobs use fast arithmetic)", k);
-        if (b.n < 0) return fail(QSL_ERR_INVALID, "job %d: negative n", k);
-        if (b.n > 0 && !io_ok(&b.io)) return fail(QSL_ERR_INVALID, "job %d: null pointer in io", k);
-        if (b.curB[0] && (!b.curB[1] || !b.curB[2] || !b.io.twist))
-            return fail(QSL_ERR_INVALID, "job %d: twist needs curB_x/y/z and twist", k);
-        if (b.order && b.n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "job %d: order map limits n", k);
-        const qsl_field* f = b.field;
-        const long long padded = (b.n + 31) / 32 * 32;
-        lines += b.n;
-        if (f->layout == LAYOUT_SOA) {
-            js0.push_back(batch_job_of(b, FieldSoA{f->bx, f->by, f->bz, f->d}));
-            b0.push_back(b0.back() + padded);
-            tw[0] = tw[0] || b.curB[0];
-        } else if (f->layout == LAYOUT_F4) {
-            js1.push_back(batch_job_of(b, FieldF4{f->f4, f->d}));
-            b1.push_back(b1.back() + padded);
-            tw[1] = tw[1] || b.curB[0];
-        } else {
-            js2.push_back(batch_job_of(b, FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}));
-            b2.push_back(b2.back() + padded);
-            tw[2] = tw[2] || b.curB[0];
-        }
-    }
+    BatchLists L;
+    int rc = batch_lists(jobs_h, njobs, L);
+    if (rc != QSL_OK) return rc;
     qsl_batch* B = new (std::nothrow) qsl_batch();
     if (!B) return fail(QSL_ERR_NOMEM, "host allocation failed");
     cudaGetDevice(&B->device);
-    B->lines = lines;
+    B->lines = L.lines;
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = batch_upload(B, 0, js0, b0, tw[0], st);
-    if (rc == QSL_OK) rc = batch_upload(B, 1, js1, b1, tw[1], st);
-    if (rc == QSL_OK) rc = batch_upload(B, 2, js2, b2, tw[2], st);
-    if (rc != QSL_OK) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < kStoreTypes && e == cudaSuccess; ++k) {
+        B->njobs[k] = (int)L.count(k);
+        B->total[k] = L.b[k].back();
+        B->twist[k] = L.tw[k];
+        if (L.j[k].empty()) continue;
+        e = cudaMalloc(&B->jobs[k], L.j[k].size());
+        if (e == cudaSuccess) e = cudaMalloc((void**)&B->begin[k], L.b[k].size() * sizeof(long long));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(B->jobs[k], L.j[k].data(), L.j[k].size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(B->begin[k], L.b[k].data(), L.b[k].size() * sizeof(long long),
+                                cudaMemcpyHostToDevice, st);
+    }
+    // the host lists die on return: make sure the copies have read them
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
         qsl_batch_destroy(B);
-        return rc;
+        return cuda_fail(e, "batch upload");
     }
     *out = B;
     return QSL_OK;
@@ -635,13 +634,8 @@ int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream
 
 int qsl_batch_launch(const qsl_batch_t* B, unsigned long long* samples_dev, qsl_stream_t stream) {
     if (!B) return fail(QSL_ERR_INVALID, "batch is null");
-    cudaStream_t st = (cudaStream_t)stream;
-    QSL_CHECK_CUDA(launch_trace_batch_soa((const TraceJob<FieldSoA>*)B->jobs[0], B->begin[0], B->njobs[0],
-                                          B->total[0], B->twist[0], samples_dev, st), "batch launch");
-    QSL_CHECK_CUDA(launch_trace_batch_f4((const TraceJob<FieldF4>*)B->jobs[1], B->begin[1], B->njobs[1],
-                                         B->total[1], B->twist[1], samples_dev, st), "batch launch");
-    QSL_CHECK_CUDA(launch_trace_batch_h4b((const TraceJob<FieldH4B>*)B->jobs[2], B->begin[2], B->njobs[2],
-                                          B->total[2], B->twist[2], samples_dev, st), "batch launch");
+    QSL_CHECK_CUDA(launch_slots(B->jobs, B->begin, B->njobs, B->total, B->twist, samples_dev, (cudaStream_t)stream),
+                   "batch launch");
     return QSL_OK;
 }
 
@@ -649,7 +643,7 @@ int64_t qsl_batch_lines(const qsl_batch_t* B) { return B ? B->lines : 0; }
 
 int qsl_batch_destroy(qsl_batch_t* B) {
     if (!B) return QSL_OK;
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < kStoreTypes; ++k) {
         cudaFree(B->jobs[k]);
         cudaFree(B->begin[k]);
     }
@@ -721,20 +715,25 @@ int qsl_trace_scott(const qsl_field_t* field, const qsl_trace_params* prm, const
     };
     if (field->layout == LAYOUT_SOA) {
         ScottJob<FieldSoA> J;
-        J.f = FieldSoA{field->bx, field->by, field->bz, field->d};
+        J.f = soa_of(field);
         common(J);
         e = prm->arith == QSL_ARITH_EXACT ? launch_scott_exact(J, twist, n, st)
                                           : launch_scott_fast_soa(J, grad_mode, twist, n, st);
     } else if (field->layout == LAYOUT_F4) {
         ScottJob<FieldF4> J;
-        J.f = FieldF4{field->f4, field->d};
+        J.f = f4_of(field);
         common(J);
         e = launch_scott_fast_f4(J, grad_mode, twist, n, st);
-    } else {
+    } else if (field->layout == LAYOUT_H4B) {
         ScottJob<FieldH4B> J;
-        J.f = FieldH4B{field->bricks, field->scale, field->d, field->nbx, field->nby};
+        J.f = h4b_of(field);
         common(J);
         e = launch_scott_fast_h4b(J, grad_mode, twist, n, st);
+    } else {
+        ScottJob<FieldH8C> J;
+        J.f = h8c_of(field);
+        common(J);
+        e = launch_scott_fast_h8c(J, grad_mode, twist, n, st);
     }
     if (e != cudaSuccess) return cuda_fail(e, "scott launch");
     return QSL_OK;

@@ -1,5 +1,6 @@
 // Conversion of the caller's SoA field (x fastest) into the GB300 stores:
-// interleaved float4 nodes and fp16 bricks with per-brick scales.
+// interleaved float4 nodes, fp16 bricks with per-brick scales and fp16 cell
+// records with per-cell power-of-two scales.
 #include "qsl_internal.h"
 
 namespace qsl {
@@ -71,6 +72,73 @@ cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, D
     const long long nb = (long long)nbx * nby * nbz;
     if (nb <= 0 || nb > 0x7fffffffLL) return cudaErrorInvalidValue;
     k_pack_h4b<<<(unsigned)nb, 256, 0, st>>>(bx, by, bz, d, nbx, nby, bricks, scale);
+    return cudaGetLastError();
+}
+
+// One thread per cell record.  The cell's 8 corner nodes are scaled by the
+// power of two 2^e with max |component| = m 2^e, m in [0.5, 1) (e clamped to
+// [-100, 127]), and rounded to fp16.  Scaling by a power of two commutes with
+// the rounding, so a node has the same value in every cell that holds it and
+// the interpolated field stays continuous across cell faces.  Records of
+// cells outside the grid (brick padding) are zero.
+__global__ void __launch_bounds__(256) k_pack_h8c(const float* __restrict__ bx, const float* __restrict__ by,
+                                                  const float* __restrict__ bz, Dims d, int nbx, int nby,
+                                                  long long nrec, uint4* __restrict__ cells) {
+    const int64_t sy = d.nx, sz = (int64_t)d.nx * d.ny;
+    for (long long rec = (long long)blockIdx.x * blockDim.x + threadIdx.x; rec < nrec;
+         rec += (long long)gridDim.x * blockDim.x) {
+        const long long brick = rec >> 9;
+        const int local = (int)(rec & 511);
+        const int bi = (int)(brick % nbx), bj = (int)((brick / nbx) % nby), bk = (int)(brick / ((long long)nbx * nby));
+        const int ix = bi * 8 + (local & 7), iy = bj * 8 + ((local >> 3) & 7), iz = bk * 8 + (local >> 6);
+        uint4* out = cells + rec * CELL_RECORD_U4;
+        if (ix > d.nx - 2 || iy > d.ny - 2 || iz > d.nz - 2) {
+            const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+            out[0] = zero; out[1] = zero; out[2] = zero; out[3] = zero;
+            continue;
+        }
+        // v[m][q]: component m of corner q = (dx << 2) | (dy << 1) | dz
+        float v[3][8];
+        float mx = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int64_t o = (ix + ((q >> 2) & 1)) + sy * (iy + ((q >> 1) & 1)) + sz * (iz + (q & 1));
+            v[0][q] = __ldg(bx + o);
+            v[1][q] = __ldg(by + o);
+            v[2][q] = __ldg(bz + o);
+            mx = fmaxf(mx, fmaxf(fabsf(v[0][q]), fmaxf(fabsf(v[1][q]), fabsf(v[2][q]))));
+        }
+        int e = 0;
+        if (mx > 0.f && isfinite(mx)) {
+            frexpf(mx, &e);
+            e = max(-100, min(127, e));
+        }
+        const float inv = ldexpf(1.f, -e);
+        unsigned w[16];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const __half2 h = __floats2half2_rn(v[m][k] * inv, v[m][4 + k] * inv);
+                w[4 * m + k] = *reinterpret_cast<const unsigned*>(&h);
+            }
+        }
+        w[12] = __float_as_uint(ldexpf(1.f, e));
+        w[13] = 0u; w[14] = 0u; w[15] = 0u;
+        out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+        out[1] = make_uint4(w[4], w[5], w[6], w[7]);
+        out[2] = make_uint4(w[8], w[9], w[10], w[11]);
+        out[3] = make_uint4(w[12], w[13], w[14], w[15]);
+    }
+}
+
+cudaError_t launch_pack_h8c(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
+                            uint4* cells, cudaStream_t st) {
+    const long long nrec = (long long)nbx * nby * nbz * 512;
+    if (nrec <= 0) return cudaErrorInvalidValue;
+    long long g = (nrec + 255) / 256;
+    if (g > 65535LL * 64) g = 65535LL * 64;
+    k_pack_h8c<<<(unsigned)g, 256, 0, st>>>(bx, by, bz, d, nbx, nby, nrec, cells);
     return cudaGetLastError();
 }
 

@@ -10,6 +10,12 @@
 //               nodes), each node four fp16 (Bx, By, Bz, 0) scaled by a
 //               per-brick float; one corner is one 8-byte load and a whole
 //               trilinear stencil never leaves its brick.
+//   FieldH8C  — fp16 cell records: each cell holds the 8 corner vectors it
+//               interpolates (64 bytes, power-of-two scale per cell), so a
+//               trilinear sample is one 32-byte and one 16-byte load, each a
+//               single L1 sector, instead of eight node loads spread over
+//               several sectors.  Nodes are stored up to 8 times over (about
+//               64 B per cell against 11 B for FieldH4B).
 //
 // Sampling comes in two arithmetics:
 //   exact — the reference's rounding sequence (weights formed in double and
@@ -109,6 +115,45 @@ struct FieldH4B {
             c[q] = v3(xy.x, xy.y, z);
         }
         return __ldg(scale + brick);
+    }
+};
+
+// fp16 cell records.  Record (64 bytes, 32-byte aligned) as 16 32-bit words:
+// w[0..3] Bx, w[4..7] By, w[8..11] Bz, where word k of a component is the
+// fp16 pair (low half: corner dx = 0, high half: corner dx = 1) of corner
+// column k = (dy << 1) | dz; w[12] the cell's scale (a power of two, so the
+// fp16 value of a node is the same in every cell that holds it); w[13..15]
+// zero.  Cells are grouped in 8^3 bricks; cell (a, b, c) of brick
+// (bi, bj, bk) is record 512 * (bi + nbx (bj + nby bk)) + a + 8 (b + 8 c).
+constexpr int CELL_RECORD_U4 = 4;  // uint4 per record
+struct FieldH8C {
+    const uint4* cells;
+    Dims d;
+    int nbx, nby;  // bricks along x and y
+    __device__ __forceinline__ unsigned long long record_index(int ix, int iy, int iz) const {
+        // brick indices fit 32 bits (field stores hold < 1.1e12 nodes)
+        const unsigned brick =
+            (unsigned)(ix >> 3) + (unsigned)nbx * ((unsigned)(iy >> 3) + (unsigned)nby * (unsigned)(iz >> 3));
+        const unsigned local = (unsigned)((ix & 7) + 8 * ((iy & 7) + 8 * (iz & 7)));
+        return ((unsigned long long)brick << 9) + local;
+    }
+    __device__ __forceinline__ const uint4* record(int ix, int iy, int iz) const {
+        return cells + record_index(ix, iy, iz) * CELL_RECORD_U4;
+    }
+    __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
+        const uint4* r = record(ix, iy, iz);
+        const uint4 wx = __ldg(r), wy = __ldg(r + 1), wz = __ldg(r + 2);
+        const unsigned ux[4] = {wx.x, wx.y, wx.z, wx.w}, uy[4] = {wy.x, wy.y, wy.z, wy.w},
+                       uz[4] = {wz.x, wz.y, wz.z, wz.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float2 x = __half22float2(*reinterpret_cast<const __half2*>(&ux[k]));
+            const float2 y = __half22float2(*reinterpret_cast<const __half2*>(&uy[k]));
+            const float2 z = __half22float2(*reinterpret_cast<const __half2*>(&uz[k]));
+            c[k] = v3(x.x, y.x, z.x);      // dx = 0
+            c[4 + k] = v3(x.y, y.y, z.y);  // dx = 1
+        }
+        return __ldg(reinterpret_cast<const float*>(r + 3));
     }
 };
 
@@ -284,6 +329,92 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
         r = v3(r.x * s, r.y * s, r.z * s);
     }
     return r;
+}
+
+// (1 - r) lo + r hi of one fp16 pair (w = the fp16 pair (1 - r, r)), the
+// products exact and the sum rounded once.
+__device__ __forceinline__ float xmix(unsigned pair, unsigned w) {
+    float d;
+    asm("{\n\t"
+        ".reg .f16 l, h, wo, wr;\n\t"
+        ".reg .f32 t;\n\t"
+        "mov.b32 {l, h}, %1;\n\t"
+        "mov.b32 {wo, wr}, %2;\n\t"
+        "fma.rn.f32.f16 t, l, wo, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %0, h, wr, t;\n\t"
+        "}"
+        : "=f"(d)
+        : "r"(pair), "r"(w));
+    return d;
+}
+
+// 32-byte read-only load (one L1 sector); p must be 32-byte aligned.
+__device__ __forceinline__ void ldg_v8(const void* p, unsigned (&v)[8]) {
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+        : "l"(p));
+}
+
+// Fast sample of the cell-record store: the same arithmetic as the fp16
+// brick store's fast sample (x fraction on the 2^-11 grid, fp16 x-lerps by
+// mixed-precision FMA, packed y/z lerps), with Bx/By in one 32-byte load
+// (WIDE) or two 16-byte loads, and Bz in one 16-byte load.  The 32-byte load
+// is used in code inlined into kernels only: ptxas 13.0 fails (segmentation
+// fault) on it inside an out-of-line device function called from several
+// kernels of one translation unit.
+template <bool WIDE>
+__device__ __forceinline__ float3 sample_h8c(const FieldH8C& f, float3 p, bool unit) {
+    int ix, iy, iz;
+    float rx, ry, rz;
+    locate_fast(p.x, f.d.nx, ix, rx);
+    locate_fast(p.y, f.d.ny, iy, ry);
+    locate_fast(p.z, f.d.nz, iz, rz);
+    const float rq = rintf(rx * 2048.f) * (1.f / 2048.f);
+    const __half2 wh = __floats2half2_rn(1.f - rq, rq);  // exact: both on the 2^-11 grid
+    const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
+    const uint4* r = f.record(ix, iy, iz);
+    uint4 bx, by;
+    if (WIDE) {
+        unsigned xy[8];
+        ldg_v8(r, xy);
+        bx = make_uint4(xy[0], xy[1], xy[2], xy[3]);
+        by = make_uint4(xy[4], xy[5], xy[6], xy[7]);
+    } else {
+        bx = __ldg(r);
+        by = __ldg(r + 1);
+    }
+    const uint4 bz = __ldg(r + 2);
+    const float2 e0 = make_float2(xmix(bx.x, w), xmix(by.x, w)), e1 = make_float2(xmix(bx.y, w), xmix(by.y, w)),
+                 e2 = make_float2(xmix(bx.z, w), xmix(by.z, w)), e3 = make_float2(xmix(bx.w, w), xmix(by.w, w));
+    const float ez0 = xmix(bz.x, w), ez1 = xmix(bz.y, w), ez2 = xmix(bz.z, w), ez3 = xmix(bz.w, w);
+    const float oy = 1.f - ry, oz = 1.f - rz;
+    const float2 g0 = lerp2(e0, e2, oy, ry), g1 = lerp2(e1, e3, oy, ry);
+    const float gz0 = fmaf(ez2, ry, ez0 * oy), gz1 = fmaf(ez3, ry, ez1 * oy);
+    const float2 rxy = lerp2(g0, g1, oz, rz);
+    float3 v = v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
+    if (unit) {
+        const float inv = rsqrtf(fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z)));
+        v = v3(v.x * inv, v.y * inv, v.z * inv);
+    } else {
+        const float s = __ldg(reinterpret_cast<const float*>(r + 3));
+        v = v3(v.x * s, v.y * s, v.z * s);
+    }
+    return v;
+}
+
+template <>
+__device__ __forceinline__ float3 sample<false, FieldH8C>(const FieldH8C& f, float3 p, bool unit) {
+    return sample_h8c<true>(f, p, unit);
+}
+
+// sample() for out-of-line device functions (see sample_h8c).
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 sample_outlined(const F& f, float3 p, bool unit) {
+    return sample<EXACT>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample_outlined<false, FieldH8C>(const FieldH8C& f, float3 p, bool unit) {
+    return sample_h8c<false>(f, p, unit);
 }
 
 // Position clamped into [1e-4, n-1-1e-4] as the scalar interpolator of the

@@ -9,7 +9,8 @@
 
 namespace qsl {
 
-enum Layout { LAYOUT_SOA = 0, LAYOUT_F4 = 1, LAYOUT_H4B = 2 };
+enum Layout { LAYOUT_SOA = 0, LAYOUT_F4 = 1, LAYOUT_H4B = 2, LAYOUT_H8C = 3 };
+constexpr int kStoreTypes = 4;
 enum Schedule { SCHED_QUEUE = 0, SCHED_STATIC = 1 };
 
 constexpr int kTraceBlock = 128;
@@ -22,12 +23,14 @@ int persistent_grid(const void* kernel, int block, size_t smem = 0);
 cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
                                cudaStream_t st);
 
-// trace_fast.cu
+// trace_fast_<store>.cu
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
                                   cudaStream_t st);
 cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
                                  cudaStream_t st);
 cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st);
+cudaError_t launch_trace_fast_h8c(const TraceJob<FieldH8C>& J, bool twist, Schedule sched, long long n_host,
                                   cudaStream_t st);
 
 // Scott tracer (one line per thread); exact arithmetic uses GRAD_FD
@@ -37,18 +40,24 @@ cudaError_t launch_scott_fast_soa(const ScottJob<FieldSoA>& J, int grad, bool tw
 cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid, cudaStream_t st);
 cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool twist, long long n_grid,
                                   cudaStream_t st);
+cudaError_t launch_scott_fast_h8c(const ScottJob<FieldH8C>& J, int grad, bool twist, long long n_grid,
+                                  cudaStream_t st);
 
-// Batched trace over a job table in device memory (trace_fast.cu)
+// Batched trace over a job table in device memory (trace_fast_<store>.cu)
 cudaError_t launch_trace_batch_soa(const TraceJob<FieldSoA>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, cudaStream_t st);
 cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs, long long total,
                                   bool twist, unsigned long long* samples, cudaStream_t st);
 cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, cudaStream_t st);
+cudaError_t launch_trace_batch_h8c(const TraceJob<FieldH8C>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st);
 
 // field_store.cu
 cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);
 cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
                             uint2* bricks, float* scale, cudaStream_t st);
+cudaError_t launch_pack_h8c(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
+                            uint4* cells, cudaStream_t st);
 
 }  // namespace qsl

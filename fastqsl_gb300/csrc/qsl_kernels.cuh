@@ -1,5 +1,7 @@
-// FP32 tracer kernels with fused multiply-add: the plain SoA form (the
-// reference's field layout) and the interleaved-float4 and fp16-brick stores.
+// Kernel templates of the fast tracers and their launchers, instantiated per
+// field store by one translation unit each (trace_fast_soa.cu, trace_fast_f4.cu,
+// trace_fast_h4b.cu, trace_fast_h8c.cu), compiled in parallel.
+#pragma once
 #include "qsl_internal.h"
 
 namespace qsl {
@@ -41,10 +43,11 @@ static cudaError_t launch_fast_minb(const TraceJob<F>& J, bool twist, Schedule s
 template <class F>
 static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
     switch (J.occupancy) {
+        case 6: return launch_fast_minb<F, 6>(J, twist, sched, n_host, st);
+        case 7: return launch_fast_minb<F, 7>(J, twist, sched, n_host, st);
         case 8: return launch_fast_minb<F, 8>(J, twist, sched, n_host, st);
         case 9: return launch_fast_minb<F, 9>(J, twist, sched, n_host, st);
         case 10: return launch_fast_minb<F, 10>(J, twist, sched, n_host, st);
-        case 12: return launch_fast_minb<F, 12>(J, twist, sched, n_host, st);
         default: return launch_fast_minb<F, 1>(J, twist, sched, n_host, st);
     }
 }
@@ -68,18 +71,6 @@ static cudaError_t launch_scott(const ScottJob<F>& J, int grad, bool twist, long
     return cudaGetLastError();
 }
 
-cudaError_t launch_scott_fast_soa(const ScottJob<FieldSoA>& J, int grad, bool twist, long long n_grid,
-                                  cudaStream_t st) {
-    return launch_scott(J, grad, twist, n_grid, st);
-}
-cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid, cudaStream_t st) {
-    return launch_scott(J, grad, twist, n_grid, st);
-}
-cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool twist, long long n_grid,
-                                  cudaStream_t st) {
-    return launch_scott(J, grad, twist, n_grid, st);
-}
-
 // Batched trace: one line per thread, 8 resident blocks/SM (the register
 // budget measured best for the lockstep tracer).
 template <bool TWIST, class F>
@@ -98,32 +89,6 @@ static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin,
     if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
     else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
     return cudaGetLastError();
-}
-
-cudaError_t launch_trace_batch_soa(const TraceJob<FieldSoA>* jobs, const long long* begin, int njobs,
-                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
-    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
-}
-cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs, long long total,
-                                  bool twist, unsigned long long* samples, cudaStream_t st) {
-    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
-}
-cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
-                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
-    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
-}
-
-cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
-                                  cudaStream_t st) {
-    return launch_fast(J, twist, sched, n_host, st);
-}
-cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
-                                 cudaStream_t st) {
-    return launch_fast(J, twist, sched, n_host, st);
-}
-cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Schedule sched, long long n_host,
-                                  cudaStream_t st) {
-    return launch_fast(J, twist, sched, n_host, st);
 }
 
 }  // namespace qsl

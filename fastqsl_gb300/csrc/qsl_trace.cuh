@@ -163,18 +163,19 @@ __device__ __forceinline__ float3 step_rk4(const F& f, float3 p, float h, unsign
 }
 
 // RK4 in the face-normal coordinate, dx/dq = b / b_d over dq = h
-// (RK4_boundary, TraceBlineAdaptive.cu:286-307).
+// (RK4_boundary, TraceBlineAdaptive.cu:286-307).  Out of line (it runs once
+// per line end); the store view is taken by value so that the caller's copy
+// never has its address taken.  4 field samples.
 template <bool EXACT, class F>
-__device__ __noinline__ float3 step_rk4_normal(const F& f, float3 p, float h, int d, unsigned& ns) {
-    float3 b = sample<EXACT>(f, p, true);
+__device__ __noinline__ float3 step_rk4_normal(const F f, float3 p, float h, int d) {
+    float3 b = sample_outlined<EXACT>(f, p, true);
     const float3 k1 = b / comp(b, d);
-    b = sample<EXACT>(f, p + (h * k1) / 2.f, true);
+    b = sample_outlined<EXACT>(f, p + (h * k1) / 2.f, true);
     const float3 k2 = b / comp(b, d);
-    b = sample<EXACT>(f, p + (h * k2) / 2.f, true);
+    b = sample_outlined<EXACT>(f, p + (h * k2) / 2.f, true);
     const float3 k3 = b / comp(b, d);
-    b = sample<EXACT>(f, p + h * k3, true);
+    b = sample_outlined<EXACT>(f, p + h * k3, true);
     const float3 k4 = b / comp(b, d);
-    ns += 4;
     const float c = EXACT ? (float)(1.0 / 6.0 * (double)h) : h * (1.f / 6.f);
     return p + c * (((k1 + 2.f * k2) + 2.f * k3) + k4);
 }
@@ -353,7 +354,8 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
                     L.out.y = (L.p.y * (q2 - qmid) + p2.y * (qmid - q1)) / (q2 - q1);
                     L.out.z = (L.p.z * (q2 - qmid) + p2.z * (qmid - q1)) / (q2 - q1);
                 } else {
-                    L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d, ns);
+                    L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d);
+                    ns += 4;
                 }
                 len_add(L, (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(u1, d))),
                         fabsf(qmid - q1) / (1e-4f + fabsf(comp(u1, d))));

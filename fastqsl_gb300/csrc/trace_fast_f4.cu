@@ -1,0 +1,21 @@
+// Fast tracer kernels on the interleaved float4 store (FieldF4).
+#include "qsl_kernels.cuh"
+
+namespace qsl {
+
+cudaError_t launch_trace_fast_f4(const TraceJob<FieldF4>& J, bool twist, Schedule sched, long long n_host,
+                                  cudaStream_t st) {
+    return launch_fast(J, twist, sched, n_host, st);
+}
+
+cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twist, long long n_grid,
+                                  cudaStream_t st) {
+    return launch_scott(J, grad, twist, n_grid, st);
+}
+
+cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs,
+                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
+}
+
+}  // namespace qsl

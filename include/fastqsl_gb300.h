@@ -143,7 +143,9 @@ int qsl_trace_all_bline(int integrator, int arith, const float *Bx, const float 
 enum qsl_layout {
     QSL_LAYOUT_SOA = 0, /* the caller's Bx, By, Bz in place */
     QSL_LAYOUT_F4 = 1,  /* interleaved float4 per node (16 B/node) */
-    QSL_LAYOUT_H4B = 2  /* fp16 8^3-cell bricks with a +1 apron and a float scale per brick */
+    QSL_LAYOUT_H4B = 2, /* fp16 8^3-cell bricks with a +1 apron and a float scale per brick */
+    QSL_LAYOUT_H8C = 3  /* fp16 cell records: each cell's 8 corner vectors in 64 B, power-of-two
+                           scale per cell (fastest fp16 store; ~64 B per cell) */
 };
 typedef struct qsl_field qsl_field_t;
 
@@ -191,7 +193,7 @@ typedef struct qsl_sched {
                                     `stream` (stream-ordered) and freed after the launch */
     unsigned long long *samples; /* optional: accumulates the number of trilinear field samples */
     int32_t occupancy;           /* fast kernels: register budget for this many resident 128-thread
-                                    blocks per SM (0 = compiler's choice, or 8, 9, 10, 12) */
+                                    blocks per SM (0 = compiler's choice, or 6, 7, 8, 9, 10) */
 } qsl_sched;
 
 /* Traces n seeds (or *n_dev seeds when n_dev is set; then the outputs must
@@ -232,9 +234,11 @@ typedef struct qsl_batch qsl_batch_t;
  * copies those bytes to device memory (256-byte aligned) by any means and
  * qsl_batch_run launches from it.  The table holds device addresses of the
  * jobs' fields and buffers, which must stay valid until the run completes. */
+/* Per store type (index = enum qsl_layout): offsets into the table, lines
+ * and job counts. */
 typedef struct qsl_batch_info {
-    int64_t jobs_offset[3], begin_offset[3], total[3];
-    int32_t njobs[3], twist[3];
+    int64_t jobs_offset[4], begin_offset[4], total[4];
+    int32_t njobs[4], twist[4];
     int64_t table_bytes, lines;
 } qsl_batch_info;
 int qsl_batch_pack(const qsl_batch_job *jobs_h, int njobs, void *table_h, int64_t table_bytes,

@@ -20,8 +20,8 @@ pytestmark = pytest.mark.gpu
 def _specs(device="cuda"):
     from fastqsl_gb300 import api, synthetic as S
     rng = np.random.default_rng(42)
-    shapes = [(48, 48, 48), (64, 56, 40), (40, 40, 32), (56, 48, 48)]
-    layouts = ["h4b", "f4", "soa", "h4b"]
+    shapes = [(48, 48, 48), (64, 56, 40), (40, 40, 32), (56, 48, 48), (44, 52, 36)]
+    layouts = ["h4b", "f4", "soa", "h4b", "h8c"]
     specs, stores = [], []
     for k, (shape, layout) in enumerate(zip(shapes, layouts)):
         spec = S.charges_random(100 + k, shape, int(rng.integers(4, 12)))

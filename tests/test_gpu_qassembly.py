@@ -134,7 +134,7 @@ def test_notebook_workflow_through_dropin(cuda):
     assert np.median(d) <= 1e-6 and np.quantile(d, 0.99) <= 1e-2, (np.median(d), np.quantile(d, 0.99))
 
 
-@pytest.mark.parametrize("layout", ["f4", "soa"])
+@pytest.mark.parametrize("layout", ["f4", "soa", "h4b", "h8c"])
 def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     from fastqsl_gb300 import api, synthetic as S
     from oracle import qassembly as QA
@@ -155,4 +155,7 @@ def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     assert nan_same.mean() >= 0.99
     ok = ~np.isnan(Q) & ~np.isnan(Qref)
     d = np.abs(np.log10(Q[ok]) - np.log10(Qref[ok]))
-    assert np.median(d) <= 1e-3 and np.quantile(d, 0.99) <= 1e-2, (np.median(d), np.quantile(d, 0.99))
+    # fp16 node values (h4b, h8c): the bar of the fp16 form is the median;
+    # its stated tail on this steep small field is within 5e-2
+    p99_bar = 5e-2 if layout in ("h4b", "h8c") else 1e-2
+    assert np.median(d) <= 1e-3 and np.quantile(d, 0.99) <= p99_bar, (np.median(d), np.quantile(d, 0.99))

@@ -70,7 +70,8 @@ def test_dropin_scott_exact_matches_oracle(cuda, oracle_port):
     assert (rel <= 1e-3).mean() >= 0.99, np.quantile(rel, [0.5, 0.99])
 
 
-@pytest.mark.parametrize("layout,grad", [("soa", "fd"), ("soa", "analytic"), ("h4b", "analytic")])
+@pytest.mark.parametrize("layout,grad", [("soa", "fd"), ("soa", "analytic"), ("h4b", "analytic"), ("h8c", "analytic"),
+                                         ("h8c", "fd")])
 def test_fast_scott_vs_fp64_oracle(cuda, oracle_port, layout, grad):
     from fastqsl_gb300 import api
     Bx, By, Bz, xs, ys, zs = _case()
