@@ -773,6 +773,13 @@ int qsl_trace_all_bline_scott(const float* Bx, const float* By, const float* Bz,
     return QSL_OK;
 }
 
+void qsl_params_reference_stretch(qsl_trace_params* p) {
+    qsl_params_reference_rkf45(p);
+    p->len_ratio = 2.0;         // x the summed coordinate extents
+    p->max_steps = 0x7fffffff;  // the reference has no step limit
+    p->boundary_twist = 1;
+}
+
 void qsl_params_reference_scott(qsl_trace_params* p) {
     qsl_params_reference_rkf45(p);
     p->tol_law = QSL_TOL_ABSOLUTE;

@@ -10,6 +10,10 @@ the presets below reproduce them:
   rejection, length limit 3*(nx+ny+nz), 500000 steps.
 * Scott — ``fastqslpy/cu/TraceBlineScott.cu:10-14``: length limit
   2*(nx+ny+nz), 10000 steps shared by both directions, tol 1e-3*tol_coef.
+* Stretched-grid RKF45 — ``fastqslpy/cu/TraceBlineAdaptiveStretch.cu:10-12,
+  336-371``: the RKF45 settings with length limit 2 x the summed coordinate
+  extents, no step limit (capped here at 2^31 - 1), exit-segment twist term
+  (``:401-404``).
 """
 import ctypes
 
@@ -61,6 +65,10 @@ def reference_scott(arith=ARITH_EXACT) -> TraceParams:
     """The Scott tracer's settings; its tolerance is 1e-3*tol_coef (the
     reference leaves the variable uninitialised, TraceBlineScott.cu:352,378)."""
     return TraceParams(RKF45, TOL_ABSOLUTE, 1e-3, 0.1, 100.0, 0.618, 2.0, 10000, 0, arith)
+
+
+def reference_stretch(arith=ARITH_EXACT) -> TraceParams:
+    return TraceParams(RKF45, TOL_REFERENCE, 1e-3, 0.1, 100.0, 0.618, 2.0, 2**31 - 1, 1, arith)
 
 
 def absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=ARITH_FAST) -> TraceParams:

@@ -173,6 +173,59 @@ def charges_tube(seed, shape, n_charges=8) -> FieldSpec:
                      f"charges{n_charges}+tube-{'x'.join(map(str, shape))}")
 
 
+# --------------------------------------------------------------------------
+# Stretched (non-uniform) grids
+# --------------------------------------------------------------------------
+
+def stretched_axes(shape, extent=(12.0, 10.0, 10.0), z_ratio=1.06):
+    """Node coordinates of a stretched grid like the reference's stretched
+    demo (TD7stretch1.sav: x, y uniform, z spacing growing with height):
+    x and y uniform over [-extent/2, extent/2], z from 0 with spacing growing
+    geometrically by z_ratio per cell, scaled to `extent[2]`.  float32."""
+    nx, ny, nz = shape
+    xa = np.linspace(-extent[0] / 2, extent[0] / 2, nx).astype(np.float32)
+    ya = np.linspace(-extent[1] / 2, extent[1] / 2, ny).astype(np.float32)
+    dz = z_ratio ** np.arange(nz - 1)
+    za = np.concatenate([[0.0], np.cumsum(dz)])
+    za = (za * (extent[2] / za[-1])).astype(np.float32)
+    return xa, ya, za
+
+
+def make_field_coords(spec: FieldSpec, xa, ya, za):
+    """The field of `spec` (charges only) sampled at the nodes of a
+    rectilinear grid with coordinates xa, ya, za; (nx, ny, nz) float32
+    Fortran-order arrays, the same float64 arithmetic as make_field."""
+    x = np.asarray(xa, np.float64).reshape(-1, 1, 1)
+    y = np.asarray(ya, np.float64).reshape(1, -1, 1)
+    z = np.asarray(za, np.float64).reshape(1, 1, -1)
+    shp = (x.shape[0], y.shape[1], z.shape[2])
+    bx = np.zeros(shp)
+    by = np.zeros(shp)
+    bz = np.zeros(shp)
+    for (cx, cy, cz), q in zip(spec.charges.pos.tolist(), spec.charges.q.tolist()):
+        dx = x - cx
+        dy = y - cy
+        dz = z - cz
+        r2 = (dx * dx + dy * dy) + dz * dz
+        inv = q / (r2 * np.sqrt(r2))
+        bx = bx + dx * inv
+        by = by + dy * inv
+        bz = bz + dz * inv
+    return tuple(np.asfortranarray(a.astype(np.float32)) for a in (bx, by, bz))
+
+
+def bipole4_stretch(seed=0, shape=(48, 40, 36)) -> FieldSpec:
+    """4 charges at depth 0.8 below z = 0 of the stretched_axes box, (x, y)
+    uniform in the central 80 %, strengths +-U(0.5, 1.5) shifted to net zero."""
+    rng = np.random.default_rng(seed)
+    xy = rng.uniform(-0.4, 0.4, size=(4, 2)) * np.array([12.0, 10.0])
+    mag = rng.uniform(0.5, 1.5, size=4)
+    q = mag * rng.choice([-1.0, 1.0], size=4)
+    q = q - q.mean()
+    pos = np.column_stack([xy, np.full(4, -0.8)])
+    return FieldSpec(tuple(shape), ChargeSet(pos, q), None, f"charges4-stretch-{'x'.join(map(str, shape))}")
+
+
 def plane_seeds(x_range, y_range, nx, ny, z, indexing="xy"):
     """Seed grid on a z = const plane, built like the reference notebooks
     (``cupy.linspace`` per axis, ``meshgrid``, flattened).  Returns

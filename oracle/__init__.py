@@ -79,12 +79,19 @@ TRACE_KEYS_I32 = ["flag_start", "flag_end", "B_flag"]
 
 
 def trace_all(impl, Bx, By, Bz, xs, ys, zs, cross_dir=(0, 0, 1), s_len=0.125, tol_coef=1.0,
-              params=None, curB=None, threads=None):
-    """Traces every seed.  impl: 'port32', 'port64' or 'ref_rk4'/'ref_rkf45'
-    (the reference build ignores `params`: its settings are compiled in).
-    Returns a dict of numpy arrays keyed like the reference kernel's outputs,
-    plus 'LineLen', 'twist' and (port) 'samples'."""
+              params=None, curB=None, threads=None, coords=None, uni=False):
+    """Traces every seed.  impl: 'port32', 'port32cr', 'port64' or
+    'ref_rk4'/'ref_rkf45'/'ref_stretch' (the reference build ignores `params`:
+    its settings are compiled in).  coords=(xa, ya, za): node coordinates of
+    a stretched grid (TraceBlineAdaptiveStretch.cu), uni: its uniform-spacing
+    index formula.  Returns a dict of numpy arrays keyed like the reference
+    kernel's outputs, plus 'LineLen', 'twist' and (port) 'samples'."""
     flat, shape = _field_ptrs(Bx, By, Bz)
+    stretch = coords is not None
+    if impl == "ref_stretch" and not stretch:
+        raise ValueError("ref_stretch needs coords")
+    ax = [_f32(c) for c in coords] if stretch else []
+    args_coords = [_p(a, _f32p) for a in ax] + [ctypes.c_int(int(bool(uni)))] if stretch else []
     xs, ys, zs = _f32(xs), _f32(ys), _f32(zs)
     n = xs.size
     out = {k: np.zeros(n, np.float32) for k in TRACE_KEYS_F32}
@@ -108,17 +115,18 @@ def trace_all(impl, Bx, By, Bz, xs, ys, zs, cross_dir=(0, 0, 1), s_len=0.125, to
         lib = ref_lib(impl.split("_", 1)[1])
         if threads:
             lib.qref_set_threads(int(threads))
-        rc = lib.qref_trace_all(*args_field, *args_cur, _p(out["twist"], _f64p), ctypes.c_int(int(twist_on)),
-                                *common, ctypes.c_float(s_len), ctypes.c_ulonglong(n),
-                                _p(out["LineLen"], _f64p), ctypes.c_float(tol_coef))
+        fn = lib.qref_trace_all_stretch if stretch else lib.qref_trace_all
+        rc = fn(*args_field, *args_coords, *args_cur, _p(out["twist"], _f64p), ctypes.c_int(int(twist_on)),
+                *common, ctypes.c_float(s_len), ctypes.c_ulonglong(n),
+                _p(out["LineLen"], _f64p), ctypes.c_float(tol_coef))
     else:
         lib = port_lib()
-        fn = getattr(lib, _PREFIX[impl] + "trace_all")
+        fn = getattr(lib, _PREFIX[impl] + ("trace_all_stretch" if stretch else "trace_all"))
         if params is None:
             raise ValueError("port oracle needs params")
         samples = ctypes.c_int64(0)
         _set_threads(threads)
-        rc = fn(*args_field, *args_cur, _p(out["twist"], _f64p), ctypes.c_int(int(twist_on)),
+        rc = fn(*args_field, *args_coords, *args_cur, _p(out["twist"], _f64p), ctypes.c_int(int(twist_on)),
                 *common, ctypes.c_float(s_len), ctypes.c_int64(n), _p(out["LineLen"], _f64p),
                 ctypes.c_float(tol_coef), ctypes.byref(params), ctypes.byref(samples))
         out["samples"] = int(samples.value)
@@ -238,3 +246,39 @@ class Probe:
         o = np.zeros(9, np.float32)
         err = self._fn("rkf45_scott")(*self.fp, self.sp, _p(_f32(v9), _f32p), ctypes.c_float(h), _p(o, _f32p))
         return o, float(err)
+
+
+class StretchProbe:
+    """Single-function calls of the stretched-grid tracer into one
+    implementation ('port32', 'port64', 'ref_stretch')."""
+
+    def __init__(self, impl, Bx, By, Bz, coords, uni=False):
+        flat, self.shape = _field_ptrs(Bx, By, Bz)
+        self.flat = flat
+        self.ax = [_f32(c) for c in coords]
+        self.fp = [_p(a, _f32p) for a in flat]
+        self.sp = _p(self.shape, _i32p)
+        self.cp = [_p(a, _f32p) for a in self.ax]
+        self.uni = ctypes.c_int(int(bool(uni)))
+        if impl.startswith("ref"):
+            self.lib, self.pre = ref_lib("stretch"), "qref_"
+        else:
+            self.lib, self.pre = port_lib(), _PREFIX[impl]
+
+    def _fn(self, name):
+        return getattr(self.lib, self.pre + name)
+
+    def index(self, p, axis, uni=None):
+        a = self.ax[axis]
+        u = bool(self.uni.value) if uni is None else uni
+        return int(self._fn("index_uni" if u else "index_bisect")(ctypes.c_float(p), ctypes.c_int(a.size),
+                                                                 _p(a, _f32p)))
+
+    def interp(self, p, unit=True):
+        o = np.zeros(3, np.float32)
+        self._fn("interp_stretch")(*self.fp, self.sp, *self.cp, self.uni, _p(_f32(p), _f32p), ctypes.c_int(int(unit)),
+                                   _p(o, _f32p))
+        return o
+
+    def checkflag(self, p):
+        return int(self._fn("checkflag_stretch")(self.sp, *self.cp, self.uni, _p(_f32(p), _f32p)))

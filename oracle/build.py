@@ -4,7 +4,7 @@
   (FP32 reference-parity ``qo32_*``, the same with a correctly rounded
   power ``qo32cr_*``, and FP64 ``qo64_*``), OpenMP-parallel.
   Built on every machine (it is the checker on the GPU host as well).
-* ``oracle/_ref/libqslref_{rk4,rkf45,scott}.so`` — the reference's own kernels
+* ``oracle/_ref/libqslref_{rk4,rkf45,scott,stretch}.so`` — the reference's own kernels
   compiled for the host by ``oracle/build_ref.sh``; only where the reference
   checkout exists.
 
@@ -61,7 +61,7 @@ def build_ref(root=REFERENCE_ROOT, force=False):
     reference checkout is absent."""
     if not reference_available(root):
         return False
-    outs = [os.path.join(REF_DIR, f"libqslref_{k}.so") for k in ("rk4", "rkf45", "scott")]
+    outs = [os.path.join(REF_DIR, f"libqslref_{k}.so") for k in ("rk4", "rkf45", "scott", "stretch")]
     srcs = [os.path.join(HERE, "ref_shim", f) for f in ("ref_driver.cpp", "cuda_runtime.h", "exports.map")]
     srcs.append(os.path.join(HERE, "build_ref.sh"))
     if not force and all(_newer(o, srcs) for o in outs):

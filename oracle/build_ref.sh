@@ -23,8 +23,8 @@ flags=(-O2 -std=c++17 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math
        -fvisibility=hidden -w -I "$here/ref_shim" -I "$cu" -I "$cuda_inc"
        -Wl,--version-script="$here/ref_shim/exports.map")
 pids=()
-for k in 1 2 3; do
-    name=(x rk4 rkf45 scott)
+for k in 1 2 3 4; do
+    name=(x rk4 rkf45 scott stretch)
     g++ "${flags[@]}" -DREF_KERNEL=$k "$here/ref_shim/ref_driver.cpp" -o "$out/libqslref_${name[$k]}.so" &
     pids+=($!)
 done

@@ -3,7 +3,8 @@
  *
  * A restatement in C of the reference's field-line tracer and Scott
  * deviation-vector tracer (peijin94/FastQSL, fastqslpy/cu/TraceBline.cu,
- * TraceBlineAdaptive.cu, TraceBlineScott.cu).  Compiled twice:
+ * TraceBlineAdaptive.cu, TraceBlineScott.cu) and of the stretched-grid
+ * tracer (TraceBlineAdaptiveStretch.cu).  Compiled three times:
  *
  *   QO_REAL=float  (prefix qo32_): reference-parity arithmetic.  Every
  *       expression rounds where the reference's does: FP32 state, corner
@@ -93,6 +94,11 @@ typedef struct {
     const float *bx, *by, *bz;
     int n[3];
     int64_t samples; /* trilinear vector samples taken (for the roofline count) */
+    /* stretched grid (TraceBlineAdaptiveStretch.cu): node coordinates per
+     * axis, NULL for the integer grid; uni selects the uniform-spacing index
+     * formula instead of the search */
+    const float *ax[3];
+    int uni;
 } fld;
 
 /* Floor to int with the device conversion's edge behaviour: NaN -> 0,
@@ -110,15 +116,64 @@ static inline int64_t node(const int n[3], int i, int j, int k)
     return (int64_t)i + (int64_t)n[0] * ((int64_t)j + (int64_t)n[1] * (int64_t)k);
 }
 
+/* Stretched grid: cell index of coordinate c on the node coordinates a[n].
+ * The reference's search (GetIndexBiSearch, TraceBlineAdaptiveStretch.cu:
+ * 42-64) narrows [i0, i1] by halving while the interval spans more than 3
+ * nodes, then takes mid or mid - 1 on one comparison; for a point in the upper
+ * part of the last interval that is the cell below the point's (the fraction
+ * then exceeds 1 and the sample extrapolates).  Restated as is. */
+static int stretch_bisect(R c, int n, const float *a)
+{
+    int i0 = 0, i1 = n - 1, mid = n / 2;
+    while (i1 - i0 > 3) {
+        if (c > a[mid]) i0 = mid;
+        else i1 = mid;
+        mid = (i0 + i1) / 2;
+    }
+    int r = (c > a[mid]) ? mid : mid - 1;
+    if (r > n - 2) r = n - 2;
+    return r;
+}
+
+/* Uniform-spacing formula (GetIndexUniStretch, :67-74): the spacing is taken
+ * as (a[n-1] - a[0]) / n (the node count, not n - 1), restated as is. */
+static int stretch_uni(R c, int n, const float *a)
+{
+    int r = floor_int((c - a[0]) / ((a[n - 1] - a[0]) / (R)n));
+    if (r < 0) r = 0;
+    if (r > n - 2) r = n - 2;
+    return r;
+}
+
+/* Stretched-grid cell and fraction of coordinate c along axis d: c clamped to
+ * (a[0] + 1e-6, a[n-1] - 1e-6) (the offsets applied in double and narrowed),
+ * then the index and r = (c - a[i]) / (a[i+1] - a[i]).
+ * Reference: Interp3dxyzn, TraceBlineAdaptiveStretch.cu:100-122. */
+static void stretch_locate(const fld *f, int d, R c, int *ix, R *fr)
+{
+    const float *a = f->ax[d];
+    const int n = f->n[d];
+    c = (c > a[0]) ? c : (R)((double)a[0] + 1e-6);
+    c = (c < a[n - 1]) ? c : (R)((double)a[n - 1] - 1e-6);
+    const int i = f->uni ? stretch_uni(c, n, a) : stretch_bisect(c, n, a);
+    *ix = i;
+    *fr = (c - a[i]) / ((R)a[i + 1] - a[i]);
+}
+
 /* Trilinear B (optionally unit b = B/|B|) at p; a coordinate at or beyond a
  * face is pinned to that face's cell with fraction 0 or 1.
- * Reference: Interp3dxyzn, TraceBlineAdaptive.cu:95-201. */
+ * Reference: Interp3dxyzn, TraceBlineAdaptive.cu:95-201 (integer grid) and
+ * TraceBlineAdaptiveStretch.cu:82-201 (stretched grid: stretch_locate). */
 static v3 sample_b(fld *f, v3 p, int unit)
 {
     const int *n = f->n;
     R fr[3], c[3] = {p.x, p.y, p.z};
     int ix[3];
     for (int d = 0; d < 3; ++d) {
+        if (f->ax[0]) {
+            stretch_locate(f, d, c[d], &ix[d], &fr[d]);
+            continue;
+        }
         fr[d] = c[d] - RFLOOR(c[d]);
         ix[d] = floor_int(c[d]);
         if (c[d] <= 0.) { fr[d] = 0; ix[d] = 0; }
@@ -207,6 +262,37 @@ static int box_flag(const int n[3], v3 p)
     if ((p.x >= 0.) & (p.y >= 0.) & (p.z < 0.) & (p.x < X) & (p.y < Y) & (p.z < Z)) f = 5;
     if ((p.x >= 0.) & (p.y >= 0.) & (p.z >= 0.) & (p.x < X) & (p.y < Y) & (p.z >= Z)) f = 6;
     return f;
+}
+
+/* checkFlag on the stretched grid (TraceBlineAdaptiveStretch.cu:309-331):
+ * the same tests against the first and last node coordinates. */
+static int box_flag_stretch(const fld *f, v3 p)
+{
+    const float *a = f->ax[0], *b = f->ax[1], *c = f->ax[2];
+    const R x0 = a[0], y0 = b[0], z0 = c[0];
+    const R X = a[f->n[0] - 1], Y = b[f->n[1] - 1], Z = c[f->n[2] - 1];
+    if ((p.x >= x0) & (p.y > y0) & (p.z >= z0) & (p.x <= X) & (p.y <= Y) & (p.z <= Z)) return 0;
+    int r = 42;
+    if ((p.x < x0) & (p.y >= y0) & (p.z >= z0) & (p.x < X) & (p.y < Y) & (p.z < Z)) r = 1;
+    if ((p.x >= x0) & (p.y >= y0) & (p.z >= z0) & (p.x >= X) & (p.y < Y) & (p.z < Z)) r = 2;
+    if ((p.x >= x0) & (p.y < y0) & (p.z >= z0) & (p.x < X) & (p.y < Y) & (p.z < Z)) r = 3;
+    if ((p.x >= x0) & (p.y >= y0) & (p.z >= z0) & (p.x < X) & (p.y >= Y) & (p.z < Z)) r = 4;
+    if ((p.x >= x0) & (p.y >= y0) & (p.z < z0) & (p.x < X) & (p.y < Y) & (p.z < Z)) r = 5;
+    if ((p.x >= x0) & (p.y >= y0) & (p.z >= z0) & (p.x < X) & (p.y < Y) & (p.z >= Z)) r = 6;
+    return r;
+}
+
+static inline int exit_flag(const fld *f, v3 p) { return f->ax[0] ? box_flag_stretch(f, p) : box_flag(f->n, p); }
+
+/* Length limit: len_ratio x (nx + ny + nz) on the integer grid; on the
+ * stretched grid len_ratio x the summed coordinate extents
+ * (TraceBlineAdaptiveStretch.cu:337-339, evaluated in float). */
+static double len_limit(const fld *f, double ratio)
+{
+    if (!f->ax[0]) return ratio * (double)(f->n[0] + f->n[1] + f->n[2]);
+    const R hi = (R)((R)f->ax[0][f->n[0] - 1] + f->ax[1][f->n[1] - 1]) + f->ax[2][f->n[2] - 1];
+    const R lo = (R)((R)f->ax[0][0] + f->ax[1][0]) + f->ax[2][0];
+    return ratio * (double)(R)(hi - lo);
 }
 
 /* Classic RK4 on the unit field.  Reference: RK4, TraceBlineAdaptive.cu:259-267.
@@ -305,7 +391,7 @@ static dir_result trace_direction(fld *f, fld *cur, int twist_on, const qsl_trac
                                   R h, R dir, R tol_coef)
 {
     const int *n = f->n;
-    const double len_lim = pr->len_ratio * (double)(n[0] + n[1] + n[2]);
+    const double len_lim = len_limit(f, pr->len_ratio);
     const int rkf = pr->integrator == QSL_RKF45;
     dir_result res;
     v3 p1 = p0, out = p0;
@@ -350,7 +436,7 @@ static dir_result trace_direction(fld *f, fld *cur, int twist_on, const qsl_trac
             td = twist_density(f, cur, p1, &b1, &j1);
             tw = tw + td / 4.0 / kRefPi * dl;
         }
-        flag = box_flag(n, p2);
+        flag = exit_flag(f, p2);
         if (flag > 0) {
             len = len - dl;
             if (twist_on) tw = tw - td / 4.0 / kRefPi * dl;
@@ -393,10 +479,82 @@ static dir_result trace_direction(fld *f, fld *cur, int twist_on, const qsl_trac
     return res;
 }
 
-/* The whole per-seed job of TraceAllBline (TraceBlineAdaptive.cu:429-510):
- * forward trace -> end footpoint, backward -> start footpoint, B at both
- * footpoints and at the seed, B_flag (field within ~0.57 deg of the seed
- * plane), line length and twist summed over both directions. */
+/* B at an endpoint or at the seed: the clamped scalar interpolator per
+ * component on the integer grid (TraceBlineAdaptive.cu:466-509), the vector
+ * interpolator on the stretched grid (TraceBlineAdaptiveStretch.cu:466-499). */
+static v3 sample_end(fld *f, v3 p)
+{
+    if (f->ax[0]) {
+        const int64_t s0 = f->samples;
+        v3 r = sample_b(f, p, 0);
+        f->samples = s0;
+        return r;
+    }
+    return mk3(sample_scalar(f->bx, f->n, p.x, p.y, p.z), sample_scalar(f->by, f->n, p.x, p.y, p.z),
+               sample_scalar(f->bz, f->n, p.x, p.y, p.z));
+}
+
+/* The whole per-seed job of TraceAllBline (TraceBlineAdaptive.cu:429-510,
+ * TraceBlineAdaptiveStretch.cu:422-508): forward trace -> end footpoint,
+ * backward -> start footpoint, B at both footpoints and at the seed, B_flag
+ * (field within ~0.57 deg of the seed plane), line length and twist summed
+ * over both directions.  ax (NULL: integer grid) and uni describe a
+ * stretched grid. */
+static int trace_seeds(const float *Bx, const float *By, const float *Bz, const int *shape,
+                       const float *const ax[3], int uni,
+                       const float *cBx, const float *cBy, const float *cBz, double *twist, int twist_on,
+                       const float *inp_x, const float *inp_y, const float *inp_z, const float *cross_dir,
+                       float *start_x, float *start_y, float *start_z, int *flag_start,
+                       float *end_x, float *end_y, float *end_z, int *flag_end,
+                       float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag,
+                       float *B_start_x, float *B_start_y, float *B_start_z,
+                       float *B_end_x, float *B_end_y, float *B_end_z,
+                       float s_len, int64_t n_seeds, double *LineLen, float tol_coef,
+                       const qsl_trace_params *pr, int64_t *samples_out)
+{
+    if (!Bx || !By || !Bz || !shape || !pr) return QSL_ERR_INVALID;
+    if (shape[0] < 2 || shape[1] < 2 || shape[2] < 2) return QSL_ERR_INVALID;
+    if (twist_on && (!cBx || !cBy || !cBz || !twist)) return QSL_ERR_INVALID;
+    int64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
+    for (int64_t i = 0; i < n_seeds; ++i) {
+        fld f = {Bx, By, Bz, {shape[0], shape[1], shape[2]}, 0, {ax[0], ax[1], ax[2]}, uni};
+        fld cur = {cBx, cBy, cBz, {shape[0], shape[1], shape[2]}, 0, {ax[0], ax[1], ax[2]}, uni};
+        const v3 p0 = mk3((R)inp_x[i], (R)inp_y[i], (R)inp_z[i]);
+        const v3 nrm = mk3((R)cross_dir[0], (R)cross_dir[1], (R)cross_dir[2]);
+        dir_result fw = trace_direction(&f, &cur, twist_on, pr, p0, nrm, (R)s_len, (R)1.0, (R)tol_coef);
+        v3 be = sample_end(&f, fw.end);
+        B_end_x[i] = (float)be.x;
+        B_end_y[i] = (float)be.y;
+        B_end_z[i] = (float)be.z;
+        end_x[i] = (float)fw.end.x;
+        end_y[i] = (float)fw.end.y;
+        end_z[i] = (float)fw.end.z;
+        flag_end[i] = fw.flag;
+        dir_result bw = trace_direction(&f, &cur, twist_on, pr, p0, nrm, (R)s_len, (R)-1.0, (R)tol_coef);
+        v3 bs = sample_end(&f, bw.end);
+        B_start_x[i] = (float)bs.x;
+        B_start_y[i] = (float)bs.y;
+        B_start_z[i] = (float)bs.z;
+        start_x[i] = (float)bw.end.x;
+        start_y[i] = (float)bw.end.y;
+        start_z[i] = (float)bw.end.z;
+        flag_start[i] = bw.flag;
+        LineLen[i] = fw.len + bw.len;
+        if (twist_on) twist[i] = fw.twist + bw.twist;
+        v3 b0 = sample_end(&f, p0);
+        const R bx = b0.x, by = b0.y, bz = b0.z;
+        B_this_x[i] = (float)bx;
+        B_this_y[i] = (float)by;
+        B_this_z[i] = (float)bz;
+        const R bn = bx * nrm.x + by * nrm.y + bz * nrm.z;
+        B_flag[i] = (RFABS(bn) * 100. < RSQRT_(bx * bx + by * by + bz * bz)) ? 1 : 0;
+        total += f.samples + cur.samples;
+    }
+    if (samples_out) *samples_out = total;
+    return 0;
+}
+
 QO_API int PFX(trace_all)(const float *Bx, const float *By, const float *Bz, const int *shape,
                           const float *cBx, const float *cBy, const float *cBz, double *twist, int twist_on,
                           const float *inp_x, const float *inp_y, const float *inp_z, const float *cross_dir,
@@ -408,46 +566,53 @@ QO_API int PFX(trace_all)(const float *Bx, const float *By, const float *Bz, con
                           float s_len, int64_t n_seeds, double *LineLen, float tol_coef,
                           const qsl_trace_params *pr, int64_t *samples_out)
 {
-    if (!Bx || !By || !Bz || !shape || !pr) return QSL_ERR_INVALID;
-    if (shape[0] < 2 || shape[1] < 2 || shape[2] < 2) return QSL_ERR_INVALID;
-    if (twist_on && (!cBx || !cBy || !cBz || !twist)) return QSL_ERR_INVALID;
-    int64_t total = 0;
-#pragma omp parallel for schedule(dynamic, 64) reduction(+ : total)
-    for (int64_t i = 0; i < n_seeds; ++i) {
-        fld f = {Bx, By, Bz, {shape[0], shape[1], shape[2]}, 0};
-        fld cur = {cBx, cBy, cBz, {shape[0], shape[1], shape[2]}, 0};
-        const v3 p0 = mk3((R)inp_x[i], (R)inp_y[i], (R)inp_z[i]);
-        const v3 nrm = mk3((R)cross_dir[0], (R)cross_dir[1], (R)cross_dir[2]);
-        dir_result fw = trace_direction(&f, &cur, twist_on, pr, p0, nrm, (R)s_len, (R)1.0, (R)tol_coef);
-        B_end_x[i] = (float)sample_scalar(Bx, f.n, fw.end.x, fw.end.y, fw.end.z);
-        B_end_y[i] = (float)sample_scalar(By, f.n, fw.end.x, fw.end.y, fw.end.z);
-        B_end_z[i] = (float)sample_scalar(Bz, f.n, fw.end.x, fw.end.y, fw.end.z);
-        end_x[i] = (float)fw.end.x;
-        end_y[i] = (float)fw.end.y;
-        end_z[i] = (float)fw.end.z;
-        flag_end[i] = fw.flag;
-        dir_result bw = trace_direction(&f, &cur, twist_on, pr, p0, nrm, (R)s_len, (R)-1.0, (R)tol_coef);
-        B_start_x[i] = (float)sample_scalar(Bx, f.n, bw.end.x, bw.end.y, bw.end.z);
-        B_start_y[i] = (float)sample_scalar(By, f.n, bw.end.x, bw.end.y, bw.end.z);
-        B_start_z[i] = (float)sample_scalar(Bz, f.n, bw.end.x, bw.end.y, bw.end.z);
-        start_x[i] = (float)bw.end.x;
-        start_y[i] = (float)bw.end.y;
-        start_z[i] = (float)bw.end.z;
-        flag_start[i] = bw.flag;
-        LineLen[i] = fw.len + bw.len;
-        if (twist_on) twist[i] = fw.twist + bw.twist;
-        const R bx = sample_scalar(Bx, f.n, p0.x, p0.y, p0.z);
-        const R by = sample_scalar(By, f.n, p0.x, p0.y, p0.z);
-        const R bz = sample_scalar(Bz, f.n, p0.x, p0.y, p0.z);
-        B_this_x[i] = (float)bx;
-        B_this_y[i] = (float)by;
-        B_this_z[i] = (float)bz;
-        const R bn = bx * nrm.x + by * nrm.y + bz * nrm.z;
-        B_flag[i] = (RFABS(bn) * 100. < RSQRT_(bx * bx + by * by + bz * bz)) ? 1 : 0;
-        total += f.samples + cur.samples;
-    }
-    if (samples_out) *samples_out = total;
-    return 0;
+    const float *const none[3] = {NULL, NULL, NULL};
+    return trace_seeds(Bx, By, Bz, shape, none, 0, cBx, cBy, cBz, twist, twist_on, inp_x, inp_y, inp_z, cross_dir,
+                       start_x, start_y, start_z, flag_start, end_x, end_y, end_z, flag_end, B_this_x, B_this_y,
+                       B_this_z, B_flag, B_start_x, B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len,
+                       n_seeds, LineLen, tol_coef, pr, samples_out);
+}
+
+/* Stretched grid: node coordinates xa[nx], ya[ny], za[nz] (increasing). */
+QO_API int PFX(trace_all_stretch)(const float *Bx, const float *By, const float *Bz, const int *shape,
+                                  const float *xa, const float *ya, const float *za, int uni,
+                                  const float *cBx, const float *cBy, const float *cBz, double *twist, int twist_on,
+                                  const float *inp_x, const float *inp_y, const float *inp_z, const float *cross_dir,
+                                  float *start_x, float *start_y, float *start_z, int *flag_start,
+                                  float *end_x, float *end_y, float *end_z, int *flag_end,
+                                  float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag,
+                                  float *B_start_x, float *B_start_y, float *B_start_z,
+                                  float *B_end_x, float *B_end_y, float *B_end_z,
+                                  float s_len, int64_t n_seeds, double *LineLen, float tol_coef,
+                                  const qsl_trace_params *pr, int64_t *samples_out)
+{
+    if (!xa || !ya || !za) return QSL_ERR_INVALID;
+    const float *const ax[3] = {xa, ya, za};
+    return trace_seeds(Bx, By, Bz, shape, ax, uni, cBx, cBy, cBz, twist, twist_on, inp_x, inp_y, inp_z, cross_dir,
+                       start_x, start_y, start_z, flag_start, end_x, end_y, end_z, flag_end, B_this_x, B_this_y,
+                       B_this_z, B_flag, B_start_x, B_start_y, B_start_z, B_end_x, B_end_y, B_end_z, s_len,
+                       n_seeds, LineLen, tol_coef, pr, samples_out);
+}
+
+/* Single-function probes of the stretched grid (unit-level pinning against
+ * the reference build). */
+QO_API int PFX(index_bisect)(float p, int n, const float *a) { return stretch_bisect((R)p, n, a); }
+QO_API int PFX(index_uni)(float p, int n, const float *a) { return stretch_uni((R)p, n, a); }
+
+QO_API void PFX(interp_stretch)(const float *Bx, const float *By, const float *Bz, const int *shape,
+                                const float *xa, const float *ya, const float *za, int uni, const float *p, int norm,
+                                float *out)
+{
+    fld f = {Bx, By, Bz, {shape[0], shape[1], shape[2]}, 0, {xa, ya, za}, uni};
+    v3 r = sample_b(&f, mk3((R)p[0], (R)p[1], (R)p[2]), norm);
+    out[0] = (float)r.x; out[1] = (float)r.y; out[2] = (float)r.z;
+}
+
+QO_API int PFX(checkflag_stretch)(const int *shape, const float *xa, const float *ya, const float *za, int uni,
+                                  const float *p)
+{
+    fld f = {NULL, NULL, NULL, {shape[0], shape[1], shape[2]}, 0, {xa, ya, za}, uni};
+    return box_flag_stretch(&f, mk3((R)p[0], (R)p[1], (R)p[2]));
 }
 
 /* ---------------------------------------------------------------------- */

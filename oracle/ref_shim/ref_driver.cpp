@@ -7,6 +7,7 @@
  *   REF_KERNEL == 1  fastqslpy/cu/TraceBline.cu          (RK4)
  *   REF_KERNEL == 2  fastqslpy/cu/TraceBlineAdaptive.cu  (RKF45)
  *   REF_KERNEL == 3  fastqslpy/cu/TraceBlineScott.cu     (RKF45 + deviation vectors)
+ *   REF_KERNEL == 4  fastqslpy/cu/TraceBlineAdaptiveStretch.cu (RKF45 on a stretched grid)
  *
  * qref_trace_all runs the reference kernel body TraceAllBline once per seed
  * (grid = block = 1, N = 1, pointer-offset slices) under an OpenMP loop, which
@@ -27,8 +28,10 @@
 #include "TraceBlineAdaptive.cu"
 #elif REF_KERNEL == 3
 #include "TraceBlineScott.cu"
+#elif REF_KERNEL == 4
+#include "TraceBlineAdaptiveStretch.cu"
 #else
-#error "REF_KERNEL must be 1, 2 or 3"
+#error "REF_KERNEL must be 1, 2, 3 or 4"
 #endif
 
 thread_local uint3 threadIdx;
@@ -70,6 +73,7 @@ QREF_API int qref_set_threads(int n)
 
 static inline int3 shape_of(const int *s) { return make_int3(s[0], s[1], s[2]); }
 
+#if REF_KERNEL != 4
 QREF_API void qref_interp3dxyzn(const float *Bx, const float *By, const float *Bz, const int *shape,
                                 const float *p, int norm, float *out)
 {
@@ -87,6 +91,7 @@ QREF_API int qref_checkflag(const int *shape, const float *p)
 {
     return checkFlag(shape_of(shape), make_float3(p[0], p[1], p[2]));
 }
+#endif
 
 #if REF_KERNEL == 1 || REF_KERNEL == 2
 QREF_API void qref_rk4_step(const float *Bx, const float *By, const float *Bz, const int *shape,
@@ -207,5 +212,69 @@ QREF_API float qref_rkf45_scott(const float *Bx, const float *By, const float *B
     float err = RKF45_Scott((float *)Bx, (float *)By, (float *)Bz, shape_of(shape), load9(v9), &o, h);
     store9(o, out9);
     return err;
+}
+#endif
+
+#if REF_KERNEL == 4
+/* Stretched-grid building blocks (TraceBlineAdaptiveStretch.cu:42-201,309-331). */
+QREF_API int qref_index_bisect(float p, int n, const float *a) { return GetIndexBiSearch(p, n, (float *)a); }
+
+QREF_API int qref_index_uni(float p, int n, const float *a) { return GetIndexUniStretch(p, n, (float *)a); }
+
+QREF_API void qref_interp_stretch(const float *Bx, const float *By, const float *Bz, const int *shape,
+                                  const float *xa, const float *ya, const float *za, int uni, const float *p,
+                                  int norm, float *out)
+{
+    float3 r = Interp3dxyzn((float *)Bx, (float *)By, (float *)Bz, shape_of(shape), make_float3(p[0], p[1], p[2]),
+                            norm != 0, (float *)xa, (float *)ya, (float *)za, uni != 0);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+QREF_API int qref_checkflag_stretch(const int *shape, const float *xa, const float *ya, const float *za, int uni,
+                                    const float *p)
+{
+    return checkFlag(shape_of(shape), make_float3(p[0], p[1], p[2]), (float *)xa, (float *)ya, (float *)za,
+                     uni != 0);
+}
+
+/* TraceAllBline of the stretched-grid file (TraceBlineAdaptiveStretch.cu:422-508) for seeds [0, n), one
+ * single-thread launch per seed as above. */
+QREF_API int qref_trace_all_stretch(const float *Bx, const float *By, const float *Bz, const int *shape,
+                                    const float *xa, const float *ya, const float *za, int uni,
+                                    const float *curBx, const float *curBy, const float *curBz, double *twist,
+                                    int twist_flag,
+                                    const float *inp_x, const float *inp_y, const float *inp_z,
+                                    const float *cross_dir,
+                                    float *start_x, float *start_y, float *start_z, int *flag_start,
+                                    float *end_x, float *end_y, float *end_z, int *flag_end,
+                                    float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag,
+                                    float *B_start_x, float *B_start_y, float *B_start_z,
+                                    float *B_end_x, float *B_end_y, float *B_end_z,
+                                    float s_len, unsigned long long n, double *LineLen, float tol_coef)
+{
+    bool flag = twist_flag != 0;
+    if (flag && (!curBx || !curBy || !curBz || !twist)) return -1;
+    const float *cx = flag ? curBx : Bx, *cy = flag ? curBy : By, *cz = flag ? curBz : Bz;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < (long long)n; ++i) {
+        set_single_thread_launch();
+        int shp[3] = {shape[0], shape[1], shape[2]};
+        float cd[3] = {cross_dir[0], cross_dir[1], cross_dir[2]};
+        float sl = s_len, tc = tol_coef;
+        unsigned long long one = 1;
+        double tw_dummy = 0;
+        bool f = flag, u = uni != 0;
+        double *tw = flag ? twist + i : &tw_dummy;
+        TraceAllBline((float *)Bx, (float *)By, (float *)Bz, shp, (float *)xa, (float *)ya, (float *)za, &u,
+                      (float *)cx, (float *)cy, (float *)cz, tw, &f,
+                      (float *)inp_x + i, (float *)inp_y + i, (float *)inp_z + i, cd,
+                      start_x + i, start_y + i, start_z + i, flag_start + i,
+                      end_x + i, end_y + i, end_z + i, flag_end + i,
+                      B_this_x + i, B_this_y + i, B_this_z + i, B_flag + i,
+                      B_start_x + i, B_start_y + i, B_start_z + i,
+                      B_end_x + i, B_end_y + i, B_end_z + i,
+                      &sl, &one, LineLen + i, &tc);
+    }
+    return 0;
 }
 #endif

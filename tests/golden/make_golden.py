@@ -7,7 +7,8 @@ Run in a checkout where the reference exists (default /root/reference):
 
 What runs:
 * tracing — the reference's own kernels (fastqslpy/cu/TraceBline.cu,
-  TraceBlineAdaptive.cu, TraceBlineScott.cu), compiled for the host by
+  TraceBlineAdaptive.cu, TraceBlineScott.cu, TraceBlineAdaptiveStretch.cu),
+  compiled for the host by
   oracle/build_ref.sh (unmodified sources, -ffp-contract=off);
 * Q assembly — the reference's own fastqslpy/FastQSL.py (QCalcPlane,
   CookPseudoLine, ResReshape) imported with NumPy standing in for CuPy, and
@@ -67,6 +68,22 @@ def trace_case(name, kind, spec_fn, seed, seeds_xy, z, s_len, tol_coef, twist=Fa
     meta = dict(kind=kind, spec=spec_fn.__name__, seed=seed, s_len=s_len, tol_coef=tol_coef, twist=twist,
                 z=z, seeds=[list(xr), list(yr), nx, ny], fingerprint=S.field_fingerprint(Bx, By, Bz))
     save(name, meta=json.dumps(meta), inp_x=xs, inp_y=ys, inp_z=zs, **out)
+
+
+def stretch_case(name, seed, z_ratio, uni, twist=False, s_len=0.01, tol_coef=1.0):
+    """TraceAllBline of TraceBlineAdaptiveStretch.cu on bipole4_stretch over
+    stretched_axes(z_ratio); 40 x 32 seeds at z = 1e-3 (as the reference's
+    stretched notebook seeds just above the bottom face)."""
+    spec = S.bipole4_stretch(seed)
+    xa, ya, za = S.stretched_axes(spec.shape, z_ratio=z_ratio)
+    Bx, By, Bz = S.make_field_coords(spec, xa, ya, za)
+    xs, ys, zs, shp = S.plane_seeds((-5, 5), (-4, 4), 40, 32, 1e-3)
+    cur = (By * np.float32(0.3) + Bz, Bz - Bx, Bx * np.float32(0.5) + By) if twist else None
+    out = oracle.trace_all("ref_stretch", Bx, By, Bz, xs, ys, zs, s_len=s_len, tol_coef=tol_coef, curB=cur,
+                           coords=(xa, ya, za), uni=uni)
+    meta = dict(kind="stretch", spec="bipole4_stretch", seed=seed, z_ratio=z_ratio, uni=uni, s_len=s_len,
+                tol_coef=tol_coef, twist=twist, fingerprint=S.field_fingerprint(Bx, By, Bz))
+    save(name, meta=json.dumps(meta), inp_x=xs, inp_y=ys, inp_z=zs, xa=xa, ya=ya, za=za, **out)
 
 
 def probes_case():
@@ -173,6 +190,8 @@ def qmap_case():
 def main():
     if not oracle.ref_available("rkf45"):
         raise SystemExit("oracle/_ref not built: run python oracle/build.py in a checkout with the reference")
+    if sys.argv[1:] == ["stretch"]:  # only the stretched-grid fixtures
+        return stretch_cases()
     trace_case("trace_rk4_bipole4_64.npz", "rk4", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 0.0, 0.1, 1.0)
     trace_case("trace_rkf45_bipole4_64.npz", "rkf45", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 1e-4,
                0.125, 0.5)
@@ -182,6 +201,12 @@ def main():
                0.1, 1.0, twist=True)
     probes_case()
     qmap_case()
+    stretch_cases()
+
+
+def stretch_cases():
+    stretch_case("trace_stretch_bipole4s.npz", 1, 1.06, False)
+    stretch_case("trace_stretch_uni_twist_bipole4s.npz", 2, 1.0, True, twist=True)
 
 
 if __name__ == "__main__":

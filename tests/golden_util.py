@@ -25,6 +25,18 @@ def field_for(meta):
     return Bx, By, Bz
 
 
+def stretch_field_for(meta):
+    """Field and node coordinates of a stretched-grid fixture."""
+    spec = S.bipole4_stretch(meta["seed"])
+    xa, ya, za = S.stretched_axes(spec.shape, z_ratio=meta["z_ratio"])
+    Bx, By, Bz = S.make_field_coords(spec, xa, ya, za)
+    assert S.field_fingerprint(Bx, By, Bz) == meta["fingerprint"], "synthetic field differs from the fixture's"
+    return Bx, By, Bz, (xa, ya, za)
+
+
+STRETCH_CASES = ["trace_stretch_bipole4s.npz", "trace_stretch_uni_twist_bipole4s.npz"]
+
+
 def twist_current(Bx, By, Bz):
     """The stand-in current density the twist fixtures were made with."""
     return (By * np.float32(0.3) + Bz, Bz - Bx, Bx * np.float32(0.5) + By)
