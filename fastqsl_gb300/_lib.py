@@ -83,6 +83,10 @@ _SIGS = {
     "qsl_batch_lines": (c_i64, [_P]),
     "qsl_batch_destroy": (c_int, [_P]),
     "qsl_trace_all_bline_scott": (c_int, [_P] * 30 + [c_i64, _P]),
+    "qsl_params_reference_stretch": (None, [_P]),
+    "qsl_trace_all_bline_stretch": (c_int, [c_int] + [_P] * 39 + [c_i64, _P]),
+    "qsl_trace_stretch": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, _P, _P, c_int, _P, _P, c_i64, c_float,
+                                  c_float, _P, _P, _P, _P, _P, _P]),
     "qsl_trace_scott": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, c_int, _P, _P]),
     "qsl_field_store_bytes": (c_i64, [c_int, c_int, c_int, c_int]),
     "qsl_field_create": (c_int, [_P, _P, _P, c_int, c_int, c_int, c_int, _P, _P]),

@@ -165,6 +165,40 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
     return out
 
 
+def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = None, s_len=0.01, tol_coef=1.0,
+                  uni=False, cross_dir=(0.0, 0.0, 1.0), curB=None, schedule="static", out=None, samples=None,
+                  order=None, stream=None):
+    """Traces every seed both ways on a stretched grid: Bx, By, Bz of shape
+    (nx, ny, nz) (x fastest; moved to the device if needed and read in place),
+    coords = (x_arr, y_arr, z_arr) increasing node coordinates, seeds in the
+    same physical coordinates (float32 CUDA vectors).  uni: index cells by the
+    uniform-spacing formula instead of the search.  Defaults to the reference
+    stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""
+    from .params import reference_stretch
+    lib = _lib.load()
+    if params is None:
+        params = reference_stretch()
+    arrs = [as_xfast(b) for b in (Bx, By, Bz)]
+    nx, ny, nz = (int(v) for v in arrs[0].shape)
+    ax = [torch.as_tensor(c).to(device=xs.device, dtype=torch.float32).contiguous() for c in coords]
+    if [a.numel() for a in ax] != [nx, ny, nz]:
+        raise ValueError("coordinate arrays must have nx, ny, nz entries")
+    n = int(xs.shape[0])
+    if out is None:
+        out = alloc_trace_outputs(n, xs.device, twist=curB is not None)
+    cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
+    curs = [as_xfast(c) for c in curB] if curB is not None else None
+    cur = [ptr(c) for c in curs] if curs is not None else [None, None, None]
+    if curB is not None and out.get("twist") is None:
+        out["twist"] = torch.zeros(n, dtype=torch.float64, device=xs.device)
+    io = _io(xs, ys, zs, out)
+    sc = _lib.Sched(SCHEDULES[schedule], 0, ptr(order), None, ptr(samples), 0)
+    _lib.check(lib.qsl_trace_stretch(*[ptr(a) for a in arrs], nx, ny, nz, *[ptr(a) for a in ax], int(bool(uni)),
+                                     ctypes.byref(params), ctypes.byref(io), n, float(s_len), float(tol_coef), cd,
+                                     *cur, ctypes.byref(sc), stream_handle(stream)), "qsl_trace_stretch")
+    return out
+
+
 def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda"):
     """A permutation of the seeds of `nplanes` stacked (n0, n1) planes that
     visits them tile by tile (ty x tx seeds, row-major inside a tile, tiles

@@ -278,6 +278,9 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
         e = launch_trace_fast_f4(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldH4B>::value) {
         e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldStretch>::value) {
+        e = arith == QSL_ARITH_EXACT ? launch_trace_exact_stretch(J, twist, sched, n_host, st)
+                                     : launch_trace_fast_stretch(J, twist, sched, n_host, st);
     } else {
         e = launch_trace_fast_h8c(J, twist, sched, n_host, st);
     }
@@ -401,6 +404,87 @@ int qsl_trace_all_bline(int integrator, int arith, const float* Bx, const float*
     J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
     J.s.s_len_dev = s_len;
     J.s.tol_coef_dev = integrator == QSL_RKF45 ? tol_coef : nullptr;
+    J.s.tol_coef = 1.f;
+    J.s.n_dev = N;
+    J.s.cross_dev = inp_cross_dir;
+    J.s.twist_flag_dev = twist_possible ? curB_flag : nullptr;
+    J.s.twist_on = 0;
+    J.s.n_cap = capacity < 0 ? -1 : capacity;
+    return run_trace(J, arith, twist_possible, QSL_SCHED_QUEUE, 0, nullptr, (cudaStream_t)stream);
+}
+
+// Stretched grid, native form: field arrays (x fastest) of shape nx x ny x nz
+// on the increasing node coordinates x_arr, y_arr, z_arr (device), host
+// scalars and settings.
+int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz,
+                      const float* x_arr, const float* y_arr, const float* z_arr, int uni,
+                      const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n, float s_len, float tol_coef,
+                      const float* cross_dir_h, const float* curBx, const float* curBy, const float* curBz,
+                      const qsl_sched* sched_h, qsl_stream_t stream) {
+    if (!Bx || !By || !Bz || !x_arr || !y_arr || !z_arr) return fail(QSL_ERR_INVALID, "null field or coordinates");
+    if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
+    if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
+    if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
+    if (n == 0) return QSL_OK;
+    if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
+    qsl_sched sc{QSL_SCHED_STATIC, 0, nullptr, nullptr, nullptr, 0};
+    if (sched_h) sc = *sched_h;
+    if (sc.schedule != QSL_SCHED_QUEUE && sc.schedule != QSL_SCHED_STATIC)
+        return fail(QSL_ERR_INVALID, "bad schedule %d", sc.schedule);
+    if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
+    const bool twist = curBx != nullptr;
+    if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
+    TraceJob<FieldStretch> J;
+    J.f = FieldStretch{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
+                       make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    fill_common(J, io, prm, sc.samples);
+    J.cur = FieldSoA{curBx, curBy, curBz, J.f.d};
+    J.order = sc.order;
+    J.chunk = sc.chunk;
+    J.s.s_len = s_len;
+    J.s.tol_coef = tol_coef;
+    J.s.n = n;
+    J.s.cross[0] = cross_dir_h ? cross_dir_h[0] : 0.f;
+    J.s.cross[1] = cross_dir_h ? cross_dir_h[1] : 0.f;
+    J.s.cross[2] = cross_dir_h ? cross_dir_h[2] : 1.f;
+    J.s.twist_on = twist ? 1 : 0;
+    return run_trace(J, prm->arith, twist, sc.schedule, n, sc.queue, (cudaStream_t)stream);
+}
+
+// Drop-in entry for the stretched-grid kernel: the argument list of
+// TraceAllBline in TraceBlineAdaptiveStretch.cu:422-433, scalars by device
+// pointer, the field read in place.
+int qsl_trace_all_bline_stretch(int arith, const float* Bx, const float* By, const float* Bz, const int* BshapeN,
+                                const float* x_arr, const float* y_arr, const float* z_arr, const bool* flag_uni,
+                                const float* curB_x, const float* curB_y, const float* curB_z, double* twist,
+                                const bool* curB_flag, const float* inp_x, const float* inp_y, const float* inp_z,
+                                const float* inp_cross_dir, float* start_x, float* start_y, float* start_z,
+                                int* flag_start, float* end_x, float* end_y, float* end_z, int* flag_end,
+                                float* B_this_x, float* B_this_y, float* B_this_z, int* B_flag, float* B_start_x,
+                                float* B_start_y, float* B_start_z, float* B_end_x, float* B_end_y, float* B_end_z,
+                                const float* s_len, const unsigned long long* N, double* LineLen,
+                                const float* tol_coef, int64_t capacity, qsl_stream_t stream) {
+    if (capacity == 0) return QSL_OK;
+    if (!Bx || !By || !Bz || !BshapeN || !x_arr || !y_arr || !z_arr || !flag_uni || !inp_cross_dir || !s_len || !N ||
+        !tol_coef)
+        return fail(QSL_ERR_INVALID, "null required pointer");
+    if (arith != QSL_ARITH_EXACT && arith != QSL_ARITH_FAST) return fail(QSL_ERR_INVALID, "bad arith %d", arith);
+    qsl_trace_params prm;
+    qsl_params_reference_stretch(&prm);
+    prm.arith = arith;
+    qsl_trace_io io{inp_x, inp_y, inp_z, start_x, start_y, start_z, flag_start, end_x, end_y, end_z, flag_end,
+                    B_this_x, B_this_y, B_this_z, B_flag, B_start_x, B_start_y, B_start_z, B_end_x, B_end_y,
+                    B_end_z, LineLen, twist};
+    if (!io_ok(&io)) return fail(QSL_ERR_INVALID, "null pointer in outputs");
+    const bool twist_possible = curB_flag && curB_x && curB_y && curB_z && twist;
+    TraceJob<FieldStretch> J;
+    J.f = FieldStretch{Bx, By, Bz, Dims{2, 2, 2}, x_arr, y_arr, z_arr, flag_uni, 0, make_float3(0.f, 0.f, 0.f),
+                       make_float3(0.f, 0.f, 0.f)};
+    fill_common(J, &io, &prm, nullptr);
+    J.shape_dev = BshapeN;
+    J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
+    J.s.s_len_dev = s_len;
+    J.s.tol_coef_dev = tol_coef;
     J.s.tol_coef = 1.f;
     J.s.n_dev = N;
     J.s.cross_dev = inp_cross_dir;

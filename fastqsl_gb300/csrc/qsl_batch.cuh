@@ -25,7 +25,8 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
     const float s_len = J.s.s_len, tol_coef = J.s.tol_coef;
     const float3 nrm = v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
     const bool tw_on = TWIST && J.s.twist_on != 0;
-    const float len_lim = (float)(J.prm.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz));
+    store_prepare(f);
+    const float len_lim = (float)(J.prm.len_ratio * len_scale(f));
     Lane<false> L;
     lane_begin<false>(f, J, L, i, +1, s_len, tol_coef, nrm, ns);
     const TraceOut& o = J.o;

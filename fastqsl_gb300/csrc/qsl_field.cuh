@@ -16,6 +16,9 @@
 //               single L1 sector, instead of eight node loads spread over
 //               several sectors.  Nodes are stored up to 8 times over (about
 //               64 B per cell against 11 B for FieldH4B).
+//   FieldStretch — the caller's SoA arrays on a stretched (rectilinear)
+//               grid: node coordinates per axis, cells found by the
+//               reference's search (fastqslpy/cu/TraceBlineAdaptiveStretch.cu).
 //
 // Sampling comes in two arithmetics:
 //   exact — the reference's rounding sequence (weights formed in double and
@@ -155,6 +158,28 @@ struct FieldH8C {
         }
         return __ldg(reinterpret_cast<const float*>(r + 3));
     }
+};
+
+// Stretched grid: the SoA arrays plus increasing node coordinates ax[nx],
+// ay[ny], az[nz].  uni selects the reference's uniform-spacing index formula
+// instead of its search; lo/hi are the first and last coordinates (set at
+// kernel start from the coordinate arrays).
+struct FieldStretch {
+    const float* bx;
+    const float* by;
+    const float* bz;
+    Dims d;
+    const float* ax;
+    const float* ay;
+    const float* az;
+    const bool* uni_dev;  // when set, uni is read from here (drop-in)
+    int uni;
+    float3 lo, hi;
+    __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
+        const FieldSoA s{bx, by, bz, d};
+        return s.corners(ix, iy, iz, c);
+    }
+    __device__ __forceinline__ const float* axis(int k) const { return k == 0 ? ax : (k == 1 ? ay : az); }
 };
 
 // ---------------------------------------------------------------------------
@@ -417,6 +442,82 @@ __device__ __forceinline__ float3 sample_outlined<false, FieldH8C>(const FieldH8
     return sample_h8c<false>(f, p, unit);
 }
 
+// ---------------------------------------------------------------------------
+// Stretched grid (fastqslpy/cu/TraceBlineAdaptiveStretch.cu)
+// ---------------------------------------------------------------------------
+// The reference's search (GetIndexBiSearch, :42-64): halve [i0, i1] while it
+// spans more than 3 nodes, then mid or mid - 1 on one comparison.  For a point
+// in the upper part of the last interval this is the cell below the point's
+// (the fraction then exceeds 1 and the sample extrapolates); kept as is so the
+// results are the reference's.  The result lies in [0, n-2] for n >= 2.
+__device__ __forceinline__ int stretch_bisect(float c, int n, const float* __restrict__ a) {
+    int i0 = 0, i1 = n - 1, mid = n / 2;
+    while (i1 - i0 > 3) {
+        if (c > __ldg(a + mid)) i0 = mid;
+        else i1 = mid;
+        mid = (i0 + i1) / 2;
+    }
+    int r = (c > __ldg(a + mid)) ? mid : mid - 1;
+    r = r > n - 2 ? n - 2 : r;
+    return r < 0 ? 0 : r;
+}
+
+// The uniform-spacing formula (GetIndexUniStretch, :67-74); its spacing is
+// (a[n-1] - a[0]) / n, the node count, as in the reference.
+__device__ __forceinline__ int stretch_uni(float c, int n, float a0, float an) {
+    int r = __float2int_rd((c - a0) / ((an - a0) / __int2float_rd(n)));
+    r = r < 0 ? 0 : r;
+    return r > n - 2 ? n - 2 : r;
+}
+
+// Cell and fraction along one axis: c clamped to (a[0] + 1e-6, a[n-1] - 1e-6)
+// (offsets applied in double and narrowed), then the index and
+// r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122).
+__device__ __forceinline__ void stretch_locate(const FieldStretch& f, int k, float c, float a0, float an, int& i,
+                                               float& r) {
+    const float* a = f.axis(k);
+    const int n = f.d.n(k);
+    c = (c > a0) ? c : (float)((double)a0 + 1e-6);
+    c = (c < an) ? c : (float)((double)an - 1e-6);
+    i = f.uni ? stretch_uni(c, n, a0, an) : stretch_bisect(c, n, a);
+    const float ai = __ldg(a + i);
+    r = (c - ai) / (__ldg(a + i + 1) - ai);
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float3 sample_stretch(const FieldStretch& f, float3 p, bool unit) {
+    int ix, iy, iz;
+    float rx, ry, rz;
+    stretch_locate(f, 0, p.x, f.lo.x, f.hi.x, ix, rx);
+    stretch_locate(f, 1, p.y, f.lo.y, f.hi.y, iy, ry);
+    stretch_locate(f, 2, p.z, f.lo.z, f.hi.z, iz, rz);
+    float w[8];
+    if (EXACT) weights_exact(rx, ry, rz, w);
+    else weights_fast(rx, ry, rz, w);
+    float3 c[8];
+    f.corners(ix, iy, iz, c);
+    float3 r = blend<EXACT>(c, w);
+    if (unit) {
+        if (EXACT) {
+            const float nb = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
+            r = v3(r.x / nb, r.y / nb, r.z / nb);
+        } else {
+            const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+            r = v3(r.x * inv, r.y * inv, r.z * inv);
+        }
+    }
+    return r;
+}
+
+template <>
+__device__ __forceinline__ float3 sample<true, FieldStretch>(const FieldStretch& f, float3 p, bool unit) {
+    return sample_stretch<true>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldStretch>(const FieldStretch& f, float3 p, bool unit) {
+    return sample_stretch<false>(f, p, unit);
+}
+
 // Position clamped into [1e-4, n-1-1e-4] as the scalar interpolator of the
 // reference does (Interp3d, TraceBlineAdaptive.cu:57-62).
 __device__ __forceinline__ float clamp_inside(float c, int n) {
@@ -467,6 +568,17 @@ template <bool EXACT, class F>
 __device__ __forceinline__ float3 sample_endpoint(const F& f, float3 p) {
     const float3 q = v3(clamp_inside(p.x, f.d.nx), clamp_inside(p.y, f.d.ny), clamp_inside(p.z, f.d.nz));
     return sample<false>(f, q, false);
+}
+
+// Stretched grid: the vector interpolator (its clamp included), as the
+// reference's stretched kernel samples its endpoints (:466-499).
+template <>
+__device__ __forceinline__ float3 sample_endpoint<true, FieldStretch>(const FieldStretch& f, float3 p) {
+    return sample_stretch<true>(f, p, false);
+}
+template <>
+__device__ __forceinline__ float3 sample_endpoint<false, FieldStretch>(const FieldStretch& f, float3 p) {
+    return sample_stretch<false>(f, p, false);
 }
 
 }  // namespace qsl

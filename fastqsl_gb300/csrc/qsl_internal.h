@@ -22,6 +22,11 @@ int persistent_grid(const void* kernel, int block, size_t smem = 0);
 // trace_exact.cu (compiled with -fmad=false)
 cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
                                cudaStream_t st);
+cudaError_t launch_trace_exact_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
+                                       cudaStream_t st);
+// trace_fast_stretch.cu
+cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
+                                      cudaStream_t st);
 
 // trace_fast_<store>.cu
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,

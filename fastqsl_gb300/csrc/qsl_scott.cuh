@@ -209,7 +209,7 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
             float td = 0.f;
             float3 bp1 = v3(0.f, 0.f, 0.f);
             if (TWIST && tw_on) {
-                const float3 j1 = sample<EXACT>(J.cur, b.p, false);
+                const float3 j1 = sample<EXACT>(current_view(f, J.cur), b.p, false);
                 bp1 = sample<EXACT>(f, b.p, false);
                 ns += 2;
                 td = dot(j1, bp1) / dot(bp1, bp1);

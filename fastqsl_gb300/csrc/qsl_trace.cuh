@@ -194,6 +194,69 @@ __device__ __forceinline__ int box_flag(const Dims& n, float3 p) {
     return f;
 }
 
+// ---------------------------------------------------------------------------
+// Per-store geometry: the box tests, the length-limit scale, the kernel-start
+// set-up and the view of the twist current density on the store's grid.
+// ---------------------------------------------------------------------------
+template <class F>
+__device__ __forceinline__ bool box_inside(const F& f, float3 p) {
+    return (p.x >= 0.f) & (p.y > 0.f) & (p.z >= 0.f) & (p.x <= (float)(f.d.nx - 1)) &
+           (p.y <= (float)(f.d.ny - 1)) & (p.z <= (float)(f.d.nz - 1));
+}
+template <class F>
+__device__ __forceinline__ int box_exit(const F& f, float3 p) {
+    return box_flag(f.d, p);
+}
+// len_lim = len_ratio * this (the node counts' sum)
+template <class F>
+__device__ __forceinline__ double len_scale(const F& f) {
+    return (double)(f.d.nx + f.d.ny + f.d.nz);
+}
+template <class F>
+__device__ __forceinline__ void store_prepare(F&) {}
+// The current density shares the traced field's grid; J.cur carries only its
+// three arrays, the geometry comes from the traced store (whose dims may have
+// been read from the device at kernel start).
+template <class F>
+__device__ __forceinline__ FieldSoA current_view(const F& f, const FieldSoA& c) {
+    return FieldSoA{c.bx, c.by, c.bz, f.d};
+}
+
+// Stretched grid (checkFlag, TraceBlineAdaptiveStretch.cu:309-331): the same
+// tests against the first and last node coordinates.
+__device__ __forceinline__ bool box_inside(const FieldStretch& f, float3 p) {
+    return (p.x >= f.lo.x) & (p.y > f.lo.y) & (p.z >= f.lo.z) & (p.x <= f.hi.x) & (p.y <= f.hi.y) &
+           (p.z <= f.hi.z);
+}
+__device__ __forceinline__ int box_exit(const FieldStretch& f, float3 p) {
+    const float3 a = f.lo, b = f.hi;
+    if ((p.x >= a.x) & (p.y > a.y) & (p.z >= a.z) & (p.x <= b.x) & (p.y <= b.y) & (p.z <= b.z)) return 0;
+    int r = 42;
+    if ((p.x < a.x) & (p.y >= a.y) & (p.z >= a.z) & (p.x < b.x) & (p.y < b.y) & (p.z < b.z)) r = 1;
+    if ((p.x >= a.x) & (p.y >= a.y) & (p.z >= a.z) & (p.x >= b.x) & (p.y < b.y) & (p.z < b.z)) r = 2;
+    if ((p.x >= a.x) & (p.y < a.y) & (p.z >= a.z) & (p.x < b.x) & (p.y < b.y) & (p.z < b.z)) r = 3;
+    if ((p.x >= a.x) & (p.y >= a.y) & (p.z >= a.z) & (p.x < b.x) & (p.y >= b.y) & (p.z < b.z)) r = 4;
+    if ((p.x >= a.x) & (p.y >= a.y) & (p.z < a.z) & (p.x < b.x) & (p.y < b.y) & (p.z < b.z)) r = 5;
+    if ((p.x >= a.x) & (p.y >= a.y) & (p.z >= a.z) & (p.x < b.x) & (p.y < b.y) & (p.z >= b.z)) r = 6;
+    return r;
+}
+// the summed coordinate extents, in float as the reference (:337-339)
+__device__ __forceinline__ double len_scale(const FieldStretch& f) {
+    return (double)(((f.hi.x + f.hi.y) + f.hi.z) - ((f.lo.x + f.lo.y) + f.lo.z));
+}
+__device__ __forceinline__ void store_prepare(FieldStretch& f) {
+    f.lo = v3(__ldg(f.ax), __ldg(f.ay), __ldg(f.az));
+    f.hi = v3(__ldg(f.ax + f.d.nx - 1), __ldg(f.ay + f.d.ny - 1), __ldg(f.az + f.d.nz - 1));
+    if (f.uni_dev) f.uni = *f.uni_dev ? 1 : 0;
+}
+__device__ __forceinline__ FieldStretch current_view(const FieldStretch& f, const FieldSoA& c) {
+    FieldStretch r = f;
+    r.bx = c.bx;
+    r.by = c.by;
+    r.bz = c.bz;
+    return r;
+}
+
 // x^y correctly rounded to float: the double-precision power narrowed once
 // (its error is far below half a float ulp except within ~2^-28 of a float
 // rounding boundary).  The exact kernels use it so that the step controller's
@@ -327,16 +390,14 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
     float td = 0.f;
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
     if (TWIST && tw_on) {
-        j1 = sample<EXACT>(J.cur, L.p, false);
+        j1 = sample<EXACT>(current_view(f, J.cur), L.p, false);
         b1 = sample<EXACT>(f, L.p, false);
         ns += 2;
         td = dot(j1, b1) / dot(b1, b1);
         L.tw = L.tw + (double)td / 4.0 / kRefPi * (double)dl;
     }
     // inside test first: the full face classification only runs on exit
-    const bool inside = (p2.x >= 0.f) & (p2.y > 0.f) & (p2.z >= 0.f) & (p2.x <= (float)(f.d.nx - 1)) &
-                        (p2.y <= (float)(f.d.ny - 1)) & (p2.z <= (float)(f.d.nz - 1));
-    const int flag = inside ? 0 : box_flag(f.d, p2);
+    const int flag = box_inside(f, p2) ? 0 : box_exit(f, p2);
     if (flag > 0) {
         len_add(L, -(double)dl, -dl);
         if (TWIST && tw_on) L.tw = L.tw - (double)td / 4.0 / kRefPi * (double)dl;
@@ -410,8 +471,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     const float3 nrm = J.s.cross_dev ? v3(__ldg(J.s.cross_dev), __ldg(J.s.cross_dev + 1), __ldg(J.s.cross_dev + 2))
                                      : v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
-    const typename Lane<EXACT>::len_t len_lim =
-        (typename Lane<EXACT>::len_t)(J.prm.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz));
+    store_prepare(f);
+    const typename Lane<EXACT>::len_t len_lim = (typename Lane<EXACT>::len_t)(J.prm.len_ratio * len_scale(f));
     unsigned ns = 0;
     unsigned long long ns_total = 0;
     const int lane_id = threadIdx.x & 31;

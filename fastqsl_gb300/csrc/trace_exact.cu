@@ -10,32 +10,42 @@
 
 namespace qsl {
 
-template <bool TWIST, bool QUEUE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_exact(const TraceJob<FieldSoA> J) {
+template <bool TWIST, bool QUEUE, class F>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_exact(const TraceJob<F> J) {
     trace_kernel_body<true, TWIST, QUEUE>(J);
 }
 
-cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
-                               cudaStream_t st) {
-    const void* k;
-    if (sched == SCHED_QUEUE) k = twist ? (const void*)k_trace_exact<true, true> : (const void*)k_trace_exact<false, true>;
-    else k = twist ? (const void*)k_trace_exact<true, false> : (const void*)k_trace_exact<false, false>;
+template <class F>
+static cudaError_t launch_exact(const TraceJob<F>& J, bool twist, Schedule sched, long long n_host, cudaStream_t st) {
+    const bool q = sched == SCHED_QUEUE;
+    const void* k = q ? (twist ? (const void*)k_trace_exact<true, true, F> : (const void*)k_trace_exact<false, true, F>)
+                      : (twist ? (const void*)k_trace_exact<true, false, F> : (const void*)k_trace_exact<false, false, F>);
     int grid;
-    if (sched == SCHED_QUEUE) {
+    if (q) {
         grid = persistent_grid(k, kTraceBlock);
     } else {
         long long g = (n_host + kTraceBlock - 1) / kTraceBlock;
         grid = (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
     }
     if (grid <= 0) return cudaErrorInvalidConfiguration;
-    if (sched == SCHED_QUEUE) {
-        if (twist) k_trace_exact<true, true><<<grid, kTraceBlock, 0, st>>>(J);
-        else k_trace_exact<false, true><<<grid, kTraceBlock, 0, st>>>(J);
+    if (q) {
+        if (twist) k_trace_exact<true, true, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_exact<false, true, F><<<grid, kTraceBlock, 0, st>>>(J);
     } else {
-        if (twist) k_trace_exact<true, false><<<grid, kTraceBlock, 0, st>>>(J);
-        else k_trace_exact<false, false><<<grid, kTraceBlock, 0, st>>>(J);
+        if (twist) k_trace_exact<true, false, F><<<grid, kTraceBlock, 0, st>>>(J);
+        else k_trace_exact<false, false, F><<<grid, kTraceBlock, 0, st>>>(J);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,
+                               cudaStream_t st) {
+    return launch_exact(J, twist, sched, n_host, st);
+}
+
+cudaError_t launch_trace_exact_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
+                                       cudaStream_t st) {
+    return launch_exact(J, twist, sched, n_host, st);
 }
 
 template <bool TWIST>

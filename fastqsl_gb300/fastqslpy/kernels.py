@@ -86,6 +86,38 @@ class TraceAllBlineScott:
         _lib.check(_lib.load().qsl_trace_all_bline_scott(*p, cap, st), "TraceAllBlineScott")
 
 
+class TraceAllBlineStretch:
+    """TraceAllBline of fastqslpy/cu/TraceBlineAdaptiveStretch.cu:422-433 (39
+    arguments: the field, BshapeN, x_arr, y_arr, z_arr, flag_uni, then the
+    35-argument list of the uniform-grid kernel from curB_x on), which the
+    reference's stretched-grid notebook compiles itself."""
+
+    # inp_x/y/z (13-15), start..B_end_z (17-34), LineLen (37)
+    _PER_SEED = [13, 14, 15] + list(range(17, 35)) + [37]
+
+    def __init__(self, arith="exact"):
+        if arith not in _ARITH:
+            raise ValueError("arith must be 'exact' or 'fast'")
+        self.arith = arith
+        _lib.load()
+
+    def __call__(self, grid, block, args, shared_mem=0, stream=None):
+        args = tuple(args)
+        if len(args) < 39:
+            raise TypeError(f"TraceAllBline (stretched grid) takes 39 arguments, got {len(args)}")
+        cap = min(_numel(args[i]) for i in self._PER_SEED)
+        p = [ptr(a) if _numel(a) else None for a in args[:39]]
+        st = stream if stream is not None else _current_stream(args)
+        _lib.check(_lib.load().qsl_trace_all_bline_stretch(_ARITH[self.arith], *p, cap, st),
+                   "TraceAllBline (stretched grid)")
+
+
+def compileTraceBlineAdaptiveStretch(arith="exact"):
+    """RKF45 tracer on a stretched grid (the reference's stretched notebook
+    compiles fastqslpy/cu/TraceBlineAdaptiveStretch.cu and takes TraceAllBline)."""
+    return TraceAllBlineStretch(arith)
+
+
 def compileTraceBlineScott():
     """Scott deviation-vector tracer (reference notebooks compile
     fastqslpy/cu/TraceBlineScott.cu and take TraceAllBlineScott)."""

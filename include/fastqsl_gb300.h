@@ -273,6 +273,47 @@ typedef struct qsl_scott_io {
     double *twist; /* needed when curB is given */
 } qsl_scott_io;
 
+/* ------------------------------------------------------------------------
+ * Stretched (rectilinear) grids — fastqslpy/cu/TraceBlineAdaptiveStretch.cu
+ * ------------------------------------------------------------------------ */
+
+/* Reference settings of the stretched-grid tracer (TraceBlineAdaptiveStretch.cu
+ * :10-12,336-371): the RKF45 settings with len_ratio 2 applied to the summed
+ * coordinate extents, no step limit (2^31-1 here), exit-segment twist term. */
+void qsl_params_reference_stretch(qsl_trace_params *p_h);
+
+/* Replaces TraceAllBline of fastqslpy/cu/TraceBlineAdaptiveStretch.cu:422-433
+ * (compiled at run time by demo/Q_RKF45CuPyStretch.ipynb cell 9): the same 39
+ * arguments in order — the field, BshapeN, the node coordinates x_arr[nx],
+ * y_arr[ny], z_arr[nz] (increasing) and *flag_uni (true: the uniform-spacing
+ * index formula instead of the search) before the twist arguments — with
+ * arith in front and capacity (length of the per-seed arrays, -1 unknown) and
+ * the stream behind.  Cells are found exactly as the reference does, including
+ * its search's choice of the cell below the point near the top of its last
+ * interval.  The footpoint of a direction that exits through a face is placed
+ * on the plane q = 0 or q = n of the exit axis in INDEX units, as the
+ * reference's exit code does (:375-400). */
+int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, const float *Bz, const int *BshapeN,
+                                const float *x_arr, const float *y_arr, const float *z_arr, const bool *flag_uni,
+                                const float *curB_x, const float *curB_y, const float *curB_z, double *twist,
+                                const bool *curB_flag, const float *inp_x, const float *inp_y, const float *inp_z,
+                                const float *inp_cross_dir, float *start_x, float *start_y, float *start_z,
+                                int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                                float *B_this_x, float *B_this_y, float *B_this_z, int *B_flag, float *B_start_x,
+                                float *B_start_y, float *B_start_z, float *B_end_x, float *B_end_y, float *B_end_z,
+                                const float *s_len, const unsigned long long *N, double *LineLen,
+                                const float *tol_coef, int64_t capacity, qsl_stream_t stream);
+
+/* Native form: host scalars and settings; Bx/By/Bz of shape nx x ny x nz (x
+ * fastest) and the coordinates on the device; uni as above.  sched may be
+ * NULL (static one-line-per-thread grid) or give the schedule, order map and
+ * sample counter (occupancy is ignored). */
+int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz,
+                      const float *x_arr, const float *y_arr, const float *z_arr, int uni,
+                      const qsl_trace_params *prm, const qsl_trace_io *io, int64_t n, float s_len, float tol_coef,
+                      const float *cross_dir_h, const float *curBx, const float *curBy, const float *curBz,
+                      const qsl_sched *sched_h, qsl_stream_t stream);
+
 /* Reference settings of the Scott tracer (TraceBlineScott.cu:10-14): absolute
  * tolerance 1e-3*tol_coef (its tolerance variable is never initialised,
  * :352,378), length limit 2*(nx+ny+nz), 10000 steps over both directions. */

@@ -1,0 +1,115 @@
+"""Stretched-grid tracer (fastqslpy/cu/TraceBlineAdaptiveStretch.cu) on the
+GPU through the C ABI:
+
+* the drop-in entry in the reference's notebook form (exact arithmetic)
+  against the reference's own outputs (golden fixtures) and bit for bit
+  against the oracle built with the same correctly rounded power function;
+* the native entry in fast arithmetic at tight settings against the FP64
+  oracle (flags identical for >= 99 %, footpoints within 1e-3 for >= 99 %).
+"""
+import numpy as np
+import pytest
+import torch
+
+import golden_util as G
+from fastqsl_gb300 import params as P
+
+pytestmark = pytest.mark.gpu
+
+F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "B_this_x", "B_this_y", "B_this_z",
+       "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z"]
+I32 = ["flag_start", "flag_end", "B_flag"]
+
+
+def _dev(a):
+    return torch.as_tensor(np.ascontiguousarray(a)).cuda()
+
+
+def _fdev(a):
+    from fastqsl_gb300.api import as_xfast
+    return as_xfast(torch.from_numpy(np.asfortranarray(a)))
+
+
+def run_dropin_stretch(Bx, By, Bz, coords, uni, xs, ys, zs, s_len, tol_coef, curB=None, arith="exact"):
+    from fastqsl_gb300.fastqslpy import kernels
+    k = kernels.compileTraceBlineAdaptiveStretch(arith)
+    n = len(xs)
+    o = {key: torch.zeros(n, dtype=torch.float32, device="cuda") for key in F32}
+    o.update({key: torch.zeros(n, dtype=torch.int32, device="cuda") for key in I32})
+    o["LineLen"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    o["twist"] = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dummy = torch.zeros((1, 1), dtype=torch.float32, device="cuda")
+    cur = [_fdev(c) for c in curB] if curB is not None else [dummy] * 3
+    args = (_fdev(Bx), _fdev(By), _fdev(Bz), torch.tensor(list(Bx.shape), dtype=torch.int32, device="cuda"),
+            *[_dev(c) for c in coords], torch.tensor([bool(uni)], device="cuda"),
+            *cur, o["twist"], torch.tensor([curB is not None], device="cuda"),
+            _dev(xs), _dev(ys), _dev(zs), torch.tensor([0, 0, 1.0], dtype=torch.float32, device="cuda"),
+            o["start_x"], o["start_y"], o["start_z"], o["flag_start"],
+            o["end_x"], o["end_y"], o["end_z"], o["flag_end"],
+            o["B_this_x"], o["B_this_y"], o["B_this_z"], o["B_flag"],
+            o["B_start_x"], o["B_start_y"], o["B_start_z"],
+            o["B_end_x"], o["B_end_y"], o["B_end_z"],
+            torch.tensor([s_len], dtype=torch.float32, device="cuda"),
+            torch.tensor([n], dtype=torch.int64, device="cuda"), o["LineLen"],
+            torch.tensor([tol_coef], dtype=torch.float32, device="cuda"))
+    k((28, 1), (128, 1, 1), args)
+    torch.cuda.synchronize()
+    return {key: v.cpu().numpy() for key, v in o.items()}
+
+
+@pytest.mark.parametrize("name", G.STRETCH_CASES)
+def test_dropin_stretch_exact_matches_reference(cuda, oracle_port, name):
+    g, meta = G.load(name)
+    Bx, By, Bz, coords = G.stretch_field_for(meta)
+    cur = G.twist_current(Bx, By, Bz) if meta["twist"] else None
+    got = run_dropin_stretch(Bx, By, Bz, coords, meta["uni"], g["inp_x"], g["inp_y"], g["inp_z"], meta["s_len"],
+                             meta["tol_coef"], cur)
+    # against the reference's outputs: flags, and footpoints within 1e-3
+    # (RKF45's power function rounds differently from the host powf in
+    # ~6e-4 of calls)
+    flags = ((got["flag_start"] == g["flag_start"]) & (got["flag_end"] == g["flag_end"])).mean()
+    assert flags >= 0.999, flags
+    live = (g["flag_start"] != 0) & (g["flag_end"] != 0)
+    d = np.max(np.abs(np.stack([got[k] - g[k] for k in ("start_x", "start_y", "start_z", "end_x", "end_y",
+                                                        "end_z")])), axis=0)
+    assert (d[live] <= 1e-3).mean() >= 0.995
+    np.testing.assert_array_equal(got["B_this_x"], g["B_this_x"])
+    np.testing.assert_array_equal(got["B_flag"], g["B_flag"])
+    if cur is not None:  # the reference's own twist (exit-segment terms with an unset p_mid aside)
+        close = np.isclose(got["twist"], g["twist"], rtol=1e-4, atol=1e-7)
+        assert close[live].mean() >= 0.95, close[live].mean()
+    # bit for bit against the oracle with the same power function
+    cr = oracle_port.trace_all("port32cr", Bx, By, Bz, g["inp_x"], g["inp_y"], g["inp_z"], s_len=meta["s_len"],
+                               tol_coef=meta["tol_coef"], params=P.reference_stretch(), coords=coords,
+                               uni=meta["uni"])
+    assert (got["flag_end"] == cr["flag_end"]).all() and (got["flag_start"] == cr["flag_start"]).all()
+    live = (cr["flag_start"] != 0) & (cr["flag_end"] != 0)
+    for k in ("end_x", "end_y", "end_z", "start_x", "start_y", "start_z", "B_end_x", "B_start_z"):
+        assert (got[k][live] == cr[k][live]).mean() >= 0.999, k
+    rel = np.abs(got["LineLen"] - cr["LineLen"]) / np.maximum(cr["LineLen"], 1e-6)
+    assert np.median(rel[live]) < 1e-6
+
+
+def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.bipole4_stretch(5)
+    coords = S.stretched_axes(spec.shape, z_ratio=1.05)
+    Bx, By, Bz = S.make_field_coords(spec, *coords)
+    xs, ys, zs, _ = S.plane_seeds((-5, 5), (-4, 4), 48, 40, 0.3)
+    prm = P.reference_stretch(arith=P.ARITH_FAST).copy(tol_law=P.TOL_ABSOLUTE, tol=1e-5, h_min=1e-3, h_max=0.25)
+    ref = oracle_port.trace_all("port64", Bx, By, Bz, xs, ys, zs, s_len=0.01, params=prm.copy(arith=P.ARITH_EXACT),
+                                coords=coords)
+    samples = torch.zeros(1, dtype=torch.int64, device="cuda")
+    out = api.trace_stretch(*[torch.from_numpy(np.asfortranarray(b)) for b in (Bx, By, Bz)],
+                            [torch.from_numpy(c).cuda() for c in coords], _dev(xs), _dev(ys), _dev(zs), prm,
+                            s_len=0.01, samples=samples)
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    flags = ((got["flag_start"] == ref["flag_start"]) & (got["flag_end"] == ref["flag_end"])).mean()
+    assert flags >= 0.99, flags
+    live = (ref["flag_start"] != 0) & (ref["flag_end"] != 0) & (got["flag_end"] == ref["flag_end"]) & \
+           (got["flag_start"] == ref["flag_start"])
+    d = np.max(np.abs(np.stack([got[k] - ref[k] for k in ("start_x", "start_y", "start_z", "end_x", "end_y",
+                                                          "end_z")])), axis=0)
+    assert (d[live] <= 1e-3).mean() >= 0.99, np.quantile(d[live], [0.5, 0.99])
+    assert int(samples.item()) > 6 * len(xs)

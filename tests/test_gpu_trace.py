@@ -118,6 +118,9 @@ def test_dropin_exact_matches_reference(cuda, name):
     assert (got["flag_end"] == cr["flag_end"]).all() and (got["flag_start"] == cr["flag_start"]).all()
     np.testing.assert_array_equal(got["B_this_x"], g["B_this_x"])
     np.testing.assert_array_equal(got["B_flag"], g["B_flag"])
+    if twist:  # the current density is sampled on the traced field's grid
+        close = np.isclose(got["twist"], cr["twist"], rtol=1e-5, atol=1e-9)
+        assert close[live].mean() >= 0.99, close[live].mean()
     same = (got["flag_end"] == g["flag_end"]) & (got["flag_start"] == g["flag_start"])
     rel = np.abs(got["LineLen"] - g["LineLen"]) / np.maximum(g["LineLen"], 1e-6)
     assert np.median(rel[same]) < 1e-6
