@@ -80,7 +80,7 @@ def test_dropin_stretch_exact_matches_reference(cuda, oracle_port, name):
         assert close[live].mean() >= 0.95, close[live].mean()
     # bit for bit against the oracle with the same power function
     cr = oracle_port.trace_all("port32cr", Bx, By, Bz, g["inp_x"], g["inp_y"], g["inp_z"], s_len=meta["s_len"],
-                               tol_coef=meta["tol_coef"], params=P.reference_stretch(), coords=coords,
+                               tol_coef=meta["tol_coef"], params=P.reference_stretch(), curB=cur, coords=coords,
                                uni=meta["uni"])
     assert (got["flag_end"] == cr["flag_end"]).all() and (got["flag_start"] == cr["flag_start"]).all()
     live = (cr["flag_start"] != 0) & (cr["flag_end"] != 0)
@@ -88,6 +88,9 @@ def test_dropin_stretch_exact_matches_reference(cuda, oracle_port, name):
         assert (got[k][live] == cr[k][live]).mean() >= 0.999, k
     rel = np.abs(got["LineLen"] - cr["LineLen"]) / np.maximum(cr["LineLen"], 1e-6)
     assert np.median(rel[live]) < 1e-6
+    if cur is not None:
+        close = np.isclose(got["twist"], cr["twist"], rtol=1e-5, atol=1e-9)
+        assert close[live].mean() >= 0.99, close[live].mean()
 
 
 def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
