@@ -100,7 +100,10 @@ def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
     coords = S.stretched_axes(spec.shape, z_ratio=1.05)
     Bx, By, Bz = S.make_field_coords(spec, *coords)
     xs, ys, zs, _ = S.plane_seeds((-5, 5), (-4, 4), 48, 40, 0.3)
-    prm = P.reference_stretch(arith=P.ARITH_FAST).copy(tol_law=P.TOL_ABSOLUTE, tol=1e-5, h_min=1e-3, h_max=0.25)
+    # tight tolerance: at 1e-5 the FP32 rounding alone already moves 13 % of
+    # the footpoints by more than 1e-3 (accept/reject decisions flip); at 1e-7
+    # the reference-rounding FP32 oracle tracks FP64 to 1e-3 on > 99.8 %
+    prm = P.reference_stretch(arith=P.ARITH_FAST).copy(tol_law=P.TOL_ABSOLUTE, tol=1e-7, h_min=1e-4, h_max=0.25)
     ref = oracle_port.trace_all("port64", Bx, By, Bz, xs, ys, zs, s_len=0.01, params=prm.copy(arith=P.ARITH_EXACT),
                                 coords=coords)
     samples = torch.zeros(1, dtype=torch.int64, device="cuda")
