@@ -84,6 +84,8 @@ _SIGS = {
     "qsl_batch_destroy": (c_int, [_P]),
     "qsl_trace_all_bline_scott": (c_int, [_P] * 30 + [c_i64, _P]),
     "qsl_params_reference_stretch": (None, [_P]),
+    "qsl_hybrid_select": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P, _P]),
+    "qsl_hybrid_merge": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P]),
     "qsl_trace_all_bline_stretch": (c_int, [c_int] + [_P] * 39 + [c_i64, _P]),
     "qsl_trace_stretch": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, _P, _P, c_int, _P, _P, c_i64, c_float,
                                   c_float, _P, _P, _P, _P, _P, _P]),

@@ -277,8 +277,14 @@ class QMapPlan:
     DEFAULT_OCCUPANCY = {"h8c": 8, "h4b": 8, "f4": 8, "soa": 0}
 
     def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True, tile=(8, 8), chunk=256, schedule="static",
-                 occupancy=None):
+                 occupancy=None, hybrid=False):
+        """hybrid: instead of the pseudo-line pass, the interior pixels with
+        B_flag set or a NaN finite-difference Q take the Scott tracer's
+        q_perp (demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9)."""
         self.n0, self.n1, self.nplanes = int(n0), int(n1), int(nplanes)
+        self.hybrid = bool(hybrid)
+        if self.hybrid:
+            pseudo = False
         if self.n0 < 3 or self.n1 < 3:
             raise ValueError("planes must be at least 3 x 3 seeds")
         self.n = self.n0 * self.n1 * self.nplanes
@@ -305,6 +311,12 @@ class QMapPlan:
             self.work_bytes = wb
             self.sub = alloc_trace_outputs(4 * m, device)
             self.qcut = torch.empty(m, dtype=torch.float64, device=device)
+        if self.hybrid:
+            m = self.nplanes * (self.n0 - 2) * (self.n1 - 2)
+            self.max_pix = m
+            self.hseeds = torch.empty(m, dtype=torch.int32, device=device)
+            self.hcount = torch.zeros(1, dtype=torch.int64, device=device)
+            self.scott = alloc_scott_outputs(self.n, device)
 
     def occupancy_for(self, field):
         if self.occupancy is not None:
@@ -320,9 +332,13 @@ class QMapPlan:
         return self.samples_buf.sum()
 
     def run(self, field, xs, ys, zs, params=None, s_len=0.125, tol_coef=1.0, stride=1.0, cross_dir=(0.0, 0.0, 1.0),
-            pseudo_tol_factor=1.0, count_samples=False, kernel_events=None, stream=None):
+            pseudo_tol_factor=1.0, count_samples=False, kernel_events=None, stream=None, scott_params=None,
+            scott_grad="analytic"):
         """Runs the pipeline; `kernel_events` (start, end) CUDA events are
-        recorded around the main trace launch when given."""
+        recorded around the main trace launch when given.  scott_params /
+        scott_grad: the Scott pass of a hybrid plan (default: the Scott
+        tracer's reference settings in fast arithmetic with the main trace's
+        tolerance and step bounds)."""
         lib = _lib.load()
         st = stream_handle(stream)
         if params is None:
@@ -345,6 +361,8 @@ class QMapPlan:
                                        ptr(m["B_start_z"]), ptr(m["B_end_z"]), ptr(m["B_this_x"]),
                                        ptr(m["B_this_y"]), ptr(m["B_this_z"]), self.n0, self.n1, self.nplanes, jac,
                                        cd, None, ptr(self.Q), st), "qsl_qcalc_plane")
+        if self.hybrid:
+            return self._hybrid(field, xs, ys, zs, params, s_len, tol_coef, scott_params, scott_grad, stream, st)
         if not self.pseudo:
             return self.Q
         _lib.check(lib.qsl_cook_pseudo_line(ptr(m["B_flag"]), ptr(m["start_x"]), ptr(m["start_y"]),
@@ -367,6 +385,27 @@ class QMapPlan:
         _lib.check(lib.qsl_qmerge(ptr(self.pix), None, ptr(self.qcut), 0, ptr(self.count[0:1]), self.max_pix,
                                   self.n0, self.n1, None, ptr(self.Q), st), "qsl_qmerge")
         return self.Q
+
+
+def _hybrid_impl(self, field, xs, ys, zs, params, s_len, tol_coef, scott_params, scott_grad, stream, st):
+    """Select -> Scott on the selected seeds (count and order on the device)
+    -> merge q_perp into Q."""
+    from .params import reference_scott
+    lib = _lib.load()
+    m = self.main
+    if scott_params is None:
+        scott_params = reference_scott(arith=params.arith).copy(tol=params.tol, h_min=params.h_min,
+                                                                h_max=params.h_max)
+    _lib.check(lib.qsl_hybrid_select(ptr(m["B_flag"]), ptr(self.Q), self.n0, self.n1, self.nplanes,
+                                     ptr(self.hseeds), ptr(self.hcount), st), "qsl_hybrid_select")
+    trace_scott(field, xs, ys, zs, scott_params, s_len, tol_coef, grad=scott_grad, out=self.scott, n=self.max_pix,
+                n_dev=self.hcount, order=self.hseeds, stream=stream)
+    _lib.check(lib.qsl_hybrid_merge(ptr(m["B_flag"]), ptr(self.scott["q_perp"]), self.n0, self.n1, self.nplanes,
+                                    ptr(self.Q), st), "qsl_hybrid_merge")
+    return self.Q
+
+
+QMapPlan._hybrid = _hybrid_impl
 
 
 def plane_seed_grid(x0, x1, nx, y0, y1, ny, zs, device="cuda"):

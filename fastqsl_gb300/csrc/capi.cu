@@ -967,6 +967,24 @@ int qsl_qmerge(const int64_t* pix, const float* Qcut32, const double* Qcut64, in
     return QSL_OK;
 }
 
+int qsl_hybrid_select(const int* B_flag, const double* Q, int n0, int n1, int64_t nplanes, unsigned* seeds,
+                      unsigned long long* count_dev, qsl_stream_t stream) {
+    if (!B_flag || !Q || !seeds || !count_dev) return fail(QSL_ERR_INVALID, "null argument");
+    if (n0 < 3 || n1 < 3 || nplanes < 0) return fail(QSL_ERR_INVALID, "planes must be at least 3 x 3");
+    if ((double)nplanes * n0 * n1 > 4294967295.0) return fail(QSL_ERR_TOO_LARGE, "seed indices exceed 32 bits");
+    QSL_CHECK_CUDA(launch_hybrid_select(B_flag, Q, n0, n1, nplanes, seeds, count_dev, (cudaStream_t)stream),
+                   "hybrid select");
+    return QSL_OK;
+}
+
+int qsl_hybrid_merge(const int* B_flag, const float* q_perp, int n0, int n1, int64_t nplanes, double* Q,
+                     qsl_stream_t stream) {
+    if (!B_flag || !q_perp || !Q) return fail(QSL_ERR_INVALID, "null argument");
+    if (n0 < 3 || n1 < 3 || nplanes < 0) return fail(QSL_ERR_INVALID, "planes must be at least 3 x 3");
+    QSL_CHECK_CUDA(launch_hybrid_merge(B_flag, q_perp, n0, n1, nplanes, Q, (cudaStream_t)stream), "hybrid merge");
+    return QSL_OK;
+}
+
 int qsl_device_sm_count(int* sms) {
     int dev = 0;
     QSL_CHECK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");

@@ -58,6 +58,12 @@ cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long lo
 cudaError_t launch_trace_batch_h8c(const TraceJob<FieldH8C>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, cudaStream_t st);
 
+// hybrid.cu
+cudaError_t launch_hybrid_select(const int* bflag, const double* q, long long n0, long long n1, long long nplanes,
+                                 unsigned* seeds, unsigned long long* count, cudaStream_t st);
+cudaError_t launch_hybrid_merge(const int* bflag, const float* qperp, long long n0, long long n1, long long nplanes,
+                                double* q, cudaStream_t st);
+
 // field_store.cu
 cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);
 cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,

@@ -314,6 +314,25 @@ int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx,
                       const float *cross_dir_h, const float *curBx, const float *curBy, const float *curBz,
                       const qsl_sched *sched_h, qsl_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Hybrid finite-difference + Scott Q — demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9
+ * ------------------------------------------------------------------------ */
+
+/* Lists the seeds of the interior pixels of nplanes stacked (n0, n1) planes
+ * whose finite-difference Q (Q, shape nplanes x (n0-2) x (n1-2), from
+ * qsl_qcalc_plane) is unusable: B_flag set at the seed, or Q NaN.  seeds
+ * (device, capacity nplanes*(n0-2)*(n1-2)) receives their seed indices in no
+ * particular order, *count_dev (device) their number; nothing is read back to
+ * the host.  Feed them to qsl_trace_scott as its order map with count_dev as
+ * the line count, then call qsl_hybrid_merge. */
+int qsl_hybrid_select(const int *B_flag, const double *Q, int n0, int n1, int64_t nplanes, unsigned *seeds,
+                      unsigned long long *count_dev, qsl_stream_t stream);
+
+/* Q of every interior pixel selected as above becomes q_perp at its seed
+ * (float, seed-indexed, the Scott tracer's output). */
+int qsl_hybrid_merge(const int *B_flag, const float *q_perp, int n0, int n1, int64_t nplanes, double *Q,
+                     qsl_stream_t stream);
+
 /* Reference settings of the Scott tracer (TraceBlineScott.cu:10-14): absolute
  * tolerance 1e-3*tol_coef (its tolerance variable is never initialised,
  * :352,378), length limit 2*(nx+ny+nz), 10000 steps over both directions. */

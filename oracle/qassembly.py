@@ -241,3 +241,41 @@ def qmap_pipeline(trace_fn, xs, ys, zs, nplanes, n0, n1, stride, cross_dir=(0.0,
         off += k
         out.append(Q)
     return np.stack(out)
+
+
+def hybrid_merge(Q, B_flag, q_perp):
+    """Hybrid finite-difference + Scott Q of one plane (the crop of
+    demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9 to the interior pixels): Q of
+    the interior pixels with B_flag set or Q NaN becomes q_perp of their seed.
+    Q: (n0-2, n1-2); B_flag, q_perp: (n0, n1)."""
+    bad = (B_flag[1:-1, 1:-1] != 0) | np.isnan(Q)
+    out = np.array(Q, dtype=np.float64, copy=True)
+    out[bad] = np.asarray(q_perp, np.float64)[1:-1, 1:-1][bad]
+    return out
+
+
+def qmap_hybrid(trace_fn, scott_fn, xs, ys, zs, nplanes, n0, n1, stride, cross_dir=(0.0, 0.0, 1.0)):
+    """The hybrid Q-map workflow on stacked (n0, n1) planes: FP64 finite
+    difference Q, then the Scott tracer (scott_fn(xs, ys, zs) -> dict with
+    'q_perp') on the seeds of the interior pixels it cannot serve.  Returns
+    (Q, n_selected)."""
+    o = trace_fn(xs, ys, zs)
+    shp = (nplanes, n0, n1)
+    r = {k: np.asarray(v).reshape(shp) for k, v in o.items() if isinstance(v, np.ndarray) and v.size == xs.size}
+    Qs, sel = [], []
+    for p in range(nplanes):
+        g = {k: v[p] for k, v in r.items()}
+        bn = (np.float64(g["B_this_x"]) * cross_dir[0] + np.float64(g["B_this_y"]) * cross_dir[1]
+              + np.float64(g["B_this_z"]) * cross_dir[2])
+        Q = qcalc_plane_f64(g["end_x"], g["end_y"], g["end_z"], g["flag_end"], g["start_x"], g["start_y"],
+                            g["start_z"], g["flag_start"], g["B_start_z"], g["B_end_z"], bn, stride)
+        bad = np.zeros((n0, n1), bool)
+        bad[1:-1, 1:-1] = (g["B_flag"][1:-1, 1:-1] != 0) | np.isnan(Q)
+        Qs.append(Q)
+        sel.append(np.flatnonzero(bad.ravel()) + p * n0 * n1)
+    idx = np.concatenate(sel) if sel else np.zeros(0, np.int64)
+    q_perp = np.full(nplanes * n0 * n1, np.nan, np.float32)
+    if idx.size:
+        q_perp[idx] = scott_fn(np.asarray(xs)[idx], np.asarray(ys)[idx], np.asarray(zs)[idx])["q_perp"]
+    q_perp = q_perp.reshape(shp)
+    return np.stack([hybrid_merge(Qs[p], r["B_flag"][p], q_perp[p]) for p in range(nplanes)]), int(idx.size)
