@@ -85,6 +85,7 @@ _SIGS = {
     "qsl_trace_all_bline_scott": (c_int, [_P] * 30 + [c_i64, _P]),
     "qsl_params_reference_stretch": (None, [_P]),
     "qsl_hybrid_select": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P, _P]),
+    "qsl_curl_grid": (c_int, [_P, _P, _P, c_int, c_int, c_int] + [_P] * 7),
     "qsl_hybrid_merge": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P]),
     "qsl_trace_all_bline_stretch": (c_int, [c_int] + [_P] * 39 + [c_i64, _P]),
     "qsl_trace_stretch": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, _P, _P, c_int, _P, _P, c_i64, c_float,

@@ -967,6 +967,18 @@ int qsl_qmerge(const int64_t* pix, const float* Qcut32, const double* Qcut64, in
     return QSL_OK;
 }
 
+int qsl_curl_grid(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz, const float* x_arr,
+                  const float* y_arr, const float* z_arr, double* curl_x, double* curl_y, double* curl_z,
+                  qsl_stream_t stream) {
+    if (!Bx || !By || !Bz || !x_arr || !y_arr || !z_arr || !curl_x || !curl_y || !curl_z)
+        return fail(QSL_ERR_INVALID, "null argument");
+    if (nx < 3 || ny < 3 || nz < 3 || !dims_ok(nx, ny, nz))
+        return fail(QSL_ERR_INVALID, "curl needs at least 3 nodes per axis (%d x %d x %d)", nx, ny, nz);
+    QSL_CHECK_CUDA(launch_curl(Bx, By, Bz, x_arr, y_arr, z_arr, nx, ny, nz, curl_x, curl_y, curl_z,
+                               (cudaStream_t)stream), "curl");
+    return QSL_OK;
+}
+
 int qsl_hybrid_select(const int* B_flag, const double* Q, int n0, int n1, int64_t nplanes, unsigned* seeds,
                       unsigned long long* count_dev, qsl_stream_t stream) {
     if (!B_flag || !Q || !seeds || !count_dev) return fail(QSL_ERR_INVALID, "null argument");

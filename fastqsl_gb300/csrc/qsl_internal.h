@@ -58,6 +58,10 @@ cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long lo
 cudaError_t launch_trace_batch_h8c(const TraceJob<FieldH8C>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, cudaStream_t st);
 
+// curl.cu (compiled with -fmad=false)
+cudaError_t launch_curl(const float* bx, const float* by, const float* bz, const float* ax, const float* ay,
+                        const float* az, int nx, int ny, int nz, double* cx, double* cy, double* cz, cudaStream_t st);
+
 // hybrid.cu
 cudaError_t launch_hybrid_select(const int* bflag, const double* q, long long n0, long long n1, long long nplanes,
                                  unsigned* seeds, unsigned long long* count, cudaStream_t st);

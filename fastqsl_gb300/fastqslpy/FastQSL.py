@@ -175,10 +175,18 @@ def copy_boundary(arr):
 
 
 def curl_of_B_grid(Bx, By, Bz, arr_x, arr_y, arr_z):
-    """curl B by three-point differences (FastQSL.py:120-131); float64."""
-    Bx, By, Bz = (torch.as_tensor(b, device="cuda").to(torch.float64) for b in (Bx, By, Bz))
-    cx, cy, cz = (torch.zeros(Bx.shape, dtype=torch.float64, device=Bx.device) for _ in range(3))
-    cx[1:-1, 1:-1, 1:-1] = diff_3point(Bz, arr_y, 1) - diff_3point(By, arr_z, 2)
-    cy[1:-1, 1:-1, 1:-1] = diff_3point(Bx, arr_z, 2) - diff_3point(Bz, arr_x, 0)
-    cz[1:-1, 1:-1, 1:-1] = diff_3point(By, arr_x, 0) - diff_3point(Bx, arr_y, 1)
-    return tuple(copy_boundary(c) for c in (cx, cy, cz))
+    """curl B by three-point differences with the boundary copy
+    (FastQSL.py:120-141) on the GPU (qsl_curl_grid): float32 arithmetic in
+    the reference's order, float64 results of shape (nx, ny, nz), x fastest in
+    memory, ready (after .float()) to be the current density of the twist
+    integral."""
+    from .. import _lib
+    from ..api import as_xfast, ptr, stream_handle
+    arrs = [as_xfast(b) for b in (Bx, By, Bz)]
+    nx, ny, nz = (int(v) for v in arrs[0].shape)
+    dev = arrs[0].device
+    ax = [torch.as_tensor(c).to(device=dev, dtype=torch.float32).contiguous() for c in (arr_x, arr_y, arr_z)]
+    out = [torch.empty((nz, ny, nx), dtype=torch.float64, device=dev).permute(2, 1, 0) for _ in range(3)]
+    _lib.check(_lib.load().qsl_curl_grid(*[ptr(a) for a in arrs], nx, ny, nz, *[ptr(a) for a in ax],
+                                         *[ptr(o) for o in out], stream_handle()), "qsl_curl_grid")
+    return tuple(out)

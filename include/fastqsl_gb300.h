@@ -314,6 +314,15 @@ int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx,
                       const float *cross_dir_h, const float *curBx, const float *curBy, const float *curBz,
                       const qsl_sched *sched_h, qsl_stream_t stream);
 
+/* curl B of a field (x fastest, nx x ny x nz) on node coordinates x_arr,
+ * y_arr, z_arr (device; 0..n-1 for the integer grid) by the reference's
+ * three-point non-uniform difference with its boundary copy
+ * (fastqslpy/FastQSL.py:120-163, curl_of_B_grid): float32 arithmetic in the
+ * reference's order, float64 outputs.  Needs at least 3 nodes per axis. */
+int qsl_curl_grid(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz, const float *x_arr,
+                  const float *y_arr, const float *z_arr, double *curl_x, double *curl_y, double *curl_z,
+                  qsl_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Hybrid finite-difference + Scott Q — demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9
  * ------------------------------------------------------------------------ */

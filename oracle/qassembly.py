@@ -279,3 +279,39 @@ def qmap_hybrid(trace_fn, scott_fn, xs, ys, zs, nplanes, n0, n1, stride, cross_d
         q_perp[idx] = scott_fn(np.asarray(xs)[idx], np.asarray(ys)[idx], np.asarray(zs)[idx])["q_perp"]
     q_perp = q_perp.reshape(shp)
     return np.stack([hybrid_merge(Qs[p], r["B_flag"][p], q_perp[p]) for p in range(nplanes)]), int(idx.size)
+
+
+def _diff3(C, a, axis):
+    """Three-point non-uniform derivative at the interior nodes along `axis`
+    (fastqslpy/FastQSL.py:143-163), in the arrays' float32 arithmetic."""
+    a = np.asarray(a, np.float32)
+    d = a[1:] - a[:-1]
+    shape = [1, 1, 1]
+    shape[axis] = -1
+    dl, dr = d[:-1].reshape(shape), d[1:].reshape(shape)
+    n = C.shape[axis]
+
+    def take(lo, hi):
+        s = [slice(1, -1)] * 3
+        s[axis] = slice(lo, hi)
+        return C[tuple(s)]
+    c0, cp, cm = take(1, n - 1), take(2, n), take(0, n - 2)
+    return (cp - c0) / dr * dl / (dr + dl) + (c0 - cm) / dl * dr / (dr + dl)
+
+
+def curl_grid(Bx, By, Bz, xa, ya, za):
+    """curl B with the reference's boundary copy (FastQSL.py:120-141);
+    float64 arrays of the field's shape."""
+    Bx, By, Bz = (np.asarray(b, np.float32) for b in (Bx, By, Bz))
+    out = [np.zeros(Bx.shape) for _ in range(3)]
+    out[0][1:-1, 1:-1, 1:-1] = _diff3(Bz, ya, 1) - _diff3(By, za, 2)
+    out[1][1:-1, 1:-1, 1:-1] = _diff3(Bx, za, 2) - _diff3(Bz, xa, 0)
+    out[2][1:-1, 1:-1, 1:-1] = _diff3(By, xa, 0) - _diff3(Bx, ya, 1)
+    for a in out:
+        a[:, :, 0] = a[:, :, 1]
+        a[:, 0, :] = a[:, 1, :]
+        a[0, :, :] = a[1, :, :]
+        a[:, :, -1] = a[:, :, -2]
+        a[:, -1, :] = a[:, -2, :]
+        a[-1, :, :] = a[-2, :, :]
+    return tuple(out)

@@ -86,6 +86,20 @@ def stretch_case(name, seed, z_ratio, uni, twist=False, s_len=0.01, tol_coef=1.0
     save(name, meta=json.dumps(meta), inp_x=xs, inp_y=ys, inp_z=zs, xa=xa, ya=ya, za=za, **out)
 
 
+def curl_case():
+    """curl_of_B_grid of the reference's FastQSL.py (NumPy as CuPy) on a
+    small stretched grid."""
+    FastQSL = reference_fastqsl()
+    spec = S.bipole4_stretch(6, shape=(20, 16, 12))
+    xa, ya, za = S.stretched_axes(spec.shape, z_ratio=1.08)
+    Bx, By, Bz = S.make_field_coords(spec, xa, ya, za)
+    cx, cy, cz = FastQSL.curl_of_B_grid(Bx, By, Bz, xa, ya, za)
+    meta = dict(spec="bipole4_stretch", seed=6, shape=[20, 16, 12], z_ratio=1.08,
+                fingerprint=S.field_fingerprint(Bx, By, Bz))
+    save("curl_stretch.npz", meta=json.dumps(meta), xa=xa, ya=ya, za=za, curl_x=np.asarray(cx),
+         curl_y=np.asarray(cy), curl_z=np.asarray(cz))
+
+
 def probes_case():
     spec = S.bipole4_64(3)
     Bx, By, Bz = S.make_field(spec)
@@ -192,6 +206,8 @@ def main():
         raise SystemExit("oracle/_ref not built: run python oracle/build.py in a checkout with the reference")
     if sys.argv[1:] == ["stretch"]:  # only the stretched-grid fixtures
         return stretch_cases()
+    if sys.argv[1:] == ["curl"]:
+        return curl_case()
     trace_case("trace_rk4_bipole4_64.npz", "rk4", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 0.0, 0.1, 1.0)
     trace_case("trace_rkf45_bipole4_64.npz", "rkf45", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 1e-4,
                0.125, 0.5)
@@ -202,6 +218,7 @@ def main():
     probes_case()
     qmap_case()
     stretch_cases()
+    curl_case()
 
 
 def stretch_cases():

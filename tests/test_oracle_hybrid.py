@@ -1,7 +1,11 @@
-"""The oracle's hybrid finite-difference + Scott Q (oracle/qassembly.py)
-against the reference's own notebook cell that defines it
-(demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9), executed from the notebook file
-with NumPy standing in for CuPy and a stand-in Scott kernel."""
+"""Host-side Q-assembly pieces of the oracle pinned to the reference:
+
+* the hybrid finite-difference + Scott Q merge (oracle/qassembly.py) against
+  the reference's own notebook cell that defines it
+  (demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9), executed from the notebook file
+  with NumPy standing in for CuPy and a stand-in Scott kernel;
+* curl B on a stretched grid against the reference's curl_of_B_grid
+  (golden fixture made by tests/golden/make_golden.py)."""
 import json
 import os
 import types
@@ -74,3 +78,15 @@ def test_hybrid_merge_matches_reference_notebook():
     mine = QA.hybrid_merge(Q, np.asarray(B_flag).reshape(xy_shape),
                            _q_of_seed(np.asarray(x_inp), np.asarray(y_inp)).reshape(xy_shape))
     np.testing.assert_array_equal(mine.astype(np.float32), ref.astype(np.float32))
+
+
+def test_curl_matches_reference_fixture():
+    import golden_util as G
+    from fastqsl_gb300 import synthetic as S
+    g, meta = G.load("curl_stretch.npz")
+    spec = S.bipole4_stretch(meta["seed"], shape=tuple(meta["shape"]))
+    xa, ya, za = S.stretched_axes(spec.shape, z_ratio=meta["z_ratio"])
+    Bx, By, Bz = S.make_field_coords(spec, xa, ya, za)
+    assert S.field_fingerprint(Bx, By, Bz) == meta["fingerprint"]
+    for mine, k in zip(QA.curl_grid(Bx, By, Bz, xa, ya, za), ("curl_x", "curl_y", "curl_z")):
+        np.testing.assert_array_equal(mine, g[k])
