@@ -42,7 +42,11 @@ def test_hybrid_qmap_vs_fp64_oracle(cuda, oracle_port):
     assert abs(nref - nsel) <= max(3, 0.02 * nref)
     nan_same = np.isnan(Q) == np.isnan(Qref)
     assert nan_same.mean() >= 0.99
-    ok = ~np.isnan(Q) & ~np.isnan(Qref)
+    # the Scott tracer leaves q_perp 0 where a line does not reach the box
+    # faces at both ends; those pixels must agree too
+    both = ~np.isnan(Q) & ~np.isnan(Qref)
+    assert ((Q[both] == 0) == (Qref[both] == 0)).mean() >= 0.99
+    ok = both & (Q > 0) & (Qref > 0)
     d = np.abs(np.log10(Q[ok]) - np.log10(Qref[ok]))
     assert np.median(d) <= 1e-3 and np.quantile(d, 0.99) <= 1e-2, (np.median(d), np.quantile(d, 0.99))
     ds = np.abs(np.log10(Q[ok & sel]) - np.log10(Qref[ok & sel]))
