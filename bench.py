@@ -146,8 +146,8 @@ def run_ours(args, rank, world):
     samples_main = int(plan.samples_main.item())
     samples_all = int(plan.samples.item())
 
-    if world > 1:
-        torch.distributed.barrier()
+    from fastqsl_gb300 import replicas
+    replicas.barrier()
     torch.cuda.synchronize()
     kev = []
     with ClockSampler(dev.index) as clk:
@@ -160,13 +160,10 @@ def run_ours(args, rank, world):
             step(ev=ev)
         t1.record(stream)
         torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms = t0.elapsed_time(t1) / args.steps
-    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(ms_t.item())
+    replicas.barrier()
+    # every rank traced its own copy of the cube (weak scaling, no exchange
+    # on the data path); the job took as long as the slowest rank
+    ms = replicas.max_over_ranks(t0.elapsed_time(t1) / args.steps, device=dev)
     k_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
     Q = plan.Q
 
@@ -411,7 +408,8 @@ def main():
         return
     peak, peak_kind = peaks()
     ms = res["ms"]
-    value = res["qpix"] * world / (ms / 1e3)
+    from fastqsl_gb300 import replicas
+    value = replicas.whole_job_rate(res["qpix"], ms, world)
     fp16 = args.layout in ("h4b", "h8c")
     bytes_per_sample = 48 if fp16 else 96
     achieved = res["samples_main"] * bytes_per_sample / (res["k_ms"] / 1e3) / 1e9
