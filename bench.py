@@ -196,6 +196,17 @@ def run_ours(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         res["ours_trace_ms"] = e0.elapsed_time(e1) / reps
+        # the reference kernel's design on this GPU: one line per thread in
+        # seed order, SoA float32 field, the reference's rounding (corner
+        # weights in double), work-queue grid; same settings, one run
+        prm_x = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_EXACT)
+        api.trace(soa, xs, ys, zz, prm_x, s_len=S_LEN, schedule="queue", out=out)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        api.trace(soa, xs, ys, zz, prm_x, s_len=S_LEN, schedule="queue", out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res["exact_trace_ms"] = e0.elapsed_time(e1)
         soa.close()
 
     # ---- end to end through the public API with host buffers ----
@@ -425,7 +436,11 @@ def main():
         "gpu_launches": None,
         "clocks": res["clocks"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     # DRAM bytes per launch: ncu's dram__bytes_read.sum + write.sum
+                     # on the 8-plane case (2.004 GB for 913.9 M samples,
+                     # profiles/trace_h4b_cube8.md) scaled by this launch's samples
+                     "traffic": (2.004e9 / 913.9e6) * res["samples_main"] if args.layout == "h4b" else None,
                      "kernel": f"k_trace_fast<static, {STORE_TYPES[args.layout]}> (main trace)",
                      "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
                              f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
@@ -439,7 +454,10 @@ def main():
                                   f"({'default' if args.no_autotune else 'autotuned'})")
     if "plain_trace_ms" in res:
         line["plain_fp32"] = {"trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
-                              "speedup": res["plain_trace_ms"] / res["ours_trace_ms"]}
+                              "speedup": res["plain_trace_ms"] / res["ours_trace_ms"],
+                              "reference_design_trace_ms": res.get("exact_trace_ms"),
+                              "speedup_vs_reference_design": res["exact_trace_ms"] / res["ours_trace_ms"]
+                              if res.get("exact_trace_ms") else None}
     if "e2e_ms" in res:
         line["e2e"] = {"value": res["qpix"] / (res["e2e_ms"] / 1e3), "unit": "Q-pixels/s",
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]}
