@@ -465,9 +465,11 @@ class BatchPlan:
         self.info = info
         self.lines = int(info.lines)
 
-    def launch(self, samples=None, stream=None):
-        _lib.check(_lib.load().qsl_batch_run(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
-                                             stream_handle(stream)), "qsl_batch_run")
+    def launch(self, samples=None, stream=None, max_blocks=0):
+        """max_blocks > 0: at most that many resident blocks (they loop over
+        the lines), leaving the rest of the GPU's block slots free."""
+        _lib.check(_lib.load().qsl_batch_run_capped(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
+                                                    int(max_blocks), stream_handle(stream)), "qsl_batch_run")
 
 
 class QBatch:
@@ -482,7 +484,14 @@ class QBatch:
     specs: list of dicts with keys field, xs, ys, zs (flattened stacked
     planes), n0, n1, nplanes, params, s_len, tol_coef, stride, cross_dir."""
 
-    def __init__(self, specs, device="cuda", tile=(8, 8), stream=None):
+    def __init__(self, specs, device="cuda", tile=(8, 8), stream=None, blocks_per_sm=0):
+        """blocks_per_sm > 0: the batched traces keep at most that many
+        resident blocks per SM (see BatchPlan.launch)."""
+        self.max_blocks = 0
+        if blocks_per_sm:
+            sms = ctypes.c_int(0)
+            _lib.check(_lib.load().qsl_device_sm_count(ctypes.byref(sms)), "qsl_device_sm_count")
+            self.max_blocks = int(blocks_per_sm) * sms.value
         self.specs = specs
         lib = _lib.load()
         self.jobs = []
@@ -518,7 +527,7 @@ class QBatch:
     def run(self, stream=None):
         lib = _lib.load()
         st = stream_handle(stream)
-        self.main_batch.launch(stream=stream)
+        self.main_batch.launch(stream=stream, max_blocks=self.max_blocks)
         for J in self.jobs:
             sp, m = J["sp"], J["main"]
             jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0
@@ -534,7 +543,7 @@ class QBatch:
                                                 float(sp.get("stride", 1.0)), ptr(J["cut"][0]), ptr(J["cut"][1]),
                                                 ptr(J["cut"][2]), ptr(J["bz0s"]), ptr(J["bz0e"]), ptr(J["pix"]),
                                                 ptr(J["count"]), ptr(J["work"]), J["work_bytes"], st), "cook")
-        self.sub_batch.launch(stream=stream)
+        self.sub_batch.launch(stream=stream, max_blocks=self.max_blocks)
         for J in self.jobs:
             sp, s = J["sp"], J["sub"]
             jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0

@@ -82,9 +82,10 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_batch(const TraceJob<F
 
 template <class F>
 static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin, int njobs, long long total,
-                                bool twist, unsigned long long* samples, cudaStream_t st) {
+                                bool twist, unsigned long long* samples, int max_blocks, cudaStream_t st) {
     if (njobs <= 0 || total <= 0) return cudaSuccess;
     long long g = (total + kTraceBlock - 1) / kTraceBlock;
+    if (max_blocks > 0 && g > max_blocks) g = max_blocks;  // the grid-stride loop covers the rest
     const int grid = (int)(g > (1 << 30) ? (1 << 30) : g);
     if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
     else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);

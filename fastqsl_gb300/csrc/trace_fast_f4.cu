@@ -14,8 +14,9 @@ cudaError_t launch_scott_fast_f4(const ScottJob<FieldF4>& J, int grad, bool twis
 }
 
 cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs,
-                                   long long total, bool twist, unsigned long long* samples, cudaStream_t st) {
-    return launch_batch(jobs, begin, njobs, total, twist, samples, st);
+                                   long long total, bool twist, unsigned long long* samples, int max_blocks,
+                                   cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, max_blocks, st);
 }
 
 }  // namespace qsl

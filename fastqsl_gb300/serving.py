@@ -15,7 +15,9 @@ sub-box) and an RKF45 tolerance.  The scheduler loop:
   CUDA streams, so a batch starts while earlier ones are still on the GPU and
   their work overlaps on the device.  Smaller classes run on higher-priority
   streams: their blocks are dispatched ahead of a large batch's remaining
-  blocks, so a small request does not wait for a large one to finish.
+  blocks, and larger classes keep at most `big_blocks_per_sm` of the 8
+  resident block slots per SM, so a small request finds free slots at once
+  instead of waiting for a large batch's blocks to retire.
 
 Nothing in the loop synchronises the device: allocations come from the
 caching allocator on the batch's stream, the job table is copied
@@ -125,7 +127,7 @@ class QServer:
     CLASSES = ((1.5e5, 32, 2), (1.2e6, 8, 2), (float("inf"), 2, 2))
 
     def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
-                 tile=(8, 8), device="cuda", classes=None):
+                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6):
         self.fields = dict(fields)
         self.budget = int(hbm_budget)
         self.used = 0
@@ -143,6 +145,10 @@ class QServer:
         self._next_stream = [0] * len(self.classes)
         self.s_len, self.h_min, self.h_max = s_len, h_min, h_max
         self.tile = tile
+        # batches of all but the smallest class keep at most this many of
+        # the 8 resident block slots per SM, so the smallest requests' blocks
+        # (on the highest-priority stream) start at once (0 = no cap)
+        self.big_blocks_per_sm = int(big_blocks_per_sm)
         self.pending = [collections.deque() for _ in self.classes]
         self.flights = []
         self.done = []
@@ -215,7 +221,8 @@ class QServer:
                 prm = absolute_rkf45(tol=r.tol, h_min=self.h_min, h_max=self.h_max)
                 specs.append(dict(field=self.fields[r.field], xs=xs, ys=ys, zs=zs, n0=r.n0, n1=r.n1,
                                   nplanes=r.nplanes, params=prm, s_len=self.s_len, stride=r.spacing, cross_dir=nrm))
-            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st)
+            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st,
+                            blocks_per_sm=self.big_blocks_per_sm if cls > 0 else 0)
             qs = qb.run(stream=st)
             hosts = []
             for q in qs:
