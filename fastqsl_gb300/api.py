@@ -465,11 +465,18 @@ class BatchPlan:
         self.info = info
         self.lines = int(info.lines)
 
-    def launch(self, samples=None, stream=None, max_blocks=0):
-        """max_blocks > 0: at most that many resident blocks (they loop over
-        the lines), leaving the rest of the GPU's block slots free."""
-        _lib.check(_lib.load().qsl_batch_run_capped(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
-                                                    int(max_blocks), stream_handle(stream)), "qsl_batch_run")
+    def launch(self, samples=None, stream=None, max_blocks=0, lo=0, hi=-1):
+        """Lines [lo, hi) of the batch (hi < 0: all); max_blocks > 0: at most
+        that many resident blocks (they loop over the lines), leaving the rest
+        of the GPU's block slots free."""
+        _lib.check(_lib.load().qsl_batch_run_window(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
+                                                    int(lo), int(hi), int(max_blocks), stream_handle(stream)),
+                   "qsl_batch_run")
+
+    @property
+    def lines(self):
+        """Length of the longest store type's line space (padded per job)."""
+        return max(int(self.info.total[k]) for k in range(4))
 
 
 class QBatch:
@@ -524,10 +531,22 @@ class QBatch:
         self.sub_batch = BatchPlan(sub_jobs, stream=stream)
         self.graph = None
 
+    @property
+    def main_lines(self):
+        return self.main_batch.lines
+
     def run(self, stream=None):
+        self.run_main(stream)
+        return self.run_post(stream)
+
+    def run_main(self, stream=None, lo=0, hi=-1):
+        """The batched main trace, or the window [lo, hi) of its lines."""
+        self.main_batch.launch(stream=stream, max_blocks=self.max_blocks, lo=lo, hi=hi)
+
+    def run_post(self, stream=None):
+        """Everything after the main trace: Q, pseudo-lines, merge."""
         lib = _lib.load()
         st = stream_handle(stream)
-        self.main_batch.launch(stream=stream, max_blocks=self.max_blocks)
         for J in self.jobs:
             sp, m = J["sp"], J["main"]
             jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0

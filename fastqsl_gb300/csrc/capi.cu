@@ -626,18 +626,18 @@ static void batch_layout(const BatchLists& L, qsl_batch_info* info) {
 // One launch per store type with jobs (a type without jobs launches nothing).
 static cudaError_t launch_slots(void* const jobs[], long long* const begin[], const int njobs[],
                                 const long long total[], const bool twist[], unsigned long long* samples,
-                                int max_blocks, cudaStream_t st) {
+                                int max_blocks, long long lo, long long hi, cudaStream_t st) {
     cudaError_t e = launch_trace_batch_soa((const TraceJob<FieldSoA>*)jobs[0], begin[0], njobs[0], total[0], twist[0],
-                                           samples, max_blocks, st);
+                                           samples, max_blocks, lo, hi, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_f4((const TraceJob<FieldF4>*)jobs[1], begin[1], njobs[1], total[1], twist[1], samples,
-                                  max_blocks, st);
+                                  max_blocks, lo, hi, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_h4b((const TraceJob<FieldH4B>*)jobs[2], begin[2], njobs[2], total[2], twist[2],
-                                   samples, max_blocks, st);
+                                   samples, max_blocks, lo, hi, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_h8c((const TraceJob<FieldH8C>*)jobs[3], begin[3], njobs[3], total[3], twist[3],
-                                   samples, max_blocks, st);
+                                   samples, max_blocks, lo, hi, st);
     return e;
 }
 
@@ -660,8 +660,8 @@ int qsl_batch_pack(const qsl_batch_job* jobs_h, int njobs, void* table_h, int64_
     return QSL_OK;
 }
 
-int qsl_batch_run_capped(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
-                         int max_blocks, qsl_stream_t stream) {
+int qsl_batch_run_window(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
+                         int64_t line_lo, int64_t line_hi, int max_blocks, qsl_stream_t stream) {
     if (!table_dev || !info_h) return fail(QSL_ERR_INVALID, "null table or info");
     if (max_blocks < 0) return fail(QSL_ERR_INVALID, "max_blocks must be >= 0");
     char* t = (char*)table_dev;
@@ -678,14 +678,15 @@ int qsl_batch_run_capped(const void* table_dev, const qsl_batch_info* info_h, un
         total[k] = I.total[k];
         tw[k] = I.twist[k] != 0;
     }
-    QSL_CHECK_CUDA(launch_slots(jobs, begin, nj, total, tw, samples_dev, max_blocks, (cudaStream_t)stream),
+    QSL_CHECK_CUDA(launch_slots(jobs, begin, nj, total, tw, samples_dev, max_blocks, line_lo, line_hi,
+                                (cudaStream_t)stream),
                    "batch run");
     return QSL_OK;
 }
 
 int qsl_batch_run(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
                   qsl_stream_t stream) {
-    return qsl_batch_run_capped(table_dev, info_h, samples_dev, 0, stream);
+    return qsl_batch_run_window(table_dev, info_h, samples_dev, 0, -1, 0, stream);
 }
 
 int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream, qsl_batch_t** out) {
@@ -725,7 +726,7 @@ int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream
 
 int qsl_batch_launch(const qsl_batch_t* B, unsigned long long* samples_dev, qsl_stream_t stream) {
     if (!B) return fail(QSL_ERR_INVALID, "batch is null");
-    QSL_CHECK_CUDA(launch_slots(B->jobs, B->begin, B->njobs, B->total, B->twist, samples_dev, 0,
+    QSL_CHECK_CUDA(launch_slots(B->jobs, B->begin, B->njobs, B->total, B->twist, samples_dev, 0, 0, -1,
                                 (cudaStream_t)stream),
                    "batch launch");
     return QSL_OK;

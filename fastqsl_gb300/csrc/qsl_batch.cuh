@@ -61,16 +61,20 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
 }
 
 // begin[j]: first line of job j (multiples of 32, increasing); begin[njobs]:
-// the total.  Each job's TraceJob sits in device memory.
+// the total.  Each job's TraceJob sits in device memory.  Only the lines of
+// the window [line_lo, line_hi) run (a multiple of 32 for line_lo keeps every
+// warp inside one job).
 template <bool TWIST, class F>
 __device__ __forceinline__ void batch_kernel_body(const TraceJob<F>* __restrict__ jobs,
                                                   const long long* __restrict__ begin, int njobs,
-                                                  unsigned long long* samples) {
-    const long long total = __ldg(begin + njobs);
+                                                  unsigned long long* samples, long long line_lo,
+                                                  long long line_hi) {
+    long long total = __ldg(begin + njobs);
+    total = line_hi < total ? line_hi : total;
     const long long stride = (long long)gridDim.x * blockDim.x;
     unsigned ns = 0;
     unsigned long long ns_total = 0;
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += stride) {
+    for (long long g = line_lo + (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += stride) {
         int lo = 0, hi = njobs - 1;  // last j with begin[j] <= g
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;

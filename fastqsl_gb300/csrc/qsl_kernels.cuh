@@ -76,19 +76,24 @@ static cudaError_t launch_scott(const ScottJob<F>& J, int grad, bool twist, long
 template <bool TWIST, class F>
 __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_batch(const TraceJob<F>* __restrict__ jobs,
                                                                  const long long* __restrict__ begin, int njobs,
-                                                                 unsigned long long* samples) {
-    batch_kernel_body<TWIST>(jobs, begin, njobs, samples);
+                                                                 unsigned long long* samples, long long line_lo,
+                                                                 long long line_hi) {
+    batch_kernel_body<TWIST>(jobs, begin, njobs, samples, line_lo, line_hi);
 }
 
 template <class F>
 static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin, int njobs, long long total,
-                                bool twist, unsigned long long* samples, int max_blocks, cudaStream_t st) {
+                                bool twist, unsigned long long* samples, int max_blocks, long long line_lo,
+                                long long line_hi, cudaStream_t st) {
     if (njobs <= 0 || total <= 0) return cudaSuccess;
-    long long g = (total + kTraceBlock - 1) / kTraceBlock;
+    if (line_lo < 0) line_lo = 0;
+    if (line_hi < 0 || line_hi > total) line_hi = total;
+    if (line_lo >= line_hi) return cudaSuccess;
+    long long g = (line_hi - line_lo + kTraceBlock - 1) / kTraceBlock;
     if (max_blocks > 0 && g > max_blocks) g = max_blocks;  // the grid-stride loop covers the rest
     const int grid = (int)(g > (1 << 30) ? (1 << 30) : g);
-    if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
-    else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples);
+    if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
+    else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
     return cudaGetLastError();
 }
 

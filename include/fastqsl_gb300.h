@@ -243,13 +243,15 @@ typedef struct qsl_batch_info {
 } qsl_batch_info;
 int qsl_batch_pack(const qsl_batch_job *jobs_h, int njobs, void *table_h, int64_t table_bytes,
                    qsl_batch_info *info_h);
-/* qsl_batch_run with at most max_blocks resident 128-thread blocks per launch
- * (0 = no limit; the blocks then loop over the lines).  A serving loop caps
- * large batches below the GPU's resident capacity (e.g. 6 of 8 blocks per SM)
- * so that the blocks of small requests on higher-priority streams find free
- * slots at once instead of waiting for a large batch's blocks to retire. */
-int qsl_batch_run_capped(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
-                         int max_blocks, qsl_stream_t stream);
+/* qsl_batch_run over the lines [line_lo, line_hi) of each store type's line
+ * space (line_hi < 0: to the end; line_lo a multiple of 32 keeps each warp
+ * inside one job) with at most max_blocks resident 128-thread blocks per
+ * launch (0 = no limit; the blocks then loop over the lines).  A serving loop
+ * runs a large batch as a sequence of such windows, so that small requests
+ * never share the GPU with more than a window of it, and caps its resident
+ * blocks below the GPU's capacity. */
+int qsl_batch_run_window(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
+                         int64_t line_lo, int64_t line_hi, int max_blocks, qsl_stream_t stream);
 int qsl_batch_run(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
                   qsl_stream_t stream);
 
