@@ -474,8 +474,9 @@ class BatchPlan:
                    "qsl_batch_run")
 
     @property
-    def lines(self):
-        """Length of the longest store type's line space (padded per job)."""
+    def window_lines(self):
+        """Length of the longest store type's line space (padded per job): the
+        end of the last window of launch(lo, hi)."""
         return max(int(self.info.total[k]) for k in range(4))
 
 
@@ -533,7 +534,7 @@ class QBatch:
 
     @property
     def main_lines(self):
-        return self.main_batch.lines
+        return self.main_batch.window_lines
 
     def run(self, stream=None):
         self.run_main(stream)

@@ -17,7 +17,13 @@ sub-box) and an RKF45 tolerance.  The scheduler loop:
   streams: their blocks are dispatched ahead of a large batch's remaining
   blocks, and larger classes keep at most `big_blocks_per_sm` of the 8
   resident block slots per SM, so a small request finds free slots at once
-  instead of waiting for a large batch's blocks to retire.
+  instead of waiting for a large batch's blocks to retire;
+* runs the main trace of larger classes' batches as windows of
+  `chunk_lines` lines (qsl_batch_run_window), at most `max_chunks` windows
+  on the device at a time and `chunks_when_interactive` while a batch of the
+  smallest class is in flight, so a small request shares the GPU with at
+  most that many windows of bulk work, not with whole bulk batches; the
+  batch's Q assembly runs after its last window.
 
 Nothing in the loop synchronises the device: allocations come from the
 caching allocator on the batch's stream, the job table is copied
@@ -109,10 +115,21 @@ def seeds_on_device(req: QRequest, device):
 
 
 class _Flight:
-    """One launched batch: its requests, buffers, pinned results, event."""
+    """One admitted batch: its requests, buffers, stream, pinned results and
+    completion event (None until the post-trace steps are queued); a chunked
+    batch also keeps the next window's first line and its windows' events."""
 
-    def __init__(self, reqs, qb, hosts, event, nbytes):
-        self.reqs, self.qb, self.hosts, self.event, self.nbytes = reqs, qb, hosts, event, nbytes
+    def __init__(self, reqs, qb, cls, stream, nbytes):
+        self.reqs, self.qb, self.cls, self.stream, self.nbytes = reqs, qb, cls, stream, nbytes
+        self.hosts, self.event = [], None
+        self.next_lo, self.lines, self.nwin = 0, 0, 0
+        self.ready = None          # recorded on `stream` once the batch's tables are queued
+        self.windows = []          # events of windows not yet seen complete
+        self.last = {}             # window stream index -> event of this batch's last window there
+
+    def windows_in_flight(self):
+        self.windows = [e for e in self.windows if not e.query()]
+        return len(self.windows)
 
 
 class QServer:
@@ -127,7 +144,8 @@ class QServer:
     CLASSES = ((1.5e5, 32, 2), (1.2e6, 8, 2), (float("inf"), 2, 2))
 
     def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
-                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6):
+                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=4,
+                 chunks_when_interactive=1, window_streams=2, window_blocks_per_sm=0):
         self.fields = dict(fields)
         self.budget = int(hbm_budget)
         self.used = 0
@@ -149,6 +167,17 @@ class QServer:
         # the 8 resident block slots per SM, so the smallest requests' blocks
         # (on the highest-priority stream) start at once (0 = no cap)
         self.big_blocks_per_sm = int(big_blocks_per_sm)
+        # main traces of classes > 0 run as windows of chunk_lines lines (a
+        # multiple of 32; 0 = one launch per batch)
+        self.chunk_lines = (int(chunk_lines) + 31) // 32 * 32
+        self.max_chunks, self.chunks_when_interactive = int(max_chunks), int(chunks_when_interactive)
+        # windows of one batch alternate over these streams (per class, at the
+        # class's priority), so one window's tail overlaps the next window;
+        # their blocks are capped at window_blocks_per_sm per SM (0 = none:
+        # one line per thread, blocks retire as they finish)
+        self.window_streams = [[torch.cuda.Stream(device=self.device, priority=prios[c])
+                                for _ in range(max(1, int(window_streams)))] for c in range(len(self.classes))]
+        self.window_blocks_per_sm = int(window_blocks_per_sm)
         self.pending = [collections.deque() for _ in self.classes]
         self.flights = []
         self.done = []
@@ -190,13 +219,59 @@ class QServer:
             if group:
                 self._launch(group, nbytes, c)
                 progressed = True
+        return self._feed() or progressed
+
+    def _feed(self):
+        """Queues main-trace windows of chunked batches, smallest class and
+        oldest batch first, while fewer than the allowed number are on the
+        device; a batch whose last window is queued gets its post steps."""
+        chunked = [fl for fl in self.flights if fl.event is None]
+        if not chunked:
+            return False
+        interactive = any(fl.cls == 0 for fl in self.flights)
+        allowed = self.chunks_when_interactive if interactive else self.max_chunks
+        busy = sum(fl.windows_in_flight() for fl in chunked)
+        progressed = False
+        for fl in sorted(chunked, key=lambda f: f.cls):
+            wss = self.window_streams[fl.cls]
+            while busy < allowed and fl.next_lo < fl.lines:
+                hi = min(fl.lines, fl.next_lo + self.chunk_lines)
+                k = fl.nwin % len(wss)
+                ws = wss[k]
+                ws.wait_event(fl.ready)
+                with torch.cuda.stream(ws):
+                    fl.qb.run_main(stream=ws, lo=fl.next_lo, hi=hi)
+                    ev = torch.cuda.Event()
+                    ev.record(ws)
+                fl.windows.append(ev)
+                fl.last[k] = ev
+                fl.next_lo, fl.nwin = hi, fl.nwin + 1
+                busy += 1
+                progressed = True
+            if fl.next_lo >= fl.lines:
+                self._post(fl)
+                progressed = True
         return progressed
+
+    def _post(self, fl):
+        """Queues the batch's post-trace steps, the D2H copies of its Q maps
+        and its completion event on its stream, after its last windows."""
+        for ev in fl.last.values():
+            fl.stream.wait_event(ev)
+        with torch.cuda.stream(fl.stream):
+            qs = fl.qb.run_post(stream=fl.stream)
+            for q in qs:
+                h = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
+                h.copy_(q, non_blocking=True)
+                fl.hosts.append(h)
+            fl.event = torch.cuda.Event()
+            fl.event.record(fl.stream)
 
     def _retire(self):
         progressed = False
         keep = []
         for fl in self.flights:
-            if fl.event.query():
+            if fl.event is not None and fl.event.query():
                 t = time.perf_counter()
                 for r, h in zip(fl.reqs, fl.hosts):
                     r.t_done = t
@@ -221,21 +296,21 @@ class QServer:
                 prm = absolute_rkf45(tol=r.tol, h_min=self.h_min, h_max=self.h_max)
                 specs.append(dict(field=self.fields[r.field], xs=xs, ys=ys, zs=zs, n0=r.n0, n1=r.n1,
                                   nplanes=r.nplanes, params=prm, s_len=self.s_len, stride=r.spacing, cross_dir=nrm))
-            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st,
-                            blocks_per_sm=self.big_blocks_per_sm if cls > 0 else 0)
-            qs = qb.run(stream=st)
-            hosts = []
-            for q in qs:
-                h = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
-                h.copy_(q, non_blocking=True)
-                hosts.append(h)
-            ev = torch.cuda.Event()
-            ev.record(st)
+            windowed = cls > 0 and self.chunk_lines > 0
+            cap = self.window_blocks_per_sm if windowed else self.big_blocks_per_sm if cls > 0 else 0
+            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st, blocks_per_sm=cap)
         self.used += nbytes
         self.batches += 1
-        fl = _Flight(group, qb, hosts, ev, nbytes)
-        fl.cls = cls
+        fl = _Flight(group, qb, cls, st, nbytes)
         self.flights.append(fl)
+        if windowed:
+            fl.lines = qb.main_lines          # windows queued by _feed
+            fl.ready = torch.cuda.Event()
+            fl.ready.record(st)
+        else:
+            with torch.cuda.stream(st):
+                qb.run_main(stream=st)
+            self._post(fl)
 
     def idle(self):
         return not any(self.pending) and not self.flights

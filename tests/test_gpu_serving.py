@@ -50,3 +50,24 @@ def test_budget_admission_and_poisson_stream(cuda):
     big = serving.QRequest(rid=99, field="f0", n0=400, n1=400)
     with pytest.raises(MemoryError):
         srv.submit(big)
+
+
+def test_windowed_bulk_equals_whole(cuda):
+    """Larger classes' main traces run as windows of a few lines (forced
+    small here, with a window limit of 1 while small batches fly): every
+    result equals the one-launch server's bit for bit."""
+    from fastqsl_gb300 import serving
+    fields = serving.make_fields(n_fields=3, shape=(48, 44, 40), seed=3)
+    classes = ((600, 4, 2), (1500, 4, 2), (float("inf"), 2, 2))
+    whole = serving.QServer(fields, streams=2, classes=classes, chunk_lines=0)
+    win = serving.QServer(fields, streams=2, classes=classes, chunk_lines=96, max_chunks=2,
+                          chunks_when_interactive=1)
+    assert win.chunk_lines == 96
+    reqs = serving.make_requests((48, 44, 40), sorted(fields), 12, 300.0, seed=11, seeds_range=(200, 4000))
+    assert len({next(c for c, (ub, _, _) in enumerate(classes) if r.seeds <= ub) for r in reqs}) == 3
+    ref = {r.rid: r.result for r in whole.run_stream(reqs)}
+    reqs2 = serving.make_requests((48, 44, 40), sorted(fields), 12, 300.0, seed=11, seeds_range=(200, 4000))
+    done = win.run_stream(reqs2)
+    assert len(done) == 12 and win.idle() and win.used == 0
+    for r in done:
+        _same(r.result, ref[r.rid])
