@@ -351,14 +351,17 @@ def batched_graph(device, n_fields=64, seed=11, reps=3):
     return out
 
 
-def serving_sweep(device, count=48):
+def serving_sweep(device, count=96):
     """8 resident 384x384x256 fields; Poisson streams of Q-map requests
-    (10^4-4x10^6 seeds, tol 1e-3/1e-4/1e-5) at fractions of the saturated
-    rate; p50/p99 latency against each request's isolated solve."""
+    (10^4-4x10^6 seeds, tol 1e-3/1e-4/1e-5) at fractions of the batched
+    (whole-batch launches, all requests at once) saturated rate, served with
+    windowed bulk traces; p50/p99 latency against each request's isolated
+    solve."""
     from fastqsl_gb300 import serving
     fields = serving.make_fields(n_fields=8, shape=(384, 384, 256), device=device)
     srv = serving.QServer(fields, hbm_budget=48 << 30, streams=3, max_batch=16)
-    out = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8))
+    whole = serving.QServer(fields, hbm_budget=48 << 30, streams=3, max_batch=16, chunk_lines=0)
+    out = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8), batched_server=whole)
     for fs in fields.values():
         fs.close()
     return out

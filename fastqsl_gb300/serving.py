@@ -413,19 +413,32 @@ def make_requests(fields_shape, names, count, rate, seed=0, seeds_range=(1e4, 4e
     return out
 
 
-def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6)):
+def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6),
+          batched_server: QServer | None = None):
     """Isolated solve of every request, the saturated throughput (all
     requests at once), then Poisson streams at fractions of the saturated
-    request rate.  Returns a dict of latency_stats per point."""
+    request rate.  With `batched_server` (e.g. one launching whole batches,
+    chunk_lines=0) the saturated rate the fractions refer to is that
+    server's, and `server`'s own saturated throughput is reported beside it.
+    Returns a dict of latency_stats per point."""
     names = sorted(server.fields)
     burst = make_requests(fields_shape, names, count, None, seed=seed, seeds_range=seeds_range)
     iso = {r.rid: solve_alone(server, r)[0] for r in burst}
-    done = server.run_stream(burst)
+    done = (batched_server or server).run_stream(burst)
     sat = latency_stats(done, iso)
     span = max(r.t_done for r in done) - min(r.t_submit for r in done)
     sat_rate = count / span
     res = {"saturated": sat, "isolated_p50_s": float(np.median(list(iso.values())))}
+    if batched_server is not None:
+        own = make_requests(fields_shape, names, count, None, seed=seed, seeds_range=seeds_range)
+        res["saturated_this_server"] = latency_stats(server.run_stream(own), iso)
     for f in fractions:
         reqs = make_requests(fields_shape, names, count, f * sat_rate, seed=seed, seeds_range=seeds_range)
-        res[f"rate_{f:.2f}"] = dict(latency_stats(server.run_stream(reqs), iso), offered_req_per_s=f * sat_rate)
+        done = server.run_stream(reqs)
+        st = dict(latency_stats(done, iso), offered_req_per_s=f * sat_rate)
+        for c in range(len(server.classes)):
+            rr = [r.latency / iso[r.rid] for r in done if r.meta["class"] == c]
+            if rr:
+                st[f"class{c}_p50_p90_over_isolated"] = [float(np.percentile(rr, 50)), float(np.percentile(rr, 90))]
+        res[f"rate_{f:.2f}"] = st
     return res
