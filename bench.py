@@ -214,26 +214,31 @@ def run_ours(args, rank, world):
         hb = [torch.empty(b.shape[::-1], dtype=torch.float32).pin_memory() for b in (bx, by, bz)]
         for h, b in zip(hb, (bx, by, bz)):
             h.copy_(b.permute(2, 1, 0))
-        dbuf = [torch.empty(b.shape[::-1], dtype=torch.float32, device=dev) for b in (bx, by, bz)]
+        up = api.FieldUploader(tuple(bx.shape), device=dev)
         qh = torch.empty(Q.shape, dtype=Q.dtype).pin_memory()
 
-        def e2e_step():
-            for d, h in zip(dbuf, hb):
-                d.copy_(h, non_blocking=True)
-            store.update(*[d.permute(2, 1, 0) for d in dbuf])
-            q = plan.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0)
-            qh.copy_(q, non_blocking=True)
+        def e2e_run(n):
+            # each step: H2D of its field (the next step's copy is queued
+            # before this step's trace, so it overlaps it), pack, Q, D2H of Q
+            slot = up.upload(*hb)
+            for k in range(n):
+                up.pack(store, slot, stream)
+                if k + 1 < n:
+                    slot = up.upload(*hb)
+                q = plan.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0)
+                qh.copy_(q, non_blocking=True)
 
-        e2e_step()
+        e2e_run(2)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = max(1, min(3, args.steps))
+        reps = max(1, min(8, args.steps))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         e0.record(stream)
-        for _ in range(reps):
-            e2e_step()
+        e2e_run(reps)
         e1.record(stream)
         torch.cuda.synchronize()
-        res["e2e_ms"] = e0.elapsed_time(e1) / reps
+        res["e2e_ms"] = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3) / reps
         res["h2d"] = int(sum(h.numel() * 4 for h in hb))
         res["d2h"] = int(qh.numel() * qh.element_size())
 

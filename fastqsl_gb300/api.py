@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -119,6 +120,63 @@ class FieldStore:
             self.close()
         except Exception:
             pass
+
+
+class FieldUploader:
+    """Double-buffered upload of host fields into a FieldStore: upload() puts
+    the H2D copy of a field (pinned host arrays) on its own copy stream into
+    one of `slots` device staging buffers, pack() makes the store's stream
+    wait for that copy and refills the store from it.  Uploading field k+1
+    before running field k's trace overlaps the copy with the trace; a slot
+    is reused only after everything queued on the store's stream up to the
+    following pack() (the pack, and the trace that read the field) is done.
+    """
+
+    def __init__(self, shape, device="cuda", slots=2):
+        nx, ny, nz = (int(v) for v in shape)
+        self.shape = (nx, ny, nz)
+        self.device = torch.device(device)
+        self.bufs = [[torch.empty((nz, ny, nx), dtype=torch.float32, device=self.device) for _ in range(3)]
+                     for _ in range(max(2, int(slots)))]
+        self.ready = [torch.cuda.Event() for _ in self.bufs]
+        self.free = [None] * len(self.bufs)
+        self.copy_stream = torch.cuda.Stream(device=self.device)
+        self._next, self._last = 0, None
+
+    def upload(self, Bx, By, Bz):
+        """Queues the copy of one field (torch CPU tensors shaped (nz, ny, nx),
+        contiguous, pinned for an asynchronous copy; or x-fastest arrays
+        shaped (nx, ny, nz)); returns the slot to pass to pack()."""
+        host = []
+        for b in (Bx, By, Bz):
+            t = b if isinstance(b, torch.Tensor) else torch.from_numpy(np.asarray(b))
+            if tuple(t.shape) == self.shape and t.dim() == 3 and t.stride(0) == 1:
+                t = t.permute(2, 1, 0)
+            if tuple(t.shape) != self.shape[::-1] or not t.is_contiguous() or t.dtype != torch.float32:
+                raise ValueError("each component must be float32, x fastest, of the uploader's shape")
+            host.append(t)
+        s = self._next
+        self._next = (s + 1) % len(self.bufs)
+        if self.free[s] is not None:
+            self.copy_stream.wait_event(self.free[s])
+        with torch.cuda.stream(self.copy_stream):
+            for d, h in zip(self.bufs[s], host):
+                d.copy_(h, non_blocking=True)
+            self.ready[s].record(self.copy_stream)
+        return s
+
+    def pack(self, store: "FieldStore", slot, stream=None):
+        """Refills `store` from an uploaded slot on `stream` (default: the
+        current stream) once its copy has landed."""
+        st = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.current_stream(self.device)
+        if self._last is not None:
+            ev = torch.cuda.Event()
+            ev.record(st)
+            self.free[self._last] = ev
+        st.wait_event(self.ready[slot])
+        with torch.cuda.stream(st):
+            store.update(*[d.permute(2, 1, 0) for d in self.bufs[slot]], stream=st)
+        self._last = slot
 
 
 def alloc_trace_outputs(n, device="cuda", twist=False):

@@ -159,3 +159,44 @@ def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     # its stated tail on this steep small field is within 5e-2
     p99_bar = 5e-2 if layout in ("h4b", "h8c") else 1e-2
     assert np.median(d) <= 1e-3 and np.quantile(d, 0.99) <= p99_bar, (np.median(d), np.quantile(d, 0.99))
+
+
+@pytest.mark.parametrize("layout", ["h4b", "soa"])
+def test_field_uploader_pipeline(cuda, layout):
+    """Fields uploaded from pinned host memory through FieldUploader, the next
+    field's copy queued before the current field's Q map: every Q map equals
+    the one from a store built directly from that field, bit for bit."""
+    from fastqsl_gb300 import api, synthetic as S
+    shape = (56, 48, 40)
+    fields = [S.make_field(S.charges_random(30 + k, shape, 4 + k)) for k in range(3)]
+    n0, n1 = 24, 28
+    xs, ys, zz = api.plane_seed_grid(3.0, 3.0 + 1.5 * (n1 - 1), n1, 3.0, 3.0 + 1.5 * (n0 - 1), n0, [0.0, 5.0])
+    prm = P.absolute_rkf45()
+    plan = api.QMapPlan(n0, n1, 2)
+    ref = []
+    for B in fields:
+        fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout=layout)
+        ref.append(plan.run(fs, xs, ys, zz, prm, s_len=0.25, stride=1.5).cpu().numpy())
+        fs.close()
+    hosts = [[torch.from_numpy(np.ascontiguousarray(b.transpose(2, 1, 0))).pin_memory() for b in B] for B in fields]
+    up = api.FieldUploader(shape)
+    store = api.FieldStore(*[torch.zeros(shape[::-1], device="cuda").permute(2, 1, 0) for _ in range(3)],
+                           layout=layout)
+    st = torch.cuda.current_stream()
+    outs = []
+    slot = up.upload(*hosts[0])
+    for k in range(len(fields)):
+        up.pack(store, slot, st)
+        if k + 1 < len(fields):
+            slot = up.upload(*hosts[k + 1])
+        q = plan.run(store, xs, ys, zz, prm, s_len=0.25, stride=1.5)
+        h = torch.empty(q.shape, dtype=q.dtype).pin_memory()
+        h.copy_(q, non_blocking=True)
+        outs.append(h)
+    torch.cuda.synchronize()
+    for a, b in zip(outs, ref):
+        a = a.numpy()
+        np.testing.assert_array_equal(np.isnan(a), np.isnan(b))
+        np.testing.assert_array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
+    with pytest.raises(ValueError):
+        up.upload(*[h[:-1] for h in hosts[0]])
