@@ -19,10 +19,10 @@ NVCC = os.environ.get("NVCC", os.path.join(os.environ.get("CUDA_HOME", "/usr/loc
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-NO_FMA = {"trace_exact.cu", "qassembly.cu", "curl.cu"}
+NO_FMA = {"trace_exact.cu", "qassembly.cu", "curl.cu", "path.cu"}
 SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast_soa.cu", "trace_fast_f4.cu", "trace_fast_h4b.cu",
            "trace_fast_h8c.cu", "trace_fast_stretch.cu", "field_store.cu", "qassembly.cu", "hybrid.cu", "curl.cu",
-           "noalloc.cu"]
+           "path.cu", "noalloc.cu"]
 
 
 def _deps():

@@ -87,6 +87,9 @@ _SIGS = {
     "qsl_params_reference_stretch": (None, [_P]),
     "qsl_hybrid_select": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P, _P]),
     "qsl_curl_grid": (c_int, [_P, _P, _P, c_int, c_int, c_int] + [_P] * 7),
+    "qsl_trace_path": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, c_i64, c_i64, c_i64, c_i64, c_double,
+                               _P, _P, _P, c_i64, _P]),
+    "qsl_sample_points": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, c_i64, c_int, _P, _P]),
     "qsl_hybrid_merge": (c_int, [_P, _P, c_int, c_int, c_i64, _P, _P]),
     "qsl_trace_all_bline_stretch": (c_int, [c_int] + [_P] * 39 + [c_i64, _P]),
     "qsl_trace_stretch": (c_int, [_P, _P, _P, c_int, c_int, c_int, _P, _P, _P, c_int, _P, _P, c_i64, c_float,

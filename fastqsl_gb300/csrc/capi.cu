@@ -988,6 +988,44 @@ int qsl_curl_grid(const float* Bx, const float* By, const float* Bz, int nx, int
     return QSL_OK;
 }
 
+int qsl_trace_path(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz, const double* seeds,
+                   int64_t n, int64_t start, int64_t stop, int64_t stride, double dr, float* out_x, float* out_y,
+                   float* out_z, int64_t out_len, qsl_stream_t stream) {
+    if (n < 0 || out_len < 0) return fail(QSL_ERR_INVALID, "negative count");
+    if (n == 0) return QSL_OK;
+    if (!Bx || !By || !Bz || !seeds || !out_x || !out_y || !out_z) return fail(QSL_ERR_INVALID, "null argument");
+    if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
+    if (stride == 0) return fail(QSL_ERR_INVALID, "index stride must not be zero");
+    if (n > (int64_t)1 << 36) return fail(QSL_ERR_TOO_LARGE, "too many seeds");
+    // every index the range visits lies in [0, out_len)
+    const bool empty = stride > 0 ? start >= stop : start <= stop;
+    if (!empty) {
+        const int64_t last = stride > 0 ? start + (stop - 1 - start) / stride * stride
+                                        : start - (start - stop - 1) / (-stride) * (-stride);
+        const int64_t lo = start < last ? start : last, hi = start < last ? last : start;
+        if (lo < 0 || hi >= out_len)
+            return fail(QSL_ERR_INVALID, "index range [%lld, %lld] outside the output rows of %lld", (long long)lo,
+                        (long long)hi, (long long)out_len);
+    }
+    if (empty) return QSL_OK;
+    QSL_CHECK_CUDA(launch_trace_path(Bx, By, Bz, nx, ny, nz, seeds, n, start, stop, stride, dr, out_x, out_y, out_z,
+                                     out_len, (cudaStream_t)stream),
+                   "trace path");
+    return QSL_OK;
+}
+
+int qsl_sample_points(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz, const double* pts,
+                      int64_t n, int normalize, double* out, qsl_stream_t stream) {
+    if (n < 0) return fail(QSL_ERR_INVALID, "negative count");
+    if (n == 0) return QSL_OK;
+    if (!Bx || !By || !Bz || !pts || !out) return fail(QSL_ERR_INVALID, "null argument");
+    if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
+    if (n > (int64_t)1 << 37) return fail(QSL_ERR_TOO_LARGE, "too many points");
+    QSL_CHECK_CUDA(launch_sample_points(Bx, By, Bz, nx, ny, nz, pts, n, normalize, out, (cudaStream_t)stream),
+                   "sample points");
+    return QSL_OK;
+}
+
 int qsl_hybrid_select(const int* B_flag, const double* Q, int n0, int n1, int64_t nplanes, unsigned* seeds,
                       unsigned long long* count_dev, qsl_stream_t stream) {
     if (!B_flag || !Q || !seeds || !count_dev) return fail(QSL_ERR_INVALID, "null argument");

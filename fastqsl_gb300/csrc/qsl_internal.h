@@ -66,6 +66,13 @@ cudaError_t launch_trace_batch_h8c(const TraceJob<FieldH8C>* jobs, const long lo
 cudaError_t launch_curl(const float* bx, const float* by, const float* bz, const float* ax, const float* ay,
                         const float* az, int nx, int ny, int nz, double* cx, double* cy, double* cz, cudaStream_t st);
 
+// path.cu (compiled with -fmad=false)
+cudaError_t launch_trace_path(const float* bx, const float* by, const float* bz, int nx, int ny, int nz,
+                              const double* seeds, long long n, long long start, long long stop, long long stride,
+                              double dr, float* ox, float* oy, float* oz, long long out_len, cudaStream_t st);
+cudaError_t launch_sample_points(const float* bx, const float* by, const float* bz, int nx, int ny, int nz,
+                                 const double* pts, long long n, int normalize, double* out, cudaStream_t st);
+
 // hybrid.cu
 cudaError_t launch_hybrid_select(const int* bflag, const double* q, long long n0, long long n1, long long nplanes,
                                  unsigned* seeds, unsigned long long* count, cudaStream_t st);

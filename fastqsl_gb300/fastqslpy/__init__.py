@@ -6,11 +6,11 @@
     TraceAllBline(blck, grd, (Bx_gpu, By_gpu, ...))   # same 35 arguments
     Q = fastqslpy.FastQSL.QCalcPlane(...)
 
-``kernels`` and ``FastQSL`` keep the reference's entry points and argument
-lists; arrays may be PyTorch CUDA tensors or CuPy arrays.  The reference's
-``MagTool`` (a NumPy toy tracer that nothing in the package calls) is not
-part of the GPU path and is not provided.
+``kernels``, ``FastQSL`` and ``MagTool`` keep the reference's entry points
+and argument lists; arrays may be PyTorch CUDA tensors or CuPy arrays
+(``MagTool`` also takes the NumPy arrays its reference takes and returns
+NumPy arrays, as there).
 """
-from . import FastQSL, kernels
+from . import FastQSL, MagTool, kernels
 
-__all__ = ["kernels", "FastQSL"]
+__all__ = ["kernels", "FastQSL", "MagTool"]

@@ -333,6 +333,29 @@ int qsl_curl_grid(const float *Bx, const float *By, const float *Bz, int nx, int
                   qsl_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Field-line polylines — fastqslpy/MagTool.py (trilerp :3-18, Bnorm :20-22,
+ * RK4_bline :24-34, TraceBline :36-45)
+ * ------------------------------------------------------------------------ */
+
+/* RK4_bline for n seeds at once (seeds: device float64, n x 3): from each
+ * seed, fixed steps of dr along the unit field (float64 arithmetic in that
+ * function's order), storing the point reached before each step as float32
+ * at out_*[s * out_len + idx] for idx = start, start + stride, ... (Python
+ * range(start, stop, stride)), until a coordinate leaves [0, nx].  Entries
+ * not visited are left as they are (TraceBline's arrays start as NaN; it
+ * runs range(maxstep/2, maxstep, 1) with dr = 0.25, then
+ * range(maxstep/2, 0, -1) with dr = -0.25).  Every visited index must lie in
+ * [0, out_len). */
+int qsl_trace_path(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz, const double *seeds,
+                   int64_t n, int64_t start, int64_t stop, int64_t stride, double dr, float *out_x, float *out_y,
+                   float *out_z, int64_t out_len, qsl_stream_t stream);
+
+/* trilerp (normalize = 0) or Bnorm (normalize = 1) at n points (device
+ * float64, n x 3) with MagTool's clamping; out: device float64, n x 3. */
+int qsl_sample_points(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz, const double *pts,
+                      int64_t n, int normalize, double *out, qsl_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Hybrid finite-difference + Scott Q — demo/Q_RKF45MixCuPyDiffScott.ipynb cell 9
  * ------------------------------------------------------------------------ */
 

@@ -13,7 +13,9 @@ What runs:
 * Q assembly — the reference's own fastqslpy/FastQSL.py (QCalcPlane,
   CookPseudoLine, ResReshape) imported with NumPy standing in for CuPy, and
   the pseudo-line Q cells of demo/Q_RKF45CuPy.ipynb (cells 9-11) executed
-  from the notebook file with the same substitution.
+  from the notebook file with the same substitution;
+* field-line polylines — the reference's own fastqslpy/MagTool.py, with the
+  np.int alias it needs restored (``make_golden.py magtool`` alone).
 
 Inputs are the seeded synthetic fields of fastqsl_gb300.synthetic (the
 reference's demo fields are not distributed); each fixture stores the field
@@ -201,7 +203,48 @@ def qmap_case():
          Qcut=ns["Qcut"], Q_all=ns["Q_all"], Q_final=ns["Q_final"])
 
 
+def reference_magtool():
+    """Imports the reference's fastqslpy/MagTool.py.  It calls np.int, which
+    NumPy 1.24 removed; the builtin int it aliased is put back first."""
+    if not hasattr(np, "int"):
+        np.int = int
+    spec = importlib.util.spec_from_file_location("ref_MagTool", os.path.join(REF, "fastqslpy", "MagTool.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+MAGTOOL_SHAPE = (40, 32, 24)
+
+
+def magtool_case():
+    """fastqslpy/MagTool.py: TraceBline polylines (maxstep 800) from float32
+    seeds on a 40 x 32 x 24 field (lines that rise above z = 24 run on along
+    the clamped top plane until z > 40, the first axis length), and trilerp /
+    Bnorm at float64 points inside, on and outside the box."""
+    mt = reference_magtool()
+    spec = S.charges_random(5, MAGTOOL_SHAPE, 5, depth=(2.0, 6.0))
+    Bx, By, Bz = S.make_field(spec)
+    rng = np.random.default_rng(17)
+    seeds = np.stack([rng.uniform(2, 37, 7), rng.uniform(2, 29, 7), rng.uniform(0.5, 20, 7)], 1).astype(np.float32)
+    seeds = np.concatenate([seeds, np.array([[39.6, 31.4, 23.7], [0.0, 0.0, 0.0]], np.float32)])
+    lines = []
+    for p in seeds:
+        lx, ly, lz = mt.TraceBline(Bx, By, Bz, p.copy(), dr=0.25, maxstep=800)
+        lines.append(np.stack([lx, ly, lz]))
+    pts = np.concatenate([rng.uniform(-2, 42, (40, 3)),
+                          np.array([[39.5, 31.5, 23.5], [40.0 - 1e-9, 0.3, 0.2], [-0.1, 31.99, 23.999],
+                                    [12.0, 7.0, 3.0], [38.0, 30.5, 22.5]])])
+    tri = np.stack([mt.trilerp(Bx, By, Bz, p.copy()) for p in pts])
+    bn = np.stack([mt.Bnorm(Bx, By, Bz, p.copy()) for p in pts])
+    save("magtool_charges5.npz", seed=np.int64(5), shape=np.array(MAGTOOL_SHAPE), seeds=seeds,
+         lines=np.stack(lines), pts=pts, trilerp=tri, bnorm=bn,
+         fingerprint=np.array([float(np.sum(Bx, dtype=np.float64)), float(np.sum(Bz, dtype=np.float64))]))
+
+
 def main():
+    if sys.argv[1:] == ["magtool"]:
+        return magtool_case()
     if not oracle.ref_available("rkf45"):
         raise SystemExit("oracle/_ref not built: run python oracle/build.py in a checkout with the reference")
     if sys.argv[1:] == ["stretch"]:  # only the stretched-grid fixtures
@@ -219,6 +262,7 @@ def main():
     qmap_case()
     stretch_cases()
     curl_case()
+    magtool_case()
 
 
 def stretch_cases():

@@ -57,3 +57,14 @@ def limit_mask(g):
     """Seeds whose both directions left the box (flag != 0); the reference's
     footpoint of a direction stopped by a limit is stale scratch memory."""
     return (g["flag_start"] != 0) & (g["flag_end"] != 0)
+
+
+def magtool_case(name="magtool_charges5.npz"):
+    """The MagTool fixture and its field (charges_random(seed, shape, 5,
+    depth 2-6), float32 (nx, ny, nz) Fortran order); checks the fingerprint."""
+    g = np.load(os.path.join(GOLDEN, name))
+    spec = S.charges_random(int(g["seed"]), tuple(int(v) for v in g["shape"]), 5, depth=(2.0, 6.0))
+    B = S.make_field(spec)
+    fp = [float(np.sum(B[0], dtype=np.float64)), float(np.sum(B[2], dtype=np.float64))]
+    assert np.allclose(fp, g["fingerprint"], rtol=0, atol=1e-9 * max(1.0, abs(fp[0]))), "field generator changed"
+    return g, B
