@@ -95,7 +95,7 @@ struct qsl_field {
     Dims d;
     const float *bx, *by, *bz;  // SOA only: the caller's arrays (borrowed)
     float4* f4;
-    uint2* bricks;
+    uint4* bricks;
     float* scale;
     uint4* cells;  // H8C records
     int nbx, nby, nbz;
@@ -115,7 +115,7 @@ static int64_t layout_bytes(int nx, int ny, int nz, int layout, int* nbx, int* n
         case LAYOUT_F4: return nodes * (int64_t)sizeof(float4);
         case LAYOUT_H4B: {
             const int64_t nb = (int64_t)bx * by * bz;
-            return nb * BRICK_U2 * (int64_t)sizeof(uint2) + nb * (int64_t)sizeof(float);
+            return nb * BRICK_U4 * (int64_t)sizeof(uint4) + nb * (int64_t)sizeof(float);
         }
         case LAYOUT_H8C: return (int64_t)bx * by * bz * 512 * CELL_RECORD_U4 * (int64_t)sizeof(uint4);
         default: return -1;
@@ -166,7 +166,7 @@ int qsl_field_create(const float* Bx, const float* By, const float* Bz, int nx, 
         if (e == cudaSuccess) e = launch_pack_f4(Bx, By, Bz, f->d, f->f4, st);
     } else if (layout == LAYOUT_H4B) {
         const int64_t nb = (int64_t)nbx * nby * nbz;
-        e = cudaMalloc(&f->bricks, (size_t)(nb * BRICK_U2 * sizeof(uint2)));
+        e = cudaMalloc(&f->bricks, (size_t)(nb * BRICK_U4 * sizeof(uint4)));
         if (e == cudaSuccess) e = cudaMalloc(&f->scale, (size_t)(nb * sizeof(float)));
         if (e == cudaSuccess) e = launch_pack_h4b(Bx, By, Bz, f->d, nbx, nby, nbz, f->bricks, f->scale, st);
     } else {

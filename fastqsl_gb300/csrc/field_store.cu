@@ -21,10 +21,11 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
 
 // One block per brick: the brick's 9^3 nodes (clamped to the grid at the far
 // faces) are scaled by the largest |component| in the brick and rounded to
-// fp16.  The scale is the brick's multiplier back to field units.
+// fp16, and written as x-pair records.  The scale is the brick's multiplier
+// back to field units.
 __global__ void __launch_bounds__(256) k_pack_h4b(const float* __restrict__ bx, const float* __restrict__ by,
                                                   const float* __restrict__ bz, Dims d, int nbx, int nby,
-                                                  uint2* __restrict__ bricks, float* __restrict__ scale) {
+                                                  uint4* __restrict__ bricks, float* __restrict__ scale) {
     const int brick = blockIdx.x;
     const int bi = brick % nbx, bj = (brick / nbx) % nby, bk = brick / (nbx * nby);
     const int64_t sy = d.nx, sz = (int64_t)d.nx * d.ny;
@@ -47,28 +48,27 @@ __global__ void __launch_bounds__(256) k_pack_h4b(const float* __restrict__ bx, 
     const float smax = red[0];
     const float sc = (smax > 0.f && isfinite(smax)) ? smax : 1.f;
     const float inv = 1.f / sc;
-    uint2* bp = bricks + (int64_t)brick * BRICK_U2;
-    for (int t = threadIdx.x; t < BRICK_U2; t += blockDim.x) {
-        if (t >= NN) {
-            bp[t] = make_uint2(0u, 0u);
-            continue;
+    uint4* bp = bricks + (int64_t)brick * BRICK_U4;
+    for (int t = threadIdx.x; t < BRICK_U4; t += blockDim.x) {
+        const int a = t & 7, row = t >> 3, b = row % BRICK_NODES, c = row / BRICK_NODES;
+        const int y = min(bj * BRICK_CELLS + b, d.ny - 1), z = min(bk * BRICK_CELLS + c, d.nz - 1);
+        unsigned w[4];
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+            const int x = min(bi * BRICK_CELLS + a + dx, d.nx - 1);
+            const int64_t o = x + sy * y + sz * z;
+            const __half2 xy = __floats2half2_rn(__ldg(bx + o) * inv, __ldg(by + o) * inv);
+            const __half hz = __float2half_rn(__ldg(bz + o) * inv);
+            w[2 * dx] = *reinterpret_cast<const unsigned*>(&xy);
+            w[2 * dx + 1] = (unsigned)__half_as_ushort(hz);
         }
-        const int a = t % BRICK_NODES, b = (t / BRICK_NODES) % BRICK_NODES, c = t / (BRICK_NODES * BRICK_NODES);
-        const int x = min(bi * BRICK_CELLS + a, d.nx - 1), y = min(bj * BRICK_CELLS + b, d.ny - 1),
-                  z = min(bk * BRICK_CELLS + c, d.nz - 1);
-        const int64_t o = x + sy * y + sz * z;
-        const __half2 xy = __floats2half2_rn(__ldg(bx + o) * inv, __ldg(by + o) * inv);
-        const __half hz = __float2half_rn(__ldg(bz + o) * inv);
-        uint2 u;
-        u.x = *reinterpret_cast<const unsigned*>(&xy);
-        u.y = (unsigned)__half_as_ushort(hz);
-        bp[t] = u;
+        bp[t] = make_uint4(w[0], w[1], w[2], w[3]);
     }
     if (threadIdx.x == 0) scale[brick] = sc;
 }
 
 cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
-                            uint2* bricks, float* scale, cudaStream_t st) {
+                            uint4* bricks, float* scale, cudaStream_t st) {
     const long long nb = (long long)nbx * nby * nbz;
     if (nb <= 0 || nb > 0x7fffffffLL) return cudaErrorInvalidValue;
     k_pack_h4b<<<(unsigned)nb, 256, 0, st>>>(bx, by, bz, d, nbx, nby, bricks, scale);
