@@ -1,8 +1,8 @@
 """Measured choice of the tracer's launch configuration.
 
 For a given field store, integrator settings and seed-plane geometry, the
-tuner times the main trace on a sample of the workload (the first few seed
-planes) for each candidate
+tuner times the main trace on a sample of the workload (a few seed planes
+spread evenly over the stack) for each candidate
 
 * seed tile — which seeds a warp's 32 lanes trace together (8x8 tiles give a
   warp a 8x4 patch; 16x16 a 16x2 strip; 4x8 a 4x8 patch),
@@ -32,13 +32,19 @@ def _key(field, params, n0, n1):
 def tune_trace(field, xs, ys, zs, params, n0, n1, nplanes, s_len=0.25, tol_coef=1.0, cross_dir=(0.0, 0.0, 1.0),
                sample_planes=4, reps=2, tiles=TILES, occupancies=OCCUPANCIES, use_cache=True):
     """Returns {'tile': (ty, tx), 'occupancy': k, 'ms': t, 'table': {...}}
-    for the fastest candidate on the first `sample_planes` planes."""
+    for the fastest candidate on `sample_planes` planes evenly spaced over
+    the stack (lines from the bottom and the middle of a cube differ in
+    length and spread)."""
     key = _key(field, params, n0, n1)
     if use_cache and key in _cache:
         return _cache[key]
     npl = max(1, min(nplanes, sample_planes))
     n = n0 * n1 * npl
-    sx, sy, sz = xs[:n], ys[:n], zs[:n]
+    per = n0 * n1
+    picks = sorted({round(k * (nplanes - 1) / max(1, npl - 1)) for k in range(npl)}) if npl > 1 else [0]
+    idx = torch.cat([torch.arange(k * per, (k + 1) * per, device=xs.device) for k in picks])
+    npl, n = len(picks), len(picks) * per
+    sx, sy, sz = xs[idx].contiguous(), ys[idx].contiguous(), zs[idx].contiguous()
     out = api.alloc_trace_outputs(n, xs.device)
     table = {}
     for tile in tiles:
