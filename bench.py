@@ -313,7 +313,7 @@ def cpu_baseline(planes, threads=None):
 
 def batched_graph(device, n_fields=64, seed=11, reps=3):
     """64 independent fields (4-32 charges; 64^3, 128^3, 192x192x128 or 256^3;
-    fp16 bricks or float32 SoA), each with an arbitrarily oriented cutting
+    fp16 bricks or float32 nodes, interleaved), each with an arbitrarily oriented cutting
     plane of 10^3-10^6 seeds (log-uniform), RK4 or RKF45; the whole Q pipeline
     of all 64 captured once into a CUDA graph and replayed."""
     import torch
@@ -325,7 +325,7 @@ def batched_graph(device, n_fields=64, seed=11, reps=3):
         shape = sizes[int(rng.integers(len(sizes)))]
         spec = S.charges_random(seed * 100 + k, shape, int(rng.integers(4, 33)))
         B = S.make_field(spec, device=device, as_numpy=False)
-        fs = api.FieldStore(*B, layout="h4b" if rng.random() < 0.5 else "soa")
+        fs = api.FieldStore(*B, layout="h4b" if rng.random() < 0.5 else "f4")
         stores.append(fs)
         total = float(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
         n0 = max(3, int(np.sqrt(total)))
