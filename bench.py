@@ -287,16 +287,26 @@ def accuracy_sample(bx, by, bz, Q, prm, ncells):
             "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None}
 
 
+_HOST_FIELD = []
+
+
+def host_field():
+    """The benchmark field on the host (generated once per process)."""
+    if not _HOST_FIELD:
+        import torch
+        (bx, by, bz), _ = make_field("cpu")
+        B = [b.numpy() if isinstance(b, torch.Tensor) else b for b in (bx, by, bz)]
+        _HOST_FIELD.extend(np.asfortranarray(b) for b in B)
+    return _HOST_FIELD
+
+
 def cpu_baseline(planes, threads=None):
     """The tracing routine (oracle port of the reference's, OpenMP) plus the
     Q assembly on `planes` z-planes of the cube, on the host cores."""
-    import torch
     import oracle
     from fastqsl_gb300 import params as P
     from oracle import qassembly as QA
-    (bx, by, bz), _ = make_field("cpu")
-    B = [b.numpy() if isinstance(b, torch.Tensor) else b for b in (bx, by, bz)]
-    B = [np.asfortranarray(b) for b in B]
+    B = host_field()
     xs, ys, zz, npl = cube_seeds("cpu", planes=planes)
     xs, ys, zz = xs.numpy(), ys.numpy(), zz.numpy()
     prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_EXACT)
