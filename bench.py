@@ -366,6 +366,104 @@ def batched_graph(device, n_fields=64, seed=11, reps=3):
     return out
 
 
+def forms(device, planes=16):
+    """The other forms of the path, each timed with CUDA events on its own
+    workload: on 16 mid-cube planes of the benchmark field (fp16 bricks) the
+    Q map by finite differences + pseudo-lines (the headline pipeline) and by
+    finite differences + Scott q_perp where they fail (hybrid), the main
+    trace with and without the twist integral (current from the GPU curl),
+    the Scott deviation-vector tracer alone on 2 planes; and the stretched-grid
+    tracer on a 256x256x128 grid, 1024x1024 seeds: the cell search with z
+    spacing growing 1 % per cell, the uniform-spacing formula on uniform
+    spacing."""
+    import torch
+    from fastqsl_gb300 import api, params as P, synthetic as S
+    from fastqsl_gb300.fastqslpy import FastQSL
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    (bx, by, bz), _ = make_field(device)
+    prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_FAST)
+    mid = SUB["nz"] // 2 - planes // 2
+    xs, ys, zz, npl = cube_seeds(device, planes=list(range(mid, mid + planes)))
+    n0, n1 = SUB["ny"] + 2, SUB["nx"] + 2
+    qpix = SUB["nx"] * SUB["ny"] * npl
+    store = api.FieldStore(bx, by, bz, layout="h4b")
+    res = {"workload": f"{npl} mid-cube planes ({qpix} Q-pixels) of the benchmark field, fp16 bricks"}
+    plan = api.QMapPlan(n0, n1, npl, device=device)
+    ms = timed(lambda: plan.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0))
+    res["q_fd_pseudo"] = {"ms": ms, "qpixels_per_s": qpix / ms * 1e3}
+    Qa = plan.Q.clone()
+    hyb = api.QMapPlan(n0, n1, npl, device=device, hybrid=True)
+    ms = timed(lambda: hyb.run(store, xs, ys, zz, prm, s_len=S_LEN, stride=1.0))
+    Qb = hyb.Q
+    both = torch.isfinite(Qa) & torch.isfinite(Qb) & (Qa > 0) & (Qb > 0)
+    d = (torch.log10(Qa[both]) - torch.log10(Qb[both])).abs()
+    res["q_hybrid_scott"] = {"ms": ms, "qpixels_per_s": qpix / ms * 1e3, "scott_pixels": int(hyb.hcount.item()),
+                             "nan_pixels": int((~torch.isfinite(Qb)).sum().item()),
+                             "nan_pixels_fd_pseudo": int((~torch.isfinite(Qa)).sum().item()),
+                             "median_dlog10Q_vs_fd_pseudo": float(d.median().item()) if d.numel() else None}
+    del hyb
+    order = api.tile_order(npl, n0, n1, 8, 8, device)
+    out = api.alloc_trace_outputs(xs.numel(), device, twist=True)
+    ax = [torch.arange(n, dtype=torch.float32, device=device) for n in bx.shape]
+    cur = [api.as_xfast(c.float()) for c in FastQSL.curl_of_B_grid(bx, by, bz, *ax)]
+    cnt = torch.zeros(1, dtype=torch.int64, device=device)
+    kw = dict(s_len=S_LEN, schedule="static", out=out, order=order, occupancy=8)
+    ms0 = timed(lambda: api.trace(store, xs, ys, zz, prm, **kw))
+    ms1 = timed(lambda: api.trace(store, xs, ys, zz, prm, curB=cur, **kw))
+    api.trace(store, xs, ys, zz, prm, curB=cur, samples=cnt, **kw)
+    torch.cuda.synchronize()
+    res["trace_twist"] = {"lines": int(xs.numel()), "ms_without": ms0, "ms_with": ms1,
+                          "samples": int(cnt.item()), "g_samples_per_s_with": cnt.item() / (ms1 * 1e6)}
+    del cur, out
+    m = 2 * n0 * n1
+    sx, sy, sz = xs[:m].contiguous(), ys[:m].contiguous(), zz[:m].contiguous()
+    so = api.alloc_scott_outputs(m, device)
+    sprm = P.reference_scott(arith=P.ARITH_FAST).copy(tol=1e-4, h_min=1e-3, h_max=1.0)
+    for g in ("analytic", "fd"):
+        cnt.zero_()
+        ms = timed(lambda: api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so))
+        api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so, samples=cnt)
+        torch.cuda.synchronize()
+        res[f"scott_{g}"] = {"lines": m, "ms": ms, "samples": int(cnt.item()),
+                             "g_samples_per_s": cnt.item() / (ms * 1e6)}
+    store.close()
+    shape = (256, 256, 128)
+    spec = S.bipole4_stretch(3, shape)
+    gx = torch.linspace(-5.5, 5.5, 1024, device=device)
+    gy = torch.linspace(-4.5, 4.5, 1024, device=device)
+    Y, X = torch.meshgrid(gy, gx, indexing="ij")
+    px, py = X.reshape(-1).contiguous(), Y.reshape(-1).contiguous()
+    sp = P.reference_stretch(arith=P.ARITH_FAST).copy(tol_law=P.TOL_ABSOLUTE, tol=1e-5, h_min=1e-4, h_max=0.05)
+    # the search on a grid whose z spacing grows 1 % per cell; the uniform
+    # formula (flag_uni) on the same box with uniform spacing, where it holds
+    for uni, ratio in ((False, 1.01), (True, 1.0)):
+        coords = S.stretched_axes(shape, z_ratio=ratio)
+        Bs = [torch.from_numpy(b).to(device) for b in S.make_field_coords(spec, *coords)]
+        pz = torch.full_like(px, float(coords[2][1]) * 0.5)
+        cnt.zero_()
+        api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01, uni=uni, samples=cnt)
+        torch.cuda.synchronize()
+        cfg_ms = {f"{sch}/occ{o}": timed(lambda: api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01, uni=uni,
+                                                                  occupancy=o, schedule=sch))
+                  for sch in ("static", "queue") for o in (0, 6)}
+        ms = min(cfg_ms.values())
+        res["stretch_" + ("uniform_formula" if uni else "search")] = {
+            "grid": "x".join(map(str, shape)), "z_ratio": ratio, "lines": int(px.numel()), "ms": ms,
+            "ms_by_launch": cfg_ms, "samples": int(cnt.item()), "g_samples_per_s": cnt.item() / (ms * 1e6)}
+    return res
+
+
 def serving_sweep(device, count=96):
     """8 resident 384x384x256 fields; Poisson streams of Q-map requests
     (10^4-4x10^6 seeds, tol 1e-3/1e-4/1e-5) at fractions of the batched
@@ -398,6 +496,7 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration (profiling)")
     ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--skip-forms", action="store_true")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     ap.add_argument("--plane-offset", type=int, default=0, help="first z-plane with --planes")
     args = ap.parse_args()
@@ -484,6 +583,9 @@ def main():
     if not args.skip_batched:
         import torch
         line["batched_graph"] = batched_graph(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
+    if not args.skip_forms:
+        import torch
+        line["forms"] = forms(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
     if not args.skip_serving:
         import torch
         line["serving"] = serving_sweep(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))

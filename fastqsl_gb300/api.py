@@ -225,12 +225,13 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
 
 def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = None, s_len=0.01, tol_coef=1.0,
                   uni=False, cross_dir=(0.0, 0.0, 1.0), curB=None, schedule="static", out=None, samples=None,
-                  order=None, stream=None):
+                  order=None, occupancy=0, stream=None):
     """Traces every seed both ways on a stretched grid: Bx, By, Bz of shape
     (nx, ny, nz) (x fastest; moved to the device if needed and read in place),
     coords = (x_arr, y_arr, z_arr) increasing node coordinates, seeds in the
     same physical coordinates (float32 CUDA vectors).  uni: index cells by the
-    uniform-spacing formula instead of the search.  Defaults to the reference
+    uniform-spacing formula instead of the search.  occupancy: resident-block
+    variant of the fast kernels (0, 6-10).  Defaults to the reference
     stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""
     from .params import reference_stretch
     lib = _lib.load()
@@ -250,7 +251,7 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     if curB is not None and out.get("twist") is None:
         out["twist"] = torch.zeros(n, dtype=torch.float64, device=xs.device)
     io = _io(xs, ys, zs, out)
-    sc = _lib.Sched(SCHEDULES[schedule], 0, ptr(order), None, ptr(samples), 0)
+    sc = _lib.Sched(SCHEDULES[schedule], 0, ptr(order), None, ptr(samples), int(occupancy))
     _lib.check(lib.qsl_trace_stretch(*[ptr(a) for a in arrs], nx, ny, nz, *[ptr(a) for a in ax], int(bool(uni)),
                                      ctypes.byref(params), ctypes.byref(io), n, float(s_len), float(tol_coef), cd,
                                      *cur, ctypes.byref(sc), stream_handle(stream)), "qsl_trace_stretch")

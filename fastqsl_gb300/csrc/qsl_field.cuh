@@ -183,7 +183,9 @@ struct FieldStretch {
     const float* az;
     const bool* uni_dev;  // when set, uni is read from here (drop-in)
     int uni;
-    float3 lo, hi;
+    float3 lo, hi;        // first and last node coordinates (read at kernel start)
+    float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
+    float3 us;            // uniform-formula spacing (hi - lo) / n
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         const FieldSoA s{bx, by, bz, d};
         return s.corners(ix, iy, iz, c);
@@ -471,24 +473,25 @@ __device__ __forceinline__ int stretch_bisect(float c, int n, const float* __res
     return r < 0 ? 0 : r;
 }
 
-// The uniform-spacing formula (GetIndexUniStretch, :67-74); its spacing is
-// (a[n-1] - a[0]) / n, the node count, as in the reference.
-__device__ __forceinline__ int stretch_uni(float c, int n, float a0, float an) {
-    int r = __float2int_rd((c - a0) / ((an - a0) / __int2float_rd(n)));
+// The uniform-spacing formula (GetIndexUniStretch, :67-74); its spacing du is
+// (a[n-1] - a[0]) / n, the node count, as in the reference (formed once per
+// kernel, the same float).
+__device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
+    int r = __float2int_rd((c - a0) / du);
     r = r < 0 ? 0 : r;
     return r > n - 2 ? n - 2 : r;
 }
 
 // Cell and fraction along one axis: c clamped to (a[0] + 1e-6, a[n-1] - 1e-6)
-// (offsets applied in double and narrowed), then the index and
-// r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122).
-__device__ __forceinline__ void stretch_locate(const FieldStretch& f, int k, float c, float a0, float an, int& i,
-                                               float& r) {
+// (offsets applied in double and narrowed, once per kernel: clo, chi), then
+// the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122).
+__device__ __forceinline__ void stretch_locate(const FieldStretch& f, int k, float c, float a0, float an, float clo,
+                                               float chi, float du, int& i, float& r) {
     const float* a = f.axis(k);
     const int n = f.d.n(k);
-    c = (c > a0) ? c : (float)((double)a0 + 1e-6);
-    c = (c < an) ? c : (float)((double)an - 1e-6);
-    i = f.uni ? stretch_uni(c, n, a0, an) : stretch_bisect(c, n, a);
+    c = (c > a0) ? c : clo;
+    c = (c < an) ? c : chi;
+    i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
     const float ai = __ldg(a + i);
     r = (c - ai) / (__ldg(a + i + 1) - ai);
 }
@@ -497,9 +500,9 @@ template <bool EXACT>
 __device__ __forceinline__ float3 sample_stretch(const FieldStretch& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
-    stretch_locate(f, 0, p.x, f.lo.x, f.hi.x, ix, rx);
-    stretch_locate(f, 1, p.y, f.lo.y, f.hi.y, iy, ry);
-    stretch_locate(f, 2, p.z, f.lo.z, f.hi.z, iz, rz);
+    stretch_locate(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, ix, rx);
+    stretch_locate(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, iy, ry);
+    stretch_locate(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, iz, rz);
     float w[8];
     if (EXACT) weights_exact(rx, ry, rz, w);
     else weights_fast(rx, ry, rz, w);

@@ -247,6 +247,12 @@ __device__ __forceinline__ double len_scale(const FieldStretch& f) {
 __device__ __forceinline__ void store_prepare(FieldStretch& f) {
     f.lo = v3(__ldg(f.ax), __ldg(f.ay), __ldg(f.az));
     f.hi = v3(__ldg(f.ax + f.d.nx - 1), __ldg(f.ay + f.d.ny - 1), __ldg(f.az + f.d.nz - 1));
+    // per-sample constants of the cell search, formed once (the FP64 pipe
+    // is narrow on this GPU)
+    f.clo = v3((float)((double)f.lo.x + 1e-6), (float)((double)f.lo.y + 1e-6), (float)((double)f.lo.z + 1e-6));
+    f.chi = v3((float)((double)f.hi.x - 1e-6), (float)((double)f.hi.y - 1e-6), (float)((double)f.hi.z - 1e-6));
+    f.us = v3((f.hi.x - f.lo.x) / __int2float_rd(f.d.nx), (f.hi.y - f.lo.y) / __int2float_rd(f.d.ny),
+              (f.hi.z - f.lo.z) / __int2float_rd(f.d.nz));
     if (f.uni_dev) f.uni = *f.uni_dev ? 1 : 0;
 }
 __device__ __forceinline__ FieldStretch current_view(const FieldStretch& f, const FieldSoA& c) {
