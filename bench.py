@@ -419,12 +419,19 @@ def forms(device, planes=16):
     cur = [api.as_xfast(c.float()) for c in FastQSL.curl_of_B_grid(bx, by, bz, *ax)]
     cnt = torch.zeros(1, dtype=torch.int64, device=device)
     kw = dict(s_len=S_LEN, schedule="static", out=out, order=order, occupancy=8)
-    ms0 = timed(lambda: api.trace(store, xs, ys, zz, prm, **kw))
-    ms1 = timed(lambda: api.trace(store, xs, ys, zz, prm, curB=cur, **kw))
-    api.trace(store, xs, ys, zz, prm, curB=cur, samples=cnt, **kw)
-    torch.cuda.synchronize()
-    res["trace_twist"] = {"lines": int(xs.numel()), "ms_without": ms0, "ms_with": ms1,
-                          "samples": int(cnt.item()), "g_samples_per_s_with": cnt.item() / (ms1 * 1e6)}
+    f4 = api.FieldStore(bx, by, bz, layout="f4")
+    for name, st in (("h4b", store), ("f4", f4)):
+        cs = api.FieldStore(*cur, layout=name)
+        ms0 = timed(lambda: api.trace(st, xs, ys, zz, prm, **kw))
+        ms1 = timed(lambda: api.trace(st, xs, ys, zz, prm, curB=cur, **kw))
+        ms2 = timed(lambda: api.trace(st, xs, ys, zz, prm, curB=cs, **kw))
+        cnt.zero_()
+        api.trace(st, xs, ys, zz, prm, curB=cs, samples=cnt, **kw)
+        torch.cuda.synchronize()
+        res[f"trace_twist_{name}"] = {"lines": int(xs.numel()), "ms_without": ms0, "ms_with_current_arrays": ms1,
+                                      "ms_with_current_store": ms2, "samples_with": int(cnt.item())}
+        cs.close()
+    f4.close()
     del cur, out
     m = 2 * n0 * n1
     sx, sy, sz = xs[:m].contiguous(), ys[:m].contiguous(), zz[:m].contiguous()

@@ -101,6 +101,7 @@ _SIGS = {
     "qsl_field_bytes": (c_i64, [_P]),
     "qsl_field_update": (c_int, [_P, _P, _P, _P, _P]),
     "qsl_trace": (c_int, [_P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P, _P, _P, _P]),
+    "qsl_trace_cur": (c_int, [_P, _P, _P, _P, c_i64, _P, c_float, c_float, _P, _P, _P]),
     "qsl_qcalc_plane": (c_int, [_P] * 13 + [c_int, c_int, c_i64, c_double, _P, _P, _P, _P]),
     "qsl_cook_workspace_bytes": (c_i64, [c_i64]),
     "qsl_cook_pseudo_line": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 8 + [c_i64, _P]),

@@ -204,7 +204,10 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
     device counter holding the seed count (outputs must then hold the largest
     count).  `samples`: optional int64 CUDA tensor accumulating the number of
     trilinear samples taken.  `order`: optional int32 permutation; line k
-    traces seed order[k] (see tile_order).  `chunk`: lines per warp refill."""
+    traces seed order[k] (see tile_order).  `chunk`: lines per warp refill.
+    `curB`: the current density for the twist integral, as three x-fastest
+    float32 device arrays or as a FieldStore of the field's layout and shape
+    (qsl_trace_cur: each current sample costs a field sample)."""
     lib = _lib.load()
     if params is None:
         params = absolute_rkf45()
@@ -212,11 +215,16 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
     if out is None:
         out = alloc_trace_outputs(n, xs.device, twist=curB is not None)
     cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
-    cur = [ptr(c) for c in curB] if curB is not None else [None, None, None]
     if curB is not None and out.get("twist") is None:
         out["twist"] = torch.zeros(out["LineLen"].shape[0], dtype=torch.float64, device=xs.device)
     io = _io(xs, ys, zs, out)
     sc = _lib.Sched(SCHEDULES[schedule], int(chunk), ptr(order), ptr(queue), ptr(samples), int(occupancy))
+    if isinstance(curB, FieldStore):
+        _lib.check(lib.qsl_trace_cur(field.handle, curB.handle, ctypes.byref(params), ctypes.byref(io), n,
+                                     ptr(n_dev), float(s_len), float(tol_coef), cd, ctypes.byref(sc),
+                                     stream_handle(stream)), "qsl_trace_cur")
+        return out
+    cur = [ptr(c) for c in curB] if curB is not None else [None, None, None]
     _lib.check(lib.qsl_trace(field.handle, ctypes.byref(params), ctypes.byref(io), n, ptr(n_dev),
                              float(s_len), float(tol_coef), cd, *cur, ctypes.byref(sc), stream_handle(stream)),
                "qsl_trace")

@@ -308,16 +308,27 @@ static void fill_common(TraceJob<F>& J, const qsl_trace_io* io, const qsl_trace_
     J.order = nullptr;
     J.chunk = 0;
     J.occupancy = 0;
+    J.cur_packed = 0;
+    J.cur_store = J.f;
     memset(&J.s, 0, sizeof(J.s));
     J.s.n_cap = -1;
 }
 
 extern "C" {
 
-int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n,
-              const unsigned long long* n_dev, float s_len, float tol_coef, const float* cross_dir_h,
-              const float* curBx, const float* curBy, const float* curBz, const qsl_sched* sched_h,
-              qsl_stream_t stream) {
+extern "C++" {
+static void store_view(const qsl_field_t* f, FieldSoA& s) { s = soa_of(f); }
+static void store_view(const qsl_field_t* f, FieldF4& s) { s = f4_of(f); }
+static void store_view(const qsl_field_t* f, FieldH4B& s) { s = h4b_of(f); }
+static void store_view(const qsl_field_t* f, FieldH8C& s) { s = h8c_of(f); }
+}
+
+// qsl_trace and qsl_trace_cur: the current density comes from the caller's
+// arrays (curBx/y/z) or from a store of the field's layout (cur_field).
+static int trace_impl(const qsl_field_t* field, const qsl_field_t* cur_field, const qsl_trace_params* prm,
+                      const qsl_trace_io* io, int64_t n, const unsigned long long* n_dev, float s_len,
+                      float tol_coef, const float* cross_dir_h, const float* curBx, const float* curBy,
+                      const float* curBz, const qsl_sched* sched_h, qsl_stream_t stream) {
     qsl_sched sc{QSL_SCHED_QUEUE, 0, nullptr, nullptr, nullptr, 0};
     if (sched_h) sc = *sched_h;
     const int schedule = sc.schedule;
@@ -334,8 +345,14 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
     if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
     if (schedule != QSL_SCHED_QUEUE && schedule != QSL_SCHED_STATIC)
         return fail(QSL_ERR_INVALID, "bad schedule %d", schedule);
-    const bool twist = curBx != nullptr;
-    if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
+    const bool twist = curBx != nullptr || cur_field != nullptr;
+    if (curBx && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
+    if (cur_field) {
+        if (!io->twist) return fail(QSL_ERR_INVALID, "twist needs the twist output");
+        if (cur_field->layout != field->layout || cur_field->d.nx != field->d.nx || cur_field->d.ny != field->d.ny ||
+            cur_field->d.nz != field->d.nz)
+            return fail(QSL_ERR_INVALID, "the current store must have the field's layout and shape");
+    }
     if (field->layout != LAYOUT_SOA && prm->arith == QSL_ARITH_EXACT)
         return fail(QSL_ERR_INVALID, "exact arithmetic needs the SoA layout");
     const float cd[3] = {cross_dir_h ? cross_dir_h[0] : 0.f, cross_dir_h ? cross_dir_h[1] : 0.f,
@@ -356,6 +373,10 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         J.f = store;
         fill_common(J, io, prm, samples_dev);
         J.cur = cur;
+        if (cur_field) {
+            store_view(cur_field, J.cur_store);
+            J.cur_packed = 1;
+        }
         J.order = sc.order;
         J.chunk = sc.chunk;
         J.occupancy = sc.occupancy;
@@ -368,6 +389,22 @@ int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_t
         case LAYOUT_H4B: return go(h4b_of(field));
         default: return go(h8c_of(field));
     }
+}
+
+int qsl_trace(const qsl_field_t* field, const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n,
+              const unsigned long long* n_dev, float s_len, float tol_coef, const float* cross_dir_h,
+              const float* curBx, const float* curBy, const float* curBz, const qsl_sched* sched_h,
+              qsl_stream_t stream) {
+    return trace_impl(field, nullptr, prm, io, n, n_dev, s_len, tol_coef, cross_dir_h, curBx, curBy, curBz, sched_h,
+                      stream);
+}
+
+int qsl_trace_cur(const qsl_field_t* field, const qsl_field_t* cur, const qsl_trace_params* prm,
+                  const qsl_trace_io* io, int64_t n, const unsigned long long* n_dev, float s_len, float tol_coef,
+                  const float* cross_dir_h, const qsl_sched* sched_h, qsl_stream_t stream) {
+    if (!cur) return fail(QSL_ERR_INVALID, "current store is null");
+    return trace_impl(field, cur, prm, io, n, n_dev, s_len, tol_coef, cross_dir_h, nullptr, nullptr, nullptr, sched_h,
+                      stream);
 }
 
 // Drop-in entry: the reference kernel's argument list (TraceBlineAdaptive.cu:

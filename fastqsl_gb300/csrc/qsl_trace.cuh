@@ -18,6 +18,10 @@
 namespace qsl {
 
 constexpr double kRefPi = 3.14159265;  // the reference's M_PI (TraceBlineAdaptive.cu:10)
+// 1 / (4 pi) for the fast twist increment: one float product per step and a
+// single double add, instead of the reference's double divides (the FP64
+// pipe is narrow on this GPU)
+constexpr float kInv4PiF = (float)(1.0 / (4.0 * kRefPi));
 
 struct TraceOut {
     float *start_x, *start_y, *start_z;
@@ -63,7 +67,9 @@ template <class F>
 struct TraceJob {
     F f;
     const int* shape_dev;  // when set, the field dims are read from here (nx, ny, nz)
-    FieldSoA cur;  // current density for the twist integral
+    FieldSoA cur;  // current density for the twist integral (the caller's arrays)
+    F cur_store;   // or, when cur_packed, the current density in a store of F's layout
+    int cur_packed;
     const float *inp_x, *inp_y, *inp_z;
     TraceOut o;
     TraceScalars s;
@@ -396,17 +402,18 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
     float td = 0.f;
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
     if (TWIST && tw_on) {
-        j1 = sample<EXACT>(current_view(f, J.cur), L.p, false);
+        j1 = J.cur_packed ? sample<EXACT>(J.cur_store, L.p, false) : sample<EXACT>(current_view(f, J.cur), L.p, false);
         b1 = sample<EXACT>(f, L.p, false);
         ns += 2;
         td = dot(j1, b1) / dot(b1, b1);
-        L.tw = L.tw + (double)td / 4.0 / kRefPi * (double)dl;
+        L.tw = L.tw + (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
     }
     // inside test first: the full face classification only runs on exit
     const int flag = box_inside(f, p2) ? 0 : box_exit(f, p2);
     if (flag > 0) {
         len_add(L, -(double)dl, -dl);
-        if (TWIST && tw_on) L.tw = L.tw - (double)td / 4.0 / kRefPi * (double)dl;
+        if (TWIST && tw_on)
+            L.tw = L.tw - (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
         if (flag <= 6) {
             const int d = (flag - 1) / 2;
             const float q1 = comp(L.p, d), q2 = comp(p2, d);

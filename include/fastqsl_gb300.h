@@ -205,6 +205,15 @@ int qsl_trace(const qsl_field_t *field, const qsl_trace_params *params_h, const 
               const float *curBx, const float *curBy, const float *curBz, const qsl_sched *sched_h,
               qsl_stream_t stream);
 
+/* qsl_trace with the twist integral's current density held in a store of
+ * the field's own layout and shape (qsl_field_create of curl B): one current
+ * sample then costs what a field sample costs, instead of 24 scalar gathers
+ * from the caller's arrays (TraceBlineAdaptive.cu:373-377 samples it at
+ * every step).  io_h->twist receives the integral. */
+int qsl_trace_cur(const qsl_field_t *field, const qsl_field_t *cur, const qsl_trace_params *params_h,
+                  const qsl_trace_io *io_h, int64_t n, const unsigned long long *n_dev, float s_len, float tol_coef,
+                  const float *cross_dir_h, const qsl_sched *sched_h, qsl_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Batched trace plans (no reference counterpart: the reference launches one
  * kernel per seed set).  Many jobs — different fields (any store), seed

@@ -212,3 +212,50 @@ def test_zero_field_terminates(cuda):
         torch.cuda.synchronize()
         assert (out["flag_end"].cpu() == 42).all()
         assert (out["flag_start"].cpu() == 42).all()
+
+
+@pytest.mark.parametrize("layout,packed", [("soa", False), ("f4", False), ("h4b", False), ("f4", True),
+                                           ("h4b", True)])
+def test_native_twist_vs_fp64_oracle(cuda, oracle_port, layout, packed):
+    """The twist integral of the fast kernels (current density J = curl B
+    stand-in, sampled on the traced grid; from the caller's arrays or, packed,
+    from a store of the field's layout) against the FP64 oracle, on lines
+    whose two exit faces agree; fp16 field storage widens the bar.  A float32
+    packed current gives the same integral as the arrays, bit for bit."""
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.charges_random(3, (96, 96, 64), 8)
+    Bx, By, Bz = S.make_field(spec)
+    cur = G.twist_current(Bx, By, Bz)
+    xs, ys, zs, shp = S.plane_seeds((2, 93), (2, 93), 48, 48, 0.5)
+    prm = P.absolute_rkf45(arith=P.ARITH_FAST)
+    ref = oracle_port.trace_all("port64", Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0,
+                                params=P.absolute_rkf45(arith=P.ARITH_EXACT), curB=cur)
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout=layout)
+    curd = _field_dev(*cur)
+    if packed:
+        cs = api.FieldStore(*curd, layout=layout)
+        out = api.trace(fs, _dev(xs), _dev(ys), _dev(zs), prm, s_len=0.25, tol_coef=1.0, schedule="static",
+                        curB=cs)
+        if layout == "f4":
+            arrays = api.trace(fs, _dev(xs), _dev(ys), _dev(zs), prm, s_len=0.25, tol_coef=1.0, schedule="static",
+                               curB=curd)
+            assert torch.equal(arrays["twist"], out["twist"])
+    else:
+        out = api.trace(fs, _dev(xs), _dev(ys), _dev(zs), prm, s_len=0.25, tol_coef=1.0, schedule="static",
+                        curB=curd)
+    torch.cuda.synchronize()
+    tw = out["twist"].cpu().numpy()
+    same = ((out["flag_start"].cpu().numpy() == ref["flag_start"]) & (out["flag_end"].cpu().numpy() == ref["flag_end"])
+            & (ref["flag_start"] != 0) & (ref["flag_end"] != 0))
+    assert same.mean() > 0.9
+    rel = np.abs(tw[same] - ref["twist"][same]) / np.maximum(np.abs(ref["twist"][same]), 1e-3)
+    med, p90 = np.median(rel), np.quantile(rel, 0.9)
+    ll = out["LineLen"].cpu().numpy()
+    rl = np.abs(ll[same] - ref["LineLen"][same]) / np.maximum(ref["LineLen"][same], 1e-6)
+    print(layout, packed, "twist rel err median %.2e p90 %.2e" % (med, p90), "len rel median %.2e p90 %.2e" % (
+        np.median(rl), np.quantile(rl, 0.9)))
+    # fp16 nodes: the integrand J.B/|B|^2 follows the stored direction of B,
+    # whose rounding (2^-11 of the brick's largest component) reaches a few
+    # 1e-3 in the weak corners of bricks next to the charges
+    bar = (2e-2, 1.5e-1) if layout == "h4b" else (1e-4, 1e-3)
+    assert med <= bar[0] and p90 <= bar[1], (med, p90)
