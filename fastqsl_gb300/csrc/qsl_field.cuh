@@ -291,6 +291,41 @@ __device__ __forceinline__ float3 sample(const F& f, float3 p, bool unit) {
     return r;
 }
 
+// Fast arithmetic: B/|B| and B at p from one interpolation (the twist kernels
+// need both at each step's start point), normalised and scaled as
+// sample<false> does with unit = true / false.  Stores without a one-pass
+// form take two samples.
+template <class F>
+__device__ __forceinline__ float3 sample_unit_raw(const F& f, float3 p, float3& raw) {
+    raw = sample<false>(f, p, false);
+    return sample<false>(f, p, true);
+}
+
+template <class F>
+__device__ __forceinline__ float3 sample_unit_raw_generic(const F& f, float3 p, float3& raw) {
+    int ix, iy, iz;
+    float rx, ry, rz;
+    locate_fast(p.x, f.d.nx, ix, rx);
+    locate_fast(p.y, f.d.ny, iy, ry);
+    locate_fast(p.z, f.d.nz, iz, rz);
+    float w[8];
+    weights_fast(rx, ry, rz, w);
+    float3 c[8];
+    const float s = f.corners(ix, iy, iz, c);
+    const float3 r = blend<false>(c, w);
+    raw = s != 1.0f ? v3(r.x * s, r.y * s, r.z * s) : r;
+    const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+    return v3(r.x * inv, r.y * inv, r.z * inv);
+}
+template <>
+__device__ __forceinline__ float3 sample_unit_raw<FieldSoA>(const FieldSoA& f, float3 p, float3& raw) {
+    return sample_unit_raw_generic(f, p, raw);
+}
+template <>
+__device__ __forceinline__ float3 sample_unit_raw<FieldF4>(const FieldF4& f, float3 p, float3& raw) {
+    return sample_unit_raw_generic(f, p, raw);
+}
+
 // ---------------------------------------------------------------------------
 // Fast sampling of the fp16 brick store without fp16->fp32 conversions.
 //
@@ -328,8 +363,8 @@ __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float o, float r) {
     return __ffma2_rn(b, make_float2(r, r), __fmul2_rn(a, make_float2(o, o)));
 }
 
-template <>
-__device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, float3 p, bool unit) {
+// The trilinear value at p in brick units (times the brick's scale = B).
+__device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsigned& brick_out) {
     int ix, iy, iz;
     float rx, ry, rz;
     locate_fast(p.x, f.d.nx, ix, rx);
@@ -356,7 +391,14 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
     const float2 g0 = lerp2(exy[0], exy[2], oy, ry), g1 = lerp2(exy[1], exy[3], oy, ry);
     const float gz0 = fmaf(ez[2], ry, ez[0] * oy), gz1 = fmaf(ez[3], ry, ez[1] * oy);
     const float2 rxy = lerp2(g0, g1, oz, rz);
-    float3 r = v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
+    brick_out = brick;
+    return v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
+}
+
+template <>
+__device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, float3 p, bool unit) {
+    unsigned brick;
+    float3 r = h4b_interp(f, p, brick);
     if (unit) {
         const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
         r = v3(r.x * inv, r.y * inv, r.z * inv);
@@ -365,6 +407,16 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
         r = v3(r.x * s, r.y * s, r.z * s);
     }
     return r;
+}
+
+template <>
+__device__ __forceinline__ float3 sample_unit_raw<FieldH4B>(const FieldH4B& f, float3 p, float3& raw) {
+    unsigned brick;
+    const float3 r = h4b_interp(f, p, brick);
+    const float s = __ldg(f.scale + brick);
+    raw = v3(r.x * s, r.y * s, r.z * s);
+    const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+    return v3(r.x * inv, r.y * inv, r.z * inv);
 }
 
 // (1 - r) lo + r hi of one fp16 pair (w = the fp16 pair (1 - r, r)), the

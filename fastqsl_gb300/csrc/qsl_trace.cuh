@@ -119,10 +119,12 @@ __device__ __forceinline__ PV scal(float a, PV x) { return {__fmul2_rn(make_floa
 // packed (x, y) pairs.  Differs from the reference's rounding sequence only
 // in rounding.
 template <class F>
-__device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h, float& err, unsigned& ns) {
+__device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h, float& err, unsigned& ns,
+                                                 float3* b_raw = nullptr) {
     using C = Fehlberg;
     const PV P = pv(p);
-    const PV b1 = pv(sample<false>(f, p, true));
+    // b_raw: also return B itself at p (from the same interpolation)
+    const PV b1 = pv(b_raw ? sample_unit_raw(f, p, *b_raw) : sample<false>(f, p, true));
     const PV b2 = pv(sample<false>(f, f3(axpy(h * C::a21, b1, P)), true));
     PV c = axpy(C::a32, b2, scal(C::a31, b1));
     const PV b3 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
@@ -139,8 +141,9 @@ __device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h,
 }
 
 template <bool EXACT, class F>
-__device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, float& err, unsigned& ns) {
-    if (!EXACT) return step_rkf45_fast(f, p, h, err, ns);
+__device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, float& err, unsigned& ns,
+                                            float3* b_raw = nullptr) {
+    if (!EXACT) return step_rkf45_fast(f, p, h, err, ns, b_raw);
     using C = Fehlberg;
     const float3 k1 = h * sample<EXACT>(f, p, true);
     const float3 k2 = h * sample<EXACT>(f, p + C::a21 * k1, true);
@@ -158,8 +161,8 @@ __device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, floa
 // Classic RK4 on b (RK4, TraceBlineAdaptive.cu:259-267); returns the
 // increment.  The 1/6 factor is formed as (1./6.)*h in double and narrowed.
 template <bool EXACT, class F>
-__device__ __forceinline__ float3 step_rk4(const F& f, float3 p, float h, unsigned& ns) {
-    const float3 k1 = sample<EXACT>(f, p, true);
+__device__ __forceinline__ float3 step_rk4(const F& f, float3 p, float h, unsigned& ns, float3* b_raw = nullptr) {
+    const float3 k1 = (!EXACT && b_raw) ? sample_unit_raw(f, p, *b_raw) : sample<EXACT>(f, p, true);
     const float3 k2 = sample<EXACT>(f, p + (h * k1) / 2.f, true);
     const float3 k3 = sample<EXACT>(f, p + (h * k2) / 2.f, true);
     const float3 k4 = sample<EXACT>(f, p + h * k3, true);
@@ -355,9 +358,12 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
     }
     const float hd = L.h * (float)L.dir;
     float3 inc;
+    // fast twist kernels: B at L.p comes out of the step's first sample
+    float3 b_at_p = v3(0.f, 0.f, 0.f);
+    float3* const want_b = (!EXACT && TWIST && tw_on) ? &b_at_p : nullptr;
     if (pr.integrator == QSL_RKF45) {
         float err;
-        inc = step_rkf45<EXACT>(f, L.p, hd, err, ns);
+        inc = step_rkf45<EXACT>(f, L.p, hd, err, ns, want_b);
         float scale;
         if (EXACT) {
             scale = pow_cr((float)((double)(L.tol / err) / 11.09), 0.2f);
@@ -384,7 +390,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         }
         L.h = h;
     } else {
-        inc = step_rk4<EXACT>(f, L.p, hd, ns);
+        inc = step_rk4<EXACT>(f, L.p, hd, ns, want_b);
     }
     float3 p2;
     if (EXACT) {
@@ -403,8 +409,13 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
     if (TWIST && tw_on) {
         j1 = J.cur_packed ? sample<EXACT>(J.cur_store, L.p, false) : sample<EXACT>(current_view(f, J.cur), L.p, false);
-        b1 = sample<EXACT>(f, L.p, false);
-        ns += 2;
+        if (EXACT) {
+            b1 = sample<EXACT>(f, L.p, false);
+            ns += 2;
+        } else {
+            b1 = b_at_p;
+            ns += 1;
+        }
         td = dot(j1, b1) / dot(b1, b1);
         L.tw = L.tw + (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
     }
