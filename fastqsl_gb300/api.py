@@ -398,14 +398,23 @@ class QMapPlan:
     def samples(self):
         return self.samples_buf.sum()
 
+    @property
+    def twist_map(self):
+        """Twist number of every seed line of the last run with a current
+        density, shape (nplanes, n0, n1) (None before such a run)."""
+        t = self.main.get("twist")
+        return None if t is None else t.view(self.nplanes, self.n0, self.n1)
+
     def run(self, field, xs, ys, zs, params=None, s_len=0.125, tol_coef=1.0, stride=1.0, cross_dir=(0.0, 0.0, 1.0),
             pseudo_tol_factor=1.0, count_samples=False, kernel_events=None, stream=None, scott_params=None,
-            scott_grad="analytic"):
+            scott_grad="analytic", curB=None):
         """Runs the pipeline; `kernel_events` (start, end) CUDA events are
         recorded around the main trace launch when given.  scott_params /
         scott_grad: the Scott pass of a hybrid plan (default: the Scott
         tracer's reference settings in fast arithmetic with the main trace's
-        tolerance and step bounds)."""
+        tolerance and step bounds).  curB: the current density (three arrays
+        or a FieldStore of the field's layout); the main trace then also
+        integrates each seed's twist number (`twist_map`)."""
         lib = _lib.load()
         st = stream_handle(stream)
         if params is None:
@@ -413,10 +422,12 @@ class QMapPlan:
         if count_samples:
             self.samples_buf.zero_()
         m = self.main
+        if curB is not None and m.get("twist") is None:
+            m["twist"] = torch.zeros(self.n, dtype=torch.float64, device=m["LineLen"].device)
         ev_stream = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.current_stream()
         if kernel_events is not None:
             kernel_events[0].record(ev_stream)
-        trace(field, xs, ys, zs, params, s_len, tol_coef, cross_dir, out=m, n=self.n,
+        trace(field, xs, ys, zs, params, s_len, tol_coef, cross_dir, curB=curB, out=m, n=self.n,
               samples=self.samples_buf[0:1] if count_samples else None, queue=self.queue, order=self.order,
               chunk=self.chunk, schedule=self.schedule, occupancy=self.occupancy_for(field), stream=stream)
         if kernel_events is not None:

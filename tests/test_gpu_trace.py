@@ -259,3 +259,26 @@ def test_native_twist_vs_fp64_oracle(cuda, oracle_port, layout, packed):
     # 1e-3 in the weak corners of bricks next to the charges
     bar = (2e-2, 1.5e-1) if layout == "h4b" else (1e-4, 1e-3)
     assert med <= bar[0] and p90 <= bar[1], (med, p90)
+
+
+def test_qmap_plan_twist_map(cuda):
+    """QMapPlan.run with a current density: Q unchanged, and each seed's twist
+    equal to the single trace's (the plan's tile order only reassigns lines
+    to threads)."""
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.charges_random(4, (64, 56, 48), 6)
+    B = S.make_field(spec)
+    cur = G.twist_current(*B)
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout="h4b")
+    cs = api.FieldStore(*_field_dev(*cur), layout="h4b")
+    n0, n1 = 20, 24
+    xs, ys, zz = api.plane_seed_grid(4.0, 4.0 + 2.0 * (n1 - 1), n1, 4.0, 4.0 + 2.0 * (n0 - 1), n0, [0.5, 3.0])
+    prm = P.absolute_rkf45(arith=P.ARITH_FAST)
+    plan = api.QMapPlan(n0, n1, 2)
+    assert plan.twist_map is None
+    Q0 = plan.run(fs, xs, ys, zz, prm, s_len=0.25, stride=2.0).clone()
+    Q1 = plan.run(fs, xs, ys, zz, prm, s_len=0.25, stride=2.0, curB=cs)
+    assert torch.equal(torch.nan_to_num(Q0, nan=-1.0), torch.nan_to_num(Q1, nan=-1.0))
+    ref = api.trace(fs, xs, ys, zz, prm, s_len=0.25, schedule="static", curB=cs, occupancy=plan.occupancy_for(fs))
+    assert plan.twist_map.shape == (2, n0, n1)
+    assert torch.equal(plan.twist_map.reshape(-1), ref["twist"])
