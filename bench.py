@@ -504,6 +504,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration (profiling)")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
+    ap.add_argument("--forms-only", action="store_true", help="only the forms section (profiling)")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     ap.add_argument("--plane-offset", type=int, default=0, help="first z-plane with --planes")
     args = ap.parse_args()
@@ -514,6 +515,11 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+
+    if args.forms_only:
+        import torch
+        print(json.dumps({"forms": forms(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))}))
+        return
 
     if args.impl == "reference":
         if rank != 0:
