@@ -27,6 +27,13 @@ static cudaError_t launch_fast_minb(const TraceJob<F>& J, bool twist, Schedule s
         grid = persistent_grid(k, kTraceBlock);
     } else {
         long long g = (n_host + kTraceBlock - 1) / kTraceBlock;
+        // a device-side count (n_host is only the capacity): two resident
+        // waves of blocks stride over the lines instead of a grid over the
+        // whole capacity whose surplus blocks would each start and exit
+        if (J.s.n_dev) {
+            const long long cap = 2LL * persistent_grid(k, kTraceBlock);
+            if (cap > 0 && g > cap) g = cap;
+        }
         grid = (int)(g < 1 ? 1 : (g > (1 << 30) ? (1 << 30) : g));
     }
     if (grid <= 0) return cudaErrorInvalidConfiguration;
