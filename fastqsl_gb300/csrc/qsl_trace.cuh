@@ -481,24 +481,33 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 template <bool EXACT, bool TWIST, bool QUEUE, class F>
 __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     F f = J.f;
-    if (J.shape_dev) {
-        f.d.nx = __ldg(J.shape_dev);
-        f.d.ny = __ldg(J.shape_dev + 1);
-        f.d.nz = __ldg(J.shape_dev + 2);
+    // only the drop-in stores (the caller's arrays) take their shape from the
+    // device; the packed stores' dims stay kernel parameters
+    if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value) {
+        if (J.shape_dev) {
+            f.d.nx = __ldg(J.shape_dev);
+            f.d.ny = __ldg(J.shape_dev + 1);
+            f.d.nz = __ldg(J.shape_dev + 2);
+        }
     }
     // a grid needs two nodes per axis for a trilinear cell (uniform exit)
     if (f.d.nx < 2 || f.d.ny < 2 || f.d.nz < 2) return;
-    const float s_len = J.s.s_len_dev ? __ldg(J.s.s_len_dev) : J.s.s_len;
-    const float tol_coef = J.s.tol_coef_dev ? __ldg(J.s.tol_coef_dev) : J.s.tol_coef;
+    // Loop invariants that are used once per line are re-read at each use
+    // (kernel parameters or one cached load) rather than held in registers:
+    // registers set how many blocks stay resident, and the gathers need
+    // every resident warp to hide their latency.
+    auto s_len_of = [&J]() { return J.s.s_len_dev ? __ldg(J.s.s_len_dev) : J.s.s_len; };
+    auto tol_coef_of = [&J]() { return J.s.tol_coef_dev ? __ldg(J.s.tol_coef_dev) : J.s.tol_coef; };
+    auto nrm_of = [&J]() {
+        return J.s.cross_dev ? v3(__ldg(J.s.cross_dev), __ldg(J.s.cross_dev + 1), __ldg(J.s.cross_dev + 2))
+                             : v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
+    };
     long long n = J.s.n_dev ? (long long)__ldg(J.s.n_dev) : J.s.n;
     if (J.s.n_cap >= 0 && n > J.s.n_cap) n = J.s.n_cap;
-    const float3 nrm = J.s.cross_dev ? v3(__ldg(J.s.cross_dev), __ldg(J.s.cross_dev + 1), __ldg(J.s.cross_dev + 2))
-                                     : v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
     store_prepare(f);
     const typename Lane<EXACT>::len_t len_lim = (typename Lane<EXACT>::len_t)(J.prm.len_ratio * len_scale(f));
     unsigned ns = 0;
-    unsigned long long ns_total = 0;
     const int lane_id = threadIdx.x & 31;
 
     Lane<EXACT> L;
@@ -509,7 +518,6 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     bool q_empty = false;
     const long long chunk = J.chunk > 0 ? J.chunk : 256;
     long long next_static = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long stride = (long long)gridDim.x * blockDim.x;
 
     while (true) {
         // ---- give lanes without a line the next ones ----
@@ -539,7 +547,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
                 if (need && rank < take) {
                     const long long line = c_next + rank;
                     const long long sidx = J.order ? (long long)__ldg(J.order + line) : line;
-                    lane_begin<EXACT>(f, J, L, sidx, +1, s_len, tol_coef, nrm, ns);
+                    lane_begin<EXACT>(f, J, L, sidx, +1, s_len_of(), tol_coef_of(), nrm_of(), ns);
                     active = true;
                     need = false;
                 }
@@ -552,8 +560,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
             if (!active) {
                 if (next_static >= n) break;
                 const long long sidx = J.order ? (long long)__ldg(J.order + next_static) : next_static;
-                lane_begin<EXACT>(f, J, L, sidx, +1, s_len, tol_coef, nrm, ns);
-                next_static += stride;
+                lane_begin<EXACT>(f, J, L, sidx, +1, s_len_of(), tol_coef_of(), nrm_of(), ns);
+                next_static += (long long)gridDim.x * blockDim.x;
                 active = true;
             }
         }
@@ -573,7 +581,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
                 o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
                 o.line_len[i] = (double)L.len;
                 if (TWIST && tw_on) o.twist[i] = L.tw;
-                lane_begin<EXACT>(f, J, L, i, -1, s_len, tol_coef, nrm, ns);
+                lane_begin<EXACT>(f, J, L, i, -1, s_len_of(), tol_coef_of(), nrm_of(), ns);
             } else {
                 const float3 ps = L.out;
                 const float3 bs = sample_endpoint<EXACT>(f, ps);
@@ -587,22 +595,22 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
                 o.line_len[i] = o.line_len[i] + (double)L.len;
                 if (TWIST && tw_on) o.twist[i] = o.twist[i] + L.tw;
                 // B nearly in the seed plane (TraceBlineAdaptive.cu:498-501)
+                const float3 nrm = nrm_of();
                 const float bn = b0.x * nrm.x + b0.y * nrm.y + b0.z * nrm.z;
                 const float bm = sqrtf(b0.x * b0.x + b0.y * b0.y + b0.z * b0.z);
                 o.b_flag[i] = ((double)fabsf(bn) * 100. < (double)bm) ? 1 : 0;
                 active = false;
             }
         }
-        if (ns > (1u << 30)) {
-            ns_total += ns;
+        if (ns > (1u << 30)) {  // a lane's count nears 32 bits: hand it over (rare)
+            if (J.samples) atomicAdd(J.samples, (unsigned long long)ns);
             ns = 0;
         }
     }
     if (J.samples) {
-        ns_total += ns;
         // one atomic per warp (blocks are whole warps; every lane gets here)
         __syncwarp();
-        unsigned long long v = ns_total;
+        unsigned long long v = ns;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane_id == 0) atomicAdd(J.samples, v);
     }
