@@ -505,6 +505,7 @@ def main():
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--skip-forms", action="store_true")
     ap.add_argument("--forms-only", action="store_true", help="only the forms section (profiling)")
+    ap.add_argument("--batched-only", action="store_true", help="only the batched-graph section (profiling)")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     ap.add_argument("--plane-offset", type=int, default=0, help="first z-plane with --planes")
     args = ap.parse_args()
@@ -516,9 +517,10 @@ def main():
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
 
-    if args.forms_only:
+    if args.forms_only or args.batched_only:
         import torch
-        print(json.dumps({"forms": forms(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))}))
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+        print(json.dumps({"forms": forms(dev)} if args.forms_only else {"batched_graph": batched_graph(dev)}))
         return
 
     if args.impl == "reference":
