@@ -141,11 +141,13 @@ class QServer:
     max_batch: requests per batch."""
 
     # size classes: (upper bound on seeds, requests per batch, batches in flight)
-    CLASSES = ((1.5e5, 32, 2), (1.2e6, 8, 2), (float("inf"), 2, 2))
+    # (larger requests fill the GPU alone: batching them only makes each
+    # wait for its batch mates)
+    CLASSES = ((1.5e5, 32, 2), (1.2e6, 2, 3), (float("inf"), 1, 3))
 
     def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
-                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=4,
-                 chunks_when_interactive=1, window_streams=2, window_blocks_per_sm=0):
+                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=6,
+                 chunks_when_interactive=2, window_streams=2, window_blocks_per_sm=0):
         self.fields = dict(fields)
         self.budget = int(hbm_budget)
         self.used = 0
