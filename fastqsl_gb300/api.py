@@ -62,10 +62,11 @@ def as_xfast(a, device="cuda"):
 class FieldStore:
     """A field resident on the device in one of the GB300 layouts.
 
-    layout: 'h8c' (fp16 cell records: each cell's 8 corners in 64 B, the
-    fastest store, ~64 B per cell), 'h4b' (fp16 8^3 bricks + per-brick scale,
-    ~11 B per node), 'f4' (interleaved float4) or 'soa' (the caller's arrays
-    in place)."""
+    layout: 'h4b' (fp16 8^3 bricks + per-brick scale, stored as x-pair
+    records of 16 B, ~20 B per node: the fastest store and the default),
+    'h8c' (fp16 cell records: each cell's 8 corners in 64 B), 'f4'
+    (interleaved float4, float32 values) or 'soa' (the caller's float32
+    arrays in place)."""
 
     def __init__(self, Bx, By, Bz, layout="h4b", stream=None):
         lib = _lib.load()
