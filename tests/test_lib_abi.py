@@ -71,3 +71,32 @@ def test_version_and_errors_without_gpu(lib):
     assert lib.qsl_field_store_bytes(1, 5, 5, 1) == -1
     assert lib.qsl_field_store_bytes(9, 9, 9, 2) == 10368 + 4  # one brick of x-pair records + its scale
     assert lib.qsl_field_store_bytes(10, 10, 10, 1) == 16000
+
+
+def test_new_entries_validate_without_gpu(lib):
+    """The polyline, current-store and window entries reject bad arguments
+    before any CUDA call."""
+    import ctypes
+    from fastqsl_gb300 import _lib
+    # qsl_trace_path: index range outside the output rows, zero stride, nulls
+    dummy = ctypes.c_void_p(16)
+    args = [dummy, dummy, dummy, 4, 4, 4, dummy, 1]
+    tail = [0.25, dummy, dummy, dummy, 10, None]
+    assert lib.qsl_trace_path(*args, 5, 11, 1, *tail) == -1
+    assert b"outside" in lib.qsl_last_error()
+    assert lib.qsl_trace_path(*args, 5, -2, -1, *tail) == -1
+    assert lib.qsl_trace_path(*args, 0, 5, 0, *tail) == -1
+    assert lib.qsl_trace_path(None, None, None, 4, 4, 4, None, 1, 0, 5, 1, 0.25, None, None, None, 10, None) == -1
+    assert lib.qsl_trace_path(*args, 0, 0, 1, *tail) == 0  # an empty range does nothing
+    assert lib.qsl_sample_points(None, None, None, 4, 4, 4, None, 3, 1, None, None) == -1
+    assert lib.qsl_sample_points(dummy, dummy, dummy, 1, 4, 4, dummy, 3, 1, dummy, None) == -1
+    # qsl_trace_cur: a null current store
+    from fastqsl_gb300 import params as P
+    prm = P.absolute_rkf45()
+    io = _lib.TraceIO()
+    assert lib.qsl_trace_cur(None, None, ctypes.byref(prm), ctypes.byref(io), 10, None, 0.25, 1.0, None, None,
+                             None) == -1
+    assert b"null" in lib.qsl_last_error()
+    # qsl_batch_run_window: null table
+    info = _lib.BatchInfo()
+    assert lib.qsl_batch_run_window(None, ctypes.byref(info), None, 0, -1, 0, None) != 0
