@@ -570,9 +570,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      # DRAM bytes per launch: ncu's dram__bytes_read.sum + write.sum
-                     # on the 8-plane case (3.361 GB for 913.9 M samples,
-                     # profiles/trace_h4b_cube8.md) scaled by this launch's samples
-                     "traffic": (3.361e9 / 913.9e6) * res["samples_main"] if args.layout == "h4b" else None,
+                     # of the full-size main trace (one-pass capture: 1.18 GB read +
+                     # 0.70 GB written for 14.82 G samples,
+                     # profiles/trace_h4b_cube_traffic.md), per this launch's samples
+                     "traffic": (1.884e9 / 14.816e9) * res["samples_main"] if args.layout == "h4b" else None,
                      "kernel": f"k_trace_fast<static, {STORE_TYPES[args.layout]}> (main trace)",
                      "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
                              f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
