@@ -370,8 +370,9 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
     locate_fast(p.x, f.d.nx, ix, rx);
     locate_fast(p.y, f.d.ny, iy, ry);
     locate_fast(p.z, f.d.nz, iz, rz);
-    const float rq = rintf(rx * 2048.f) * (1.f / 2048.f);
-    const __half2 wh = __floats2half2_rn(1.f - rq, rq);  // exact: both on the 2^-11 grid
+    // the x weights (1 - rx, rx) rounded to fp16 each (they sum to 1 within
+    // 2^-11; a normalised sample does not see their sum)
+    const __half2 wh = __floats2half2_rn(1.f - rx, rx);
     const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
     // brick indices fit 32 bits (field stores hold < 1.1e12 nodes, so fewer
     // than 2.2e9 bricks)
@@ -389,10 +390,11 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
         xlerp_h4(make_uint2(u[q].x, u[q].y), make_uint2(u[q].z, u[q].w), w, exy[q].x, exy[q].y, ez[q]);
     const float oy = 1.f - ry, oz = 1.f - rz;
     const float2 g0 = lerp2(exy[0], exy[2], oy, ry), g1 = lerp2(exy[1], exy[3], oy, ry);
-    const float gz0 = fmaf(ez[2], ry, ez[0] * oy), gz1 = fmaf(ez[3], ry, ez[1] * oy);
+    // the two z-column y-lerps as one packed pair
+    const float2 gz = lerp2(make_float2(ez[0], ez[1]), make_float2(ez[2], ez[3]), oy, ry);
     const float2 rxy = lerp2(g0, g1, oz, rz);
     brick_out = brick;
-    return v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
+    return v3(rxy.x, rxy.y, fmaf(gz.y, rz, gz.x * oz));
 }
 
 template <>
@@ -401,7 +403,8 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
     float3 r = h4b_interp(f, p, brick);
     if (unit) {
         const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
-        r = v3(r.x * inv, r.y * inv, r.z * inv);
+        const float2 xy = __fmul2_rn(make_float2(r.x, r.y), make_float2(inv, inv));
+        r = v3(xy.x, xy.y, r.z * inv);
     } else {
         const float s = __ldg(f.scale + brick);
         r = v3(r.x * s, r.y * s, r.z * s);
