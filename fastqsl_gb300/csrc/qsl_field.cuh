@@ -205,14 +205,17 @@ __device__ __forceinline__ void locate(float c, int n, int& i, float& r) {
     if (c >= (float)(n - 1)) { r = 1.f; i = n - 2; }
 }
 
-// Fast form of locate(): clamp into [0, n-1] first, then the cell index is
-// min(trunc, n-2) and the fraction the remainder (6 instructions per axis
-// instead of 8).  Identical for finite coordinates; a NaN coordinate lands on
-// cell 0 with fraction 0 (the line's position is NaN anyway and leaves with
-// flag 42 at the boundary test).
+// Fast form of locate(): clamp into [0, top] with top the largest float
+// below n-1, so that the truncation is at most n-2 and the fraction the
+// remainder (5 instructions per axis instead of 8).  A point on the far face
+// samples cell n-2 at a fraction 1 - 2^-24 (n-1) below 1 rather than at 1;
+// elsewhere it is locate().  A NaN coordinate lands on cell 0 with fraction 0
+// (the line's position is NaN anyway and leaves with flag 42 at the boundary
+// test).
 __device__ __forceinline__ void locate_fast(float c, int n, int& i, float& r) {
-    const float cc = fminf(fmaxf(c, 0.f), (float)(n - 1));
-    i = min(__float2int_rz(cc), n - 2);
+    const float top = __int_as_float(__float_as_int((float)(n - 1)) - 1);
+    const float cc = fminf(fmaxf(c, 0.f), top);
+    i = __float2int_rz(cc);
     r = cc - (float)i;
 }
 
