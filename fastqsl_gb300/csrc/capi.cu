@@ -146,6 +146,14 @@ int qsl_field_create(const float* Bx, const float* By, const float* Bz, int nx, 
     int nbx, nby, nbz;
     const int64_t bytes = layout_bytes(nx, ny, nz, layout, &nbx, &nby, &nbz);
     if (bytes < 0) return fail(QSL_ERR_INVALID, "unknown layout %d", layout);
+    if (layout == LAYOUT_H4B) {
+        // the brick sampler forms a record index within a z-slab of bricks
+        // in 32 bits (FieldH4B::ky, kz)
+        const unsigned long long slab = (unsigned long long)BRICK_U4 * nbx * nby + 640ull * nbx + 64ull * nby +
+                                        576ull * nbz;
+        if (slab >= (1ull << 32))
+            return fail(QSL_ERR_TOO_LARGE, "field too wide for fp16 bricks (%d x %d nodes per z-slab)", nx, ny);
+    }
     qsl_field* f = new (std::nothrow) qsl_field();
     if (!f) return fail(QSL_ERR_NOMEM, "host allocation failed");
     f->layout = layout;
@@ -219,7 +227,10 @@ int qsl_field_update(qsl_field_t* f, const float* Bx, const float* By, const flo
 // device views of a store
 static FieldSoA soa_of(const qsl_field* f) { return FieldSoA{f->bx, f->by, f->bz, f->d}; }
 static FieldF4 f4_of(const qsl_field* f) { return FieldF4{f->f4, f->d}; }
-static FieldH4B h4b_of(const qsl_field* f) { return FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby}; }
+static FieldH4B h4b_of(const qsl_field* f) {
+    return FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby, (unsigned)(BRICK_U4 * f->nbx - 64),
+                    (unsigned)((unsigned long long)BRICK_U4 * f->nbx * f->nby - 576)};
+}
 static FieldH8C h8c_of(const qsl_field* f) { return FieldH8C{f->cells, f->d, f->nbx, f->nby}; }
 
 // ---------------------------------------------------------------------------

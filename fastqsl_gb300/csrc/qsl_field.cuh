@@ -110,6 +110,10 @@ struct FieldH4B {
     const float* scale;  // per brick
     Dims d;
     int nbx, nby;        // bricks along x and y
+    // record index of cell (ix, iy, iz) = h4b_record(): brick * BRICK_U4 +
+    // (ix & 7) + 8 (iy & 7) + 72 (iz & 7) regrouped per axis as
+    // ix + 640 (ix >> 3) + 8 iy + ky (iy >> 3) + 72 iz + kz (iz >> 3)
+    unsigned ky, kz;     // BRICK_U4 nbx - 64, BRICK_U4 nbx nby - 576
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         const int bi = ix >> 3, bj = iy >> 3, bk = iz >> 3;
         const int64_t brick = bi + (int64_t)nbx * (bj + (int64_t)nby * bk);
@@ -377,11 +381,11 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
     // 2^-11; a normalised sample does not see their sum)
     const __half2 wh = __floats2half2_rn(1.f - rx, rx);
     const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
-    // brick indices fit 32 bits (field stores hold < 1.1e12 nodes, so fewer
-    // than 2.2e9 bricks)
-    const unsigned brick = (unsigned)(ix >> 3) + (unsigned)f.nbx * ((unsigned)(iy >> 3) + (unsigned)f.nby * (unsigned)(iz >> 3));
-    const unsigned rec = (unsigned)((ix & 7) + 8 * ((iy & 7) + BRICK_NODES * (iz & 7)));
-    const uint4* bp = f.bricks + ((unsigned long long)brick * BRICK_U4 + rec);
+    // the record index, with the z term (the only one that can pass 2^32) in
+    // 64 bits
+    const unsigned part = (unsigned)ix + 640u * (unsigned)(ix >> 3) + 8u * (unsigned)iy + f.ky * (unsigned)(iy >> 3) +
+                          72u * (unsigned)iz;
+    const uint4* bp = f.bricks + ((unsigned long long)f.kz * (unsigned)(iz >> 3) + part);
     uint4 u[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) u[q] = __ldg(bp + ((q >> 1) & 1) * 8 + (q & 1) * (8 * BRICK_NODES));
@@ -396,7 +400,9 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
     // the two z-column y-lerps as one packed pair
     const float2 gz = lerp2(make_float2(ez[0], ez[1]), make_float2(ez[2], ez[3]), oy, ry);
     const float2 rxy = lerp2(g0, g1, oz, rz);
-    brick_out = brick;
+    // brick indices fit 32 bits (field stores hold < 1.1e12 nodes, so fewer
+    // than 2.2e9 bricks); only the unnormalised samples use it
+    brick_out = (unsigned)(ix >> 3) + (unsigned)f.nbx * ((unsigned)(iy >> 3) + (unsigned)f.nby * (unsigned)(iz >> 3));
     return v3(rxy.x, rxy.y, fmaf(gz.y, rz, gz.x * oz));
 }
 
