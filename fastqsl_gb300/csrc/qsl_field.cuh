@@ -43,6 +43,14 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) { return v3(s * a
 __device__ __forceinline__ float3 operator/(float3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float norm(float3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+// |a| with the hardware square-root approximation (sqrt.approx.f32, relative
+// error ~2^-22): the fast stepper's error norm and step length, where the
+// IEEE square root's range checks and fix-up cost more than they are worth
+__device__ __forceinline__ float norm_fast(float3 a) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(fmaf(a.x, a.x, fmaf(a.y, a.y, a.z * a.z))));
+    return r;
+}
 __device__ __forceinline__ float comp(float3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }
 __device__ __forceinline__ float fcomp(const float* a, int d) { return a[d]; }
 

@@ -135,7 +135,7 @@ __device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h,
     c = axpy(C::a65, b5, axpy(C::a64, b4, axpy(C::a63, b3, axpy(C::a62, b2, scal(C::a61, b1)))));
     const PV b6 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
     const PV e = axpy(C::e6, b6, axpy(C::e5, b5, axpy(C::e4, b4, axpy(C::e3, b3, scal(C::e1, b1)))));
-    err = fabsf(h) * norm(f3(e));
+    err = fabsf(h) * norm_fast(f3(e));
     ns += 6;
     return f3(scal(h, axpy(C::b6, b6, axpy(C::b5, b5, axpy(C::b4, b4, axpy(C::b3, b3, scal(C::b1, b1)))))));
 }
@@ -374,7 +374,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         } else {
             // only the next step size depends on this power: hardware
             // log2 / exp2 are accurate enough
-            scale = exp2f(0.2f * __log2f(L.tol / err * (float)(1.0 / 11.09)));
+            scale = exp2f(0.2f * __log2f(__fdividef(L.tol, err) * (float)(1.0 / 11.09)));
             if (scale < 0.618f) {
                 L.h = L.h * J.lim.reject;
                 return false;
@@ -403,7 +403,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         p2 = L.p + y;
         L.pc = (p2 - L.p) - y;
     }
-    const float dl = norm(L.p - p2);
+    const float dl = EXACT ? norm(L.p - p2) : norm_fast(L.p - p2);
     len_add(L, (double)dl, dl);
     float td = 0.f;
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
