@@ -314,6 +314,8 @@ static void fill_common(TraceJob<F>& J, const qsl_trace_io* io, const qsl_trace_
     J.lim.h_max = (float)prm->h_max;
     J.lim.reject = (float)prm->reject_factor;
     J.lim.max_steps = prm->max_steps > INT_MAX ? INT_MAX : (prm->max_steps < 0 ? 0 : (int)prm->max_steps);
+    // the kernels' own product, (float)(len_ratio * (double)(nx + ny + nz))
+    J.lim.len_lim = (float)(prm->len_ratio * (double)(J.f.d.nx + J.f.d.ny + J.f.d.nz));
     J.queue = nullptr;
     J.samples = samples_dev;
     J.order = nullptr;

@@ -26,7 +26,12 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
     const float3 nrm = v3(J.s.cross[0], J.s.cross[1], J.s.cross[2]);
     const bool tw_on = TWIST && J.s.twist_on != 0;
     store_prepare(f);
-    const float len_lim = (float)(J.prm.len_ratio * len_scale(f));
+    float len_lim;
+    if constexpr (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldF4>::value ||
+                  std::is_same<F, FieldH8C>::value)
+        len_lim = J.lim.len_lim;
+    else
+        len_lim = (float)(J.prm.len_ratio * len_scale(f));
     Lane<false> L;
     lane_begin<false>(f, J, L, i, +1, s_len, tol_coef, nrm, ns);
     const TraceOut& o = J.o;

@@ -61,6 +61,7 @@ struct TraceScalars {
 struct StepLimits {
     float h_min, h_max, reject;
     int max_steps;
+    float len_lim;  // len_ratio x (nx + ny + nz) in float, formed on the host (packed stores)
 };
 
 template <class F>
@@ -341,6 +342,14 @@ __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lan
     }
 }
 
+// 2^x by the hardware approximation (ex2.approx.ftz.f32): the fast step
+// controller only needs the next step size to a few digits.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // One trial step of the current direction.  Returns true when the direction
 // is finished (left the box, or stopped by the length / step limit) with
 // L.out, L.flag, L.len, L.tw final.  Reference: TraceBlineAdap,
@@ -374,7 +383,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         } else {
             // only the next step size depends on this power: hardware
             // log2 / exp2 are accurate enough
-            scale = exp2f(0.2f * __log2f(__fdividef(L.tol, err) * (float)(1.0 / 11.09)));
+            scale = ex2_approx(0.2f * __log2f(__fdividef(L.tol, err) * (float)(1.0 / 11.09)));
             if (scale < 0.618f) {
                 L.h = L.h * J.lim.reject;
                 return false;
@@ -506,7 +515,15 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     if (J.s.n_cap >= 0 && n > J.s.n_cap) n = J.s.n_cap;
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
     store_prepare(f);
-    const typename Lane<EXACT>::len_t len_lim = (typename Lane<EXACT>::len_t)(J.prm.len_ratio * len_scale(f));
+    // the packed stores' dims are known on the host: their length limit is a
+    // kernel parameter (a register would be re-formed from the double
+    // product at every step once the loop runs short of registers)
+    typename Lane<EXACT>::len_t len_lim;
+    if constexpr (!EXACT && (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldF4>::value ||
+                             std::is_same<F, FieldH8C>::value))
+        len_lim = J.lim.len_lim;
+    else
+        len_lim = (typename Lane<EXACT>::len_t)(J.prm.len_ratio * len_scale(f));
     unsigned ns = 0;
     const int lane_id = threadIdx.x & 31;
 
