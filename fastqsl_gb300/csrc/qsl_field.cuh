@@ -347,11 +347,12 @@ __device__ __forceinline__ float3 sample_unit_raw<FieldF4>(const FieldF4& f, flo
 // The x-lerp of each corner pair reads the fp16 components directly with the
 // mixed-precision multiply-add (fma.rn.f32.f16: the f16 x f16 product is exact
 // and the sum is rounded once to f32); the y and z lerps run on packed f32
-// pairs (fma.rn.f32x2) for (Bx, By) and scalar f32 for Bz.  The x fraction
-// is rounded to a multiple of 2^-11, on which both r and 1 - r are exact in
-// fp16, so the x weights sum to exactly 1 and the result is the trilinear
-// value at a point within 2^-12 cell of p along x (the fp16 node values
-// themselves carry a relative rounding of up to 2^-12).
+// pairs (fma.rn.f32x2) for (Bx, By) and scalar f32 for Bz.  The x weights
+// enter as fp16: in the brick store (1 - r, r) each rounded to fp16 (their
+// sum is 1 within 2^-11, which a normalised sample does not see), in the
+// cell-record store r rounded to the 2^-11 grid first so that both weights
+// are exact and sum to 1 (the fp16 node values themselves carry a relative
+// rounding of up to 2^-12).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void xlerp_h4(uint2 lo, uint2 hi, unsigned w, float& x, float& y, float& z) {
     asm("{\n\t"
