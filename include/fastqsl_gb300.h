@@ -143,9 +143,11 @@ int qsl_trace_all_bline(int integrator, int arith, const float *Bx, const float 
 enum qsl_layout {
     QSL_LAYOUT_SOA = 0, /* the caller's Bx, By, Bz in place */
     QSL_LAYOUT_F4 = 1,  /* interleaved float4 per node (16 B/node) */
-    QSL_LAYOUT_H4B = 2, /* fp16 8^3-cell bricks with a +1 apron and a float scale per brick */
+    QSL_LAYOUT_H4B = 2, /* fp16 8^3-cell bricks with a +1 apron and a float scale per brick, as x-pair
+                           records (node i and i+1 in 16 B; ~20 B/node): the fastest store.  A
+                           z-slab of bricks must hold < 2^32 records (nx, ny up to ~20,000) */
     QSL_LAYOUT_H8C = 3  /* fp16 cell records: each cell's 8 corner vectors in 64 B, power-of-two
-                           scale per cell (fastest fp16 store; ~64 B per cell) */
+                           scale per cell (~64 B per cell) */
 };
 typedef struct qsl_field qsl_field_t;
 
