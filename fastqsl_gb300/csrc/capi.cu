@@ -289,6 +289,8 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
         e = launch_trace_fast_f4(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldH4B>::value) {
         e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldStretchP>::value) {
+        e = launch_trace_fast_stretch_packed(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldStretch>::value) {
         e = arith == QSL_ARITH_EXACT ? launch_trace_exact_stretch(J, twist, sched, n_host, st)
                                      : launch_trace_fast_stretch(J, twist, sched, n_host, st);
@@ -486,22 +488,52 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
     const bool twist = curBx != nullptr;
     if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
-    TraceJob<FieldStretch> J;
-    J.f = FieldStretch{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
-                       make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    fill_common(J, io, prm, sc.samples);
-    J.cur = FieldSoA{curBx, curBy, curBz, J.f.d};
-    J.order = sc.order;
-    J.chunk = sc.chunk;
-    J.occupancy = sc.occupancy;
-    J.s.s_len = s_len;
-    J.s.tol_coef = tol_coef;
-    J.s.n = n;
-    J.s.cross[0] = cross_dir_h ? cross_dir_h[0] : 0.f;
-    J.s.cross[1] = cross_dir_h ? cross_dir_h[1] : 0.f;
-    J.s.cross[2] = cross_dir_h ? cross_dir_h[2] : 1.f;
-    J.s.twist_on = twist ? 1 : 0;
-    return run_trace(J, prm->arith, twist, sc.schedule, n, sc.queue, (cudaStream_t)stream);
+    cudaStream_t st = (cudaStream_t)stream;
+    auto go = [&](auto store) {
+        TraceJob<decltype(store)> J;
+        J.f = store;
+        fill_common(J, io, prm, sc.samples);
+        J.cur = FieldSoA{curBx, curBy, curBz, J.f.d};
+        J.order = sc.order;
+        J.chunk = sc.chunk;
+        J.occupancy = sc.occupancy;
+        J.s.s_len = s_len;
+        J.s.tol_coef = tol_coef;
+        J.s.n = n;
+        J.s.cross[0] = cross_dir_h ? cross_dir_h[0] : 0.f;
+        J.s.cross[1] = cross_dir_h ? cross_dir_h[1] : 0.f;
+        J.s.cross[2] = cross_dir_h ? cross_dir_h[2] : 1.f;
+        J.s.twist_on = twist ? 1 : 0;
+        return run_trace(J, prm->arith, twist, sc.schedule, n, sc.queue, st);
+    };
+    const FieldStretch f{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
+                         make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+    if (prm->arith != QSL_ARITH_FAST) return go(f);
+    // fast arithmetic: the nodes interleaved into a stream-ordered float4
+    // copy for the launch (one 16-byte load per corner; the same values)
+    const int64_t nodes = (int64_t)nx * ny * nz;
+    float4* b4 = nullptr;
+    QSL_CHECK_CUDA(cudaMallocAsync((void**)&b4, (size_t)nodes * sizeof(float4), st), "node copy allocation");
+    cudaError_t e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(b4, st);
+        return cuda_fail(e, "node copy");
+    }
+    FieldStretchP fp;
+    fp.bx = Bx;
+    fp.by = By;
+    fp.bz = Bz;
+    fp.d = f.d;
+    fp.ax = x_arr;
+    fp.ay = y_arr;
+    fp.az = z_arr;
+    fp.uni_dev = nullptr;
+    fp.uni = f.uni;
+    fp.lo = fp.hi = fp.clo = fp.chi = fp.us = make_float3(0.f, 0.f, 0.f);
+    fp.b4 = b4;
+    const int rc = go(fp);
+    cudaFreeAsync(b4, st);
+    return rc;
 }
 
 // Drop-in entry for the stretched-grid kernel: the argument list of

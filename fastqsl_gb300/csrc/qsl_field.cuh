@@ -185,7 +185,11 @@ struct FieldH8C {
 // ay[ny], az[nz].  uni selects the reference's uniform-spacing index formula
 // instead of its search; lo/hi are the first and last coordinates (set at
 // kernel start from the coordinate arrays).
-struct FieldStretch {
+// PACKED: the node values come from an interleaved float4 copy (b4: one
+// 16-byte load per corner instead of three 4-byte gathers; the same float
+// values, so the same results).
+template <bool PACKED>
+struct FieldStretchT {
     const float* bx;
     const float* by;
     const float* bz;
@@ -198,12 +202,20 @@ struct FieldStretch {
     float3 lo, hi;        // first and last node coordinates (read at kernel start)
     float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
     float3 us;            // uniform-formula spacing (hi - lo) / n
+    const float4* b4;     // PACKED: Bx, By, Bz, 0 per node, x fastest
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
-        const FieldSoA s{bx, by, bz, d};
-        return s.corners(ix, iy, iz, c);
+        if constexpr (PACKED) {
+            const FieldF4 s{b4, d};
+            return s.corners(ix, iy, iz, c);
+        } else {
+            const FieldSoA s{bx, by, bz, d};
+            return s.corners(ix, iy, iz, c);
+        }
     }
     __device__ __forceinline__ const float* axis(int k) const { return k == 0 ? ax : (k == 1 ? ay : az); }
 };
+using FieldStretch = FieldStretchT<false>;
+using FieldStretchP = FieldStretchT<true>;
 
 // ---------------------------------------------------------------------------
 // Cell location with the reference's face pinning (Interp3dxyzn,
@@ -558,8 +570,9 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
 // Cell and fraction along one axis: c clamped to (a[0] + 1e-6, a[n-1] - 1e-6)
 // (offsets applied in double and narrowed, once per kernel: clo, chi), then
 // the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122).
-__device__ __forceinline__ void stretch_locate(const FieldStretch& f, int k, float c, float a0, float an, float clo,
-                                               float chi, float du, int& i, float& r) {
+template <bool P>
+__device__ __forceinline__ void stretch_locate(const FieldStretchT<P>& f, int k, float c, float a0, float an,
+                                               float clo, float chi, float du, int& i, float& r) {
     const float* a = f.axis(k);
     const int n = f.d.n(k);
     c = (c > a0) ? c : clo;
@@ -569,8 +582,8 @@ __device__ __forceinline__ void stretch_locate(const FieldStretch& f, int k, flo
     r = (c - ai) / (__ldg(a + i + 1) - ai);
 }
 
-template <bool EXACT>
-__device__ __forceinline__ float3 sample_stretch(const FieldStretch& f, float3 p, bool unit) {
+template <bool EXACT, bool P>
+__device__ __forceinline__ float3 sample_stretch(const FieldStretchT<P>& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
     stretch_locate(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, ix, rx);
@@ -600,6 +613,10 @@ __device__ __forceinline__ float3 sample<true, FieldStretch>(const FieldStretch&
 }
 template <>
 __device__ __forceinline__ float3 sample<false, FieldStretch>(const FieldStretch& f, float3 p, bool unit) {
+    return sample_stretch<false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldStretchP>(const FieldStretchP& f, float3 p, bool unit) {
     return sample_stretch<false>(f, p, unit);
 }
 
@@ -663,6 +680,10 @@ __device__ __forceinline__ float3 sample_endpoint<true, FieldStretch>(const Fiel
 }
 template <>
 __device__ __forceinline__ float3 sample_endpoint<false, FieldStretch>(const FieldStretch& f, float3 p) {
+    return sample_stretch<false>(f, p, false);
+}
+template <>
+__device__ __forceinline__ float3 sample_endpoint<false, FieldStretchP>(const FieldStretchP& f, float3 p) {
     return sample_stretch<false>(f, p, false);
 }
 

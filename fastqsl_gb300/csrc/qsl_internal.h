@@ -27,6 +27,8 @@ cudaError_t launch_trace_exact_stretch(const TraceJob<FieldStretch>& J, bool twi
 // trace_fast_stretch.cu
 cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
                                       cudaStream_t st);
+cudaError_t launch_trace_fast_stretch_packed(const TraceJob<FieldStretchP>& J, bool twist, Schedule sched,
+                                             long long n_host, cudaStream_t st);
 
 // trace_fast_<store>.cu
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,

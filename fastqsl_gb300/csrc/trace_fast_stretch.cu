@@ -10,4 +10,9 @@ cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twis
     return launch_fast(J, twist, sched, n_host, st);
 }
 
+cudaError_t launch_trace_fast_stretch_packed(const TraceJob<FieldStretchP>& J, bool twist, Schedule sched,
+                                             long long n_host, cudaStream_t st) {
+    return launch_fast(J, twist, sched, n_host, st);
+}
+
 }  // namespace qsl

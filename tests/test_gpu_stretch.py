@@ -125,3 +125,29 @@ def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
         d = np.max(np.abs(np.stack([got[f"{side}_{a}"] - ref[f"{side}_{a}"] for a in "xyz"])), axis=0)
         assert (d[m] <= 1e-3).mean() >= 0.99, (side, np.quantile(d[m], [0.5, 0.99]))
     assert int(samples.item()) > 6 * len(xs)
+
+
+@pytest.mark.parametrize("uni,twist", [(False, False), (True, True)])
+def test_native_fast_packed_equals_dropin_fast(cuda, uni, twist):
+    """The native stretched entry in fast arithmetic reads the nodes from an
+    interleaved float4 copy, the drop-in from the caller's three arrays: the
+    same float values through the same arithmetic, so every output is the
+    same bit for bit (twist included: the current stays the caller's
+    arrays)."""
+    from fastqsl_gb300 import api, synthetic as S
+    spec = S.bipole4_stretch(7)
+    coords = S.stretched_axes(spec.shape, z_ratio=1.0 if uni else 1.05)
+    Bx, By, Bz = S.make_field_coords(spec, *coords)
+    cur = G.twist_current(Bx, By, Bz) if twist else None
+    xs, ys, zs, _ = S.plane_seeds((-5, 5), (-4, 4), 40, 32, 0.3)
+    got_d = run_dropin_stretch(Bx, By, Bz, coords, uni, xs, ys, zs, 0.01, 1.0, curB=cur, arith="fast")
+    prm = P.reference_stretch(arith=P.ARITH_FAST)
+    out = api.trace_stretch(*[torch.from_numpy(np.asfortranarray(b)) for b in (Bx, By, Bz)],
+                            [torch.from_numpy(c).cuda() for c in coords], _dev(xs), _dev(ys), _dev(zs), prm,
+                            s_len=0.01, uni=uni, curB=[_fdev(c) for c in cur] if twist else None)
+    torch.cuda.synchronize()
+    got_n = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    keys = F32 + I32 + ["LineLen"] + (["twist"] if twist else [])
+    for k in keys:
+        a, b = got_n[k], got_d[k]
+        assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]), k
