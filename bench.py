@@ -461,9 +461,11 @@ def forms(device, planes=16):
         cnt.zero_()
         api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01, uni=uni, samples=cnt)
         torch.cuda.synchronize()
-        cfg_ms = {f"{sch}/occ{o}": timed(lambda: api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01, uni=uni,
-                                                                  occupancy=o, schedule=sch))
-                  for sch in ("static", "queue") for o in (0, 6)}
+        tiles = api.tile_order(1, 1024, 1024, 8, 8, device)
+        cfg_ms = {f"{sch}/occ{o}/{name}": timed(lambda: api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01,
+                                                                          uni=uni, occupancy=o, schedule=sch,
+                                                                          order=order))
+                  for sch in ("static", "queue") for o in (0, 6) for name, order in (("rows", None), ("tiles", tiles))}
         ms = min(cfg_ms.values())
         res["stretch_" + ("uniform_formula" if uni else "search")] = {
             "grid": "x".join(map(str, shape)), "z_ratio": ratio, "lines": int(px.numel()), "ms": ms,
