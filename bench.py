@@ -372,7 +372,8 @@ def forms(device, planes=16):
     Q map by finite differences + pseudo-lines (the headline pipeline) and by
     finite differences + Scott q_perp where they fail (hybrid), the main
     trace with and without the twist integral (current from the GPU curl),
-    the Scott deviation-vector tracer alone on 2 planes; and the stretched-grid
+    the Scott deviation-vector tracer alone on 2 planes (seeds in 8x8 tiles);
+    and the stretched-grid
     tracer on a 256x256x128 grid, 1024x1024 seeds: the cell search with z
     spacing growing 1 % per cell, the uniform-spacing formula on uniform
     spacing."""
@@ -437,10 +438,11 @@ def forms(device, planes=16):
     sx, sy, sz = xs[:m].contiguous(), ys[:m].contiguous(), zz[:m].contiguous()
     so = api.alloc_scott_outputs(m, device)
     sprm = P.reference_scott(arith=P.ARITH_FAST).copy(tol=1e-4, h_min=1e-3, h_max=1.0)
+    sorder = api.tile_order(2, n0, n1, 8, 8, device)
     for g in ("analytic", "fd"):
         cnt.zero_()
-        ms = timed(lambda: api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so))
-        api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so, samples=cnt)
+        ms = timed(lambda: api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so, order=sorder))
+        api.trace_scott(store, sx, sy, sz, sprm, s_len=S_LEN, grad=g, out=so, samples=cnt, order=sorder)
         torch.cuda.synchronize()
         res[f"scott_{g}"] = {"lines": m, "ms": ms, "samples": int(cnt.item()),
                              "g_samples_per_s": cnt.item() / (ms * 1e6)}
