@@ -240,7 +240,8 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     coords = (x_arr, y_arr, z_arr) increasing node coordinates, seeds in the
     same physical coordinates (float32 CUDA vectors).  uni: index cells by the
     uniform-spacing formula instead of the search.  occupancy: resident-block
-    variant of the fast kernels (0, 6-10).  Defaults to the reference
+    variant of the fast kernels (6; any other value takes the compiler's
+    register choice).  Defaults to the reference
     stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""
     from .params import reference_stretch
     lib = _lib.load()

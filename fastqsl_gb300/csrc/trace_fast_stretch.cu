@@ -1,18 +1,16 @@
-// Fast tracer kernels on a stretched grid (FieldStretch), in the same
-// resident-block variants as the uniform stores (the compiler's register
-// choice leaves 3 blocks per SM for this gather-latency-bound loop).
+// Fast tracer kernels on a stretched grid, reading the caller's three arrays
+// (FieldStretch, the drop-in).  Two resident-block variants: the compiler's
+// register choice (3 blocks per SM) and the 6-block budget; the others
+// spill without gain on this gather-latency-bound loop, and each variant
+// costs compile time.
 #include "qsl_kernels.cuh"
 
 namespace qsl {
 
 cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
                                       cudaStream_t st) {
-    return launch_fast(J, twist, sched, n_host, st);
-}
-
-cudaError_t launch_trace_fast_stretch_packed(const TraceJob<FieldStretchP>& J, bool twist, Schedule sched,
-                                             long long n_host, cudaStream_t st) {
-    return launch_fast(J, twist, sched, n_host, st);
+    return J.occupancy == 6 ? launch_fast_minb<FieldStretch, 6>(J, twist, sched, n_host, st)
+                            : launch_fast_minb<FieldStretch, 1>(J, twist, sched, n_host, st);
 }
 
 }  // namespace qsl
