@@ -47,7 +47,7 @@ __global__ void k_qcalc_plane(const QPlaneArgs a) {
         const long long base = pl * (long long)a.n0 * a.n1;
         const long long c = base + (long long)i * a.n1 + j;
         const long long up = c + a.n1, dn = c - a.n1, rt = c + 1, lf = c - 1;
-        T X1u, Y1u, X1d, Y1d, X1r, Y1r, X1l, Y1l, X2u, Y2u, X2d, Y2d, X2r, Y2r, X2l, Y2l;
+        float X1u, Y1u, X1d, Y1d, X1r, Y1r, X1l, Y1l, X2u, Y2u, X2d, Y2d, X2r, Y2r, X2l, Y2l;
         face_xy(a.xs[up], a.ys[up], a.zs[up], a.fs[up], X1u, Y1u);
         face_xy(a.xs[dn], a.ys[dn], a.zs[dn], a.fs[dn], X1d, Y1d);
         face_xy(a.xs[rt], a.ys[rt], a.zs[rt], a.fs[rt], X1r, Y1r);
@@ -56,11 +56,13 @@ __global__ void k_qcalc_plane(const QPlaneArgs a) {
         face_xy(a.xe[dn], a.ye[dn], a.ze[dn], a.fe[dn], X2d, Y2d);
         face_xy(a.xe[rt], a.ye[rt], a.ze[rt], a.fe[rt], X2r, Y2r);
         face_xy(a.xe[lf], a.ye[lf], a.ze[lf], a.fe[lf], X2l, Y2l);
-        // central differences along axis 0 ("xc") and axis 1 ("yc")
-        const T dx2xc = X2u - X2d, dx2yc = X2r - X2l;
-        const T dy2xc = Y2u - Y2d, dy2yc = Y2r - Y2l;
-        const T dx1xc = X1u - X1d, dx1yc = X1r - X1l;
-        const T dy1xc = Y1u - Y1d, dy1yc = Y1r - Y1l;
+        // central differences along axis 0 ("xc") and axis 1 ("yc"), taken in
+        // float as the reference takes them (the FP64 form widens the
+        // differences, exact in most cells, before the Jacobian products)
+        const T dx2xc = (T)(X2u - X2d), dx2yc = (T)(X2r - X2l);
+        const T dy2xc = (T)(Y2u - Y2d), dy2yc = (T)(Y2r - Y2l);
+        const T dx1xc = (T)(X1u - X1d), dx1yc = (T)(X1r - X1l);
+        const T dy1xc = (T)(Y1u - Y1d), dy1yc = (T)(Y1r - Y1l);
         const T qa = dx2xc * dy1yc - dx2yc * dy1xc;
         const T qb = dx2yc * dx1xc - dx2xc * dx1yc;
         const T qc = dy2xc * dy1yc - dy2yc * dy1xc;
