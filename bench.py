@@ -582,6 +582,19 @@ def main():
                      "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
                              f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
     }
+    # Secondary roofline in FP32 flops: 75 per normalised field sample (18
+    # weights, 24 FMA, 9 to normalise) plus 130 per RKF45 step for the
+    # combine and error estimate, one step per 6 samples.  The peak is
+    # nominal (152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz); no measured
+    # FP32 figure exists for this GPU.
+    flops = res["samples_main"] * (75.0 + 130.0 / 6.0)
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    line["roofline"]["flops"] = {"achieved": flops / (res["k_ms"] / 1e3) / 1e12, "peak": fp32_peak,
+                                 "unit": "TFLOP/s", "frac": flops / (res["k_ms"] / 1e3) / 1e12 / fp32_peak,
+                                 "peak_kind": "nominal"}
+    line["roofline"]["limiter"] = ("SM issue and the L1 data pipe together (ncu on 32 mid-cube planes: "
+                                   "issue active 80.9 %, L1 LSU wavefronts 80.7 % of peak); the field "
+                                   "gathers hit L1 (96.7 %) and L2, so the HBM frac exceeds 1")
     # launches per step: main trace, qcalc, flag_count, tile_scan, cook_write,
     # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
     line["gpu_launches"] = 8 * args.steps
