@@ -415,6 +415,109 @@ def make_requests(fields_shape, names, count, rate, seed=0, seeds_range=(1e4, 4e
     return out
 
 
+# --------------------------------------------------------------------------
+# An ideal scheduler on the same request stream: the bound on what any
+# scheduler of this server could reach
+# --------------------------------------------------------------------------
+
+def fluid_schedule(arrival, work, cap, capacity=1.0, policy="srpt"):
+    """Completion times of jobs on a fluid server of `capacity` work units
+    per second with free, instant preemption: job i arrives at arrival[i],
+    needs work[i] units and runs at most cap[i] units per second (its rate
+    when alone).  Policies share the capacity among the jobs present:
+    'srpt' (least remaining work first, each up to its cap), 'ps' (equal
+    shares, water-filled over the caps) or 'fcfs' (oldest first, up to its
+    cap).  Returns an array of completion times."""
+    arrival = np.asarray(arrival, float)
+    work = np.asarray(work, float)
+    cap = np.asarray(cap, float)
+    n = len(arrival)
+    if n == 0:
+        return np.zeros(0)
+    if np.any(work < 0) or np.any(cap <= 0) or capacity <= 0:
+        raise ValueError("work must be >= 0 and caps and capacity > 0")
+    order = np.argsort(arrival, kind="stable")
+    rem = work.copy()
+    done = np.full(n, np.nan)
+    active = []
+    nxt = 0
+    t = float(arrival[order[0]])
+    while nxt < n or active:
+        while nxt < n and arrival[order[nxt]] <= t:
+            i = int(order[nxt])
+            nxt += 1
+            if rem[i] <= 0:
+                done[i] = arrival[i]
+            else:
+                active.append(i)
+        if not active:
+            t = float(arrival[order[nxt]])
+            continue
+        rate = {}
+        if policy == "ps":
+            left, pending = capacity, sorted(active, key=lambda j: cap[j])
+            while pending:
+                share = left / len(pending)
+                j = pending[0]
+                if cap[j] <= share:
+                    rate[j] = cap[j]
+                    left -= cap[j]
+                    pending.pop(0)
+                else:
+                    for k in pending:
+                        rate[k] = share
+                    break
+        else:
+            key = (lambda j: (rem[j], arrival[j], j)) if policy == "srpt" else (lambda j: (arrival[j], j))
+            if policy not in ("srpt", "fcfs"):
+                raise ValueError(f"unknown policy {policy!r}")
+            left = capacity
+            for j in sorted(active, key=key):
+                rate[j] = min(cap[j], left)
+                left -= rate[j]
+        dt_done = min((rem[j] / rate[j] for j in active if rate[j] > 0), default=np.inf)
+        dt_arr = arrival[order[nxt]] - t if nxt < n else np.inf
+        dt = min(dt_done, dt_arr)
+        for j in active:
+            rem[j] -= rate[j] * dt
+        t += dt
+        still = []
+        for j in active:
+            if rem[j] <= 1e-9 * work[j]:  # remaining work within rounding of zero
+                done[j] = t
+            else:
+                still.append(j)
+        active = still
+    return done
+
+
+def ideal_bound(requests, isolated, saturated_span, policies=("srpt", "ps")):
+    """p50/p99 of latency / isolated solve that an ideal fluid scheduler
+    (free preemption, perfect sharing of the GPU) reaches on `requests`.
+
+    A request's work is its Q-pixels times the GPU time per Q-pixel of the
+    most efficient isolated solve at its tolerance (the largest requests fill
+    the GPU, so theirs is the full-GPU cost); its rate when alone is
+    work / isolated (small requests cannot fill the GPU).  The capacity is
+    the work of the whole set over the span the server took to finish it
+    when all were submitted at once, so the offered load of the stream is
+    the same fraction of capacity as the measured stream's."""
+    tpx = {}
+    for r in requests:
+        c = isolated[r.rid] / r.qpixels
+        tpx[r.tol] = min(tpx.get(r.tol, np.inf), c)
+    work = np.array([r.qpixels * tpx[r.tol] for r in requests])
+    iso = np.array([isolated[r.rid] for r in requests])
+    cap = work / iso
+    capacity = work.sum() / saturated_span
+    arrival = np.array([r.arrival for r in requests])
+    out = {}
+    for pol in policies:
+        ratio = (fluid_schedule(arrival, work, cap, capacity, pol) - arrival) / iso
+        out[pol] = [float(np.percentile(ratio, 50)), float(np.percentile(ratio, 99))]
+    return out
+
+
 def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6),
           batched_server: QServer | None = None):
     """Isolated solve of every request, the saturated throughput (all
@@ -438,6 +541,8 @@ def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7,
         reqs = make_requests(fields_shape, names, count, f * sat_rate, seed=seed, seeds_range=seeds_range)
         done = server.run_stream(reqs)
         st = dict(latency_stats(done, iso), offered_req_per_s=f * sat_rate)
+        # what an ideal fluid scheduler reaches on the same stream: [p50, p99]
+        st["ideal_fluid_p50_p99_over_isolated"] = ideal_bound(reqs, iso, span)
         for c in range(len(server.classes)):
             rr = [r.latency / iso[r.rid] for r in done if r.meta["class"] == c]
             if rr:
