@@ -508,13 +508,20 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     };
     const FieldStretch f{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
                          make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    if (prm->arith != QSL_ARITH_FAST) return go(f);
+    const int64_t cells = (int64_t)(nx - 1) + (ny - 1) + (nz - 1);
+    if (prm->arith != QSL_ARITH_FAST || cells * (1 + STRETCH_BINS_PER_CELL) >= (1LL << 31)) return go(f);
     // fast arithmetic: the nodes interleaved into a stream-ordered float4
-    // copy for the launch (one 16-byte load per corner; the same values)
+    // copy for the launch (one 16-byte load per corner; the same values),
+    // followed by the search tables (a 16-byte record per cell, an int2
+    // range per bin)
     const int64_t nodes = (int64_t)nx * ny * nz;
+    const size_t bytes = (size_t)(nodes + cells) * sizeof(float4) + (size_t)cells * STRETCH_BINS_PER_CELL * sizeof(int2);
     float4* b4 = nullptr;
-    QSL_CHECK_CUDA(cudaMallocAsync((void**)&b4, (size_t)nodes * sizeof(float4), st), "node copy allocation");
+    QSL_CHECK_CUDA(cudaMallocAsync((void**)&b4, bytes, st), "node copy allocation");
+    float4* srec = b4 + nodes;
+    int2* sbin = reinterpret_cast<int2*>(srec + cells);
     cudaError_t e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
+    if (e == cudaSuccess) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {
         cudaFreeAsync(b4, st);
         return cuda_fail(e, "node copy");
@@ -531,6 +538,9 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     fp.uni = f.uni;
     fp.lo = fp.hi = fp.clo = fp.chi = fp.us = make_float3(0.f, 0.f, 0.f);
     fp.b4 = b4;
+    fp.srec = srec;
+    fp.sbin = sbin;
+    fp.sbinv = make_float3(0.f, 0.f, 0.f);
     const int rc = go(fp);
     cudaFreeAsync(b4, st);
     return rc;

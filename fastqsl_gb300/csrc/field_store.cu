@@ -19,6 +19,62 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
     return cudaGetLastError();
 }
 
+// Search tables of a stretched grid (FieldStretchP::srec / sbin), all three
+// axes in one launch: one thread per cell and per bin.
+//  * cell j: the reference's search at c = a[j+1] (its comparisons c > a[m]
+//    come out the same for every c in (a[j], a[j+1]], and it never compares
+//    with a[0], so a coordinate pinned at a[0] gets cell 0's answer too);
+//  * bin b: the cells of its edges moved out by 1 % of a bin (in double),
+//    each the largest j <= n-2 with a[j] below the edge (0 if none).  A
+//    coordinate the kernel puts in bin b lies within those edges, so its
+//    interval is in the range.
+__device__ __forceinline__ int stretch_cell_below(double c, int n, const float* __restrict__ a) {
+    int lo = 0, hi = n - 2;  // largest j in [0, n-2] with a[j] < c, else 0
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((double)__ldg(a + mid) < c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_stretch_tables(const float* __restrict__ ax, const float* __restrict__ ay,
+                                 const float* __restrict__ az, Dims d, float4* __restrict__ srec,
+                                 int2* __restrict__ sbin) {
+    const int cells = (d.nx - 1) + (d.ny - 1) + (d.nz - 1);
+    const int bins = STRETCH_BINS_PER_CELL * cells;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells + bins; t += gridDim.x * blockDim.x) {
+        const bool is_bin = t >= cells;
+        const int u = is_bin ? (t - cells) / STRETCH_BINS_PER_CELL : t;  // cell index over the three axes
+        const int k = u < d.nx - 1 ? 0 : (u < d.nx + d.ny - 2 ? 1 : 2);
+        const float* a = k == 0 ? ax : (k == 1 ? ay : az);
+        const int n = d.n(k);
+        const int c0 = stretch_cell_offset(d, k);
+        if (!is_bin) {
+            const int j = u - c0;
+            const int i = stretch_bisect(__ldg(a + j + 1), n, a);
+            const float ai = __ldg(a + i);
+            srec[t] = make_float4(ai, __ldg(a + i + 1) - ai, __int_as_float(i), 0.f);
+        } else {
+            const int b = t - cells - STRETCH_BINS_PER_CELL * c0;
+            const int nb = STRETCH_BINS_PER_CELL * (n - 1);
+            const double a0 = __ldg(a), w = ((double)__ldg(a + n - 1) - a0) / nb;
+            const int lo = stretch_cell_below(a0 + (b - 0.01) * w, n, a);
+            const int hi = stretch_cell_below(a0 + (b + 1.01) * w, n, a);
+            sbin[t - cells] = make_int2(lo, hi < lo ? lo : hi);
+        }
+    }
+}
+
+cudaError_t launch_stretch_tables(const float* ax, const float* ay, const float* az, Dims d, float4* srec,
+                                  int2* sbin, cudaStream_t st) {
+    const long long total = (long long)(1 + STRETCH_BINS_PER_CELL) * ((d.nx - 1) + (d.ny - 1) + (d.nz - 1));
+    long long g = (total + 255) / 256;
+    if (g > 4096) g = 4096;
+    k_stretch_tables<<<(unsigned)g, 256, 0, st>>>(ax, ay, az, d, srec, sbin);
+    return cudaGetLastError();
+}
+
 // One block per brick: the brick's 9^3 nodes (clamped to the grid at the far
 // faces) are scaled by the largest |component| in the brick and rounded to
 // fp16, and written as x-pair records.  The scale is the brick's multiplier

@@ -51,6 +51,15 @@ __device__ __forceinline__ float norm_fast(float3 a) {
     asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(fmaf(a.x, a.x, fmaf(a.y, a.y, a.z * a.z))));
     return r;
 }
+// x / y as x times the hardware reciprocal approximation (rcp.approx.f32,
+// relative error ~2^-23), the product rounded on its own (__fmul_rn is never
+// merged into a fused multiply-add), so that every kernel that inlines it
+// gets the same bits
+__device__ __forceinline__ float div_fast(float x, float y) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(y));
+    return __fmul_rn(x, r);
+}
 __device__ __forceinline__ float comp(float3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }
 __device__ __forceinline__ float fcomp(const float* a, int d) { return a[d]; }
 
@@ -187,7 +196,9 @@ struct FieldH8C {
 // kernel start from the coordinate arrays).
 // PACKED: the node values come from an interleaved float4 copy (b4: one
 // 16-byte load per corner instead of three 4-byte gathers; the same float
-// values, so the same results).
+// values, so the same results), and the search uses per-axis tables (srec,
+// sbin; built by launch_stretch_tables) that give the reference search's own
+// cell for every coordinate in two dependent loads instead of ~log2(n).
 template <bool PACKED>
 struct FieldStretchT {
     const float* bx;
@@ -203,6 +214,17 @@ struct FieldStretchT {
     float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
     float3 us;            // uniform-formula spacing (hi - lo) / n
     const float4* b4;     // PACKED: Bx, By, Bz, 0 per node, x fastest
+    // PACKED search tables, axes x, y, z one after another (axis k starts at
+    // cell offset stretch_cell_offset(k)):
+    //   srec[j]  the cell the reference's search gives for any coordinate in
+    //            (a[j], a[j+1]] and its first coordinate and width:
+    //            {a[i], a[i+1] - a[i], i as int bits, 0}
+    //   sbin[b]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins over [a[0],
+    //            a[n-1]] per axis: the lowest and highest cell a coordinate
+    //            of the bin (widened by 1 % of a bin) can lie in
+    const float4* srec;
+    const int2* sbin;
+    float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (PACKED) {
             const FieldF4 s{b4, d};
@@ -216,6 +238,12 @@ struct FieldStretchT {
 };
 using FieldStretch = FieldStretchT<false>;
 using FieldStretchP = FieldStretchT<true>;
+
+constexpr int STRETCH_BINS_PER_CELL = 4;
+// first table cell of axis k (0, 1, 2) for node counts d
+__host__ __device__ __forceinline__ int stretch_cell_offset(const Dims& d, int k) {
+    return k == 0 ? 0 : (k == 1 ? d.nx - 1 : d.nx + d.ny - 2);
+}
 
 // ---------------------------------------------------------------------------
 // Cell location with the reference's face pinning (Interp3dxyzn,
@@ -567,28 +595,66 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
     return r > n - 2 ? n - 2 : r;
 }
 
+// The reference search's cell for c through the tables of a packed store
+// (FieldStretchP): the bin of c gives the range of cells c can lie in
+// (usually one, else a few), a bisection over that range the cell j with
+// a[j] < c <= a[j+1] (or the range's low end), and srec[j] the cell the
+// reference's search returns for every coordinate of that interval (its
+// comparisons are all of the form c > a[m]), with that cell's first
+// coordinate and width.  The same cell, coordinate and width as
+// stretch_bisect followed by the two coordinate loads, for c clamped as
+// stretch_locate clamps it.
+template <bool P>
+__device__ __forceinline__ int stretch_table(const FieldStretchT<P>& f, int k, float c, float a0, float binv,
+                                             float& ai, float& di) {
+    const float* a = f.axis(k);
+    const int n = f.d.n(k);
+    const int c0 = stretch_cell_offset(f.d, k);
+    const int nb = STRETCH_BINS_PER_CELL * (n - 1);
+    int b = __float2int_rz((c - a0) * binv);
+    b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
+    const int2 range = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
+    int lo = range.x, hi = range.y;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (c > __ldg(a + mid)) lo = mid;
+        else hi = mid - 1;
+    }
+    const float4 rec = __ldg(f.srec + c0 + lo);
+    ai = rec.x;
+    di = rec.y;
+    return __float_as_int(rec.z);
+}
+
 // Cell and fraction along one axis: c clamped to (a[0] + 1e-6, a[n-1] - 1e-6)
 // (offsets applied in double and narrowed, once per kernel: clo, chi), then
-// the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122).
-template <bool P>
+// the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122);
+// the fast arithmetic divides with the hardware reciprocal (div_fast).
+template <bool EXACT, bool P>
 __device__ __forceinline__ void stretch_locate(const FieldStretchT<P>& f, int k, float c, float a0, float an,
-                                               float clo, float chi, float du, int& i, float& r) {
+                                               float clo, float chi, float du, float binv, int& i, float& r) {
     const float* a = f.axis(k);
     const int n = f.d.n(k);
     c = (c > a0) ? c : clo;
     c = (c < an) ? c : chi;
-    i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
-    const float ai = __ldg(a + i);
-    r = (c - ai) / (__ldg(a + i + 1) - ai);
+    float ai, di;
+    if (P && !f.uni) {
+        i = stretch_table(f, k, c, a0, binv, ai, di);
+    } else {
+        i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
+        ai = __ldg(a + i);
+        di = __ldg(a + i + 1) - ai;
+    }
+    r = EXACT ? (c - ai) / di : div_fast(__fsub_rn(c, ai), di);
 }
 
 template <bool EXACT, bool P>
 __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<P>& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
-    stretch_locate(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, ix, rx);
-    stretch_locate(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, iy, ry);
-    stretch_locate(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, iz, rz);
+    stretch_locate<EXACT>(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, f.sbinv.x, ix, rx);
+    stretch_locate<EXACT>(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, f.sbinv.y, iy, ry);
+    stretch_locate<EXACT>(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, f.sbinv.z, iz, rz);
     float w[8];
     if (EXACT) weights_exact(rx, ry, rz, w);
     else weights_fast(rx, ry, rz, w);

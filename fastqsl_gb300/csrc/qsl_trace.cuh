@@ -268,6 +268,13 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<P>& f) {
     f.us = v3((f.hi.x - f.lo.x) / __int2float_rd(f.d.nx), (f.hi.y - f.lo.y) / __int2float_rd(f.d.ny),
               (f.hi.z - f.lo.z) / __int2float_rd(f.d.nz));
     if (f.uni_dev) f.uni = *f.uni_dev ? 1 : 0;
+    if constexpr (P) {
+        // the bin width of the search tables (only picks the bin; the
+        // tables' ranges absorb its rounding)
+        f.sbinv = v3((float)(STRETCH_BINS_PER_CELL * (f.d.nx - 1)) / (f.hi.x - f.lo.x),
+                     (float)(STRETCH_BINS_PER_CELL * (f.d.ny - 1)) / (f.hi.y - f.lo.y),
+                     (float)(STRETCH_BINS_PER_CELL * (f.d.nz - 1)) / (f.hi.z - f.lo.z));
+    }
 }
 // (the current density is always the caller's arrays: an unpacked view)
 template <bool P>
@@ -288,6 +295,9 @@ __device__ __forceinline__ FieldStretch current_view(const FieldStretchT<P>& f, 
     r.chi = f.chi;
     r.us = f.us;
     r.b4 = nullptr;
+    r.srec = nullptr;
+    r.sbin = nullptr;
+    r.sbinv = make_float3(0.f, 0.f, 0.f);
     return r;
 }
 
@@ -296,6 +306,19 @@ __device__ __forceinline__ FieldStretch current_view(const FieldStretchT<P>& f, 
 // rounding boundary).  The exact kernels use it so that the step controller's
 // decisions do not depend on one library's powf rounding.
 __device__ __forceinline__ float pow_cr(float x, float y) { return (float)pow((double)x, (double)y); }
+
+// J.B / |B|^2, the twist integrand.  The fast form fixes its rounding
+// sequence with explicit multiply-adds: left as plain expressions, the
+// compiler is free to fuse the products in an order that depends on the code
+// around them, and two kernels tracing the same line would then differ in
+// the last bit.  (The exact form is compiled without fusion.)
+template <bool EXACT>
+__device__ __forceinline__ float twist_density(float3 j, float3 b) {
+    if (EXACT) return dot(j, b) / dot(b, b);
+    const float jb = fmaf(j.z, b.z, fmaf(j.y, b.y, __fmul_rn(j.x, b.x)));
+    const float bb = fmaf(b.z, b.z, fmaf(b.y, b.y, __fmul_rn(b.x, b.x)));
+    return jb / bb;
+}
 
 // Per-lane state of one direction of one line.  The length accumulates in
 // double for exact arithmetic (as the reference does) and in Kahan-
@@ -443,7 +466,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
             b1 = b_at_p;
             ns += 1;
         }
-        td = dot(j1, b1) / dot(b1, b1);
+        td = twist_density<EXACT>(j1, b1);
         L.tw = L.tw + (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
     }
     // inside test first: the full face classification only runs on exit
@@ -476,7 +499,7 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
                 L.out = L.p;
             }
             if (TWIST && tw_on && pr.boundary_twist) {
-                L.tw = L.tw + (double)(dot(j1, b1) / dot(b1, b1)) / 4.0 / kRefPi * (double)fabsf(qmid - q1) /
+                L.tw = L.tw + (double)twist_density<EXACT>(j1, b1) / 4.0 / kRefPi * (double)fabsf(qmid - q1) /
                                   (1e-4 + (double)fabsf(comp(b1, d)));
             }
         } else {

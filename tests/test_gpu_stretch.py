@@ -127,13 +127,14 @@ def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
     assert int(samples.item()) > 6 * len(xs)
 
 
-@pytest.mark.parametrize("uni,twist", [(False, False), (True, True)])
+@pytest.mark.parametrize("uni,twist", [(False, False), (True, True), (False, True)])
 def test_native_fast_packed_equals_dropin_fast(cuda, uni, twist):
     """The native stretched entry in fast arithmetic reads the nodes from an
-    interleaved float4 copy, the drop-in from the caller's three arrays: the
-    same float values through the same arithmetic, so every output is the
-    same bit for bit (twist included: the current stays the caller's
-    arrays)."""
+    interleaved float4 copy and finds cells through its search tables, the
+    drop-in reads the caller's three arrays and runs the reference's
+    search: the same float values, the same cells and the same arithmetic,
+    so every output is the same bit for bit (twist included: the current
+    stays the caller's arrays)."""
     from fastqsl_gb300 import api, synthetic as S
     spec = S.bipole4_stretch(7)
     coords = S.stretched_axes(spec.shape, z_ratio=1.0 if uni else 1.05)
