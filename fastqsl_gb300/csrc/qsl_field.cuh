@@ -641,7 +641,10 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<P>& f, int k,
     if (P && !f.uni) {
         i = stretch_table(f, k, c, a0, binv, ai, di);
     } else {
-        i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
+        // (a packed store never runs the search: its copy of the loop is
+        // left out of every inlined sample, which keeps the loop body small
+        // for the instruction cache)
+        i = (P || f.uni) ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
         ai = __ldg(a + i);
         di = __ldg(a + i + 1) - ai;
     }
