@@ -432,10 +432,14 @@ def fluid_schedule(arrival, work, cap, capacity=1.0, policy="srpt"):
     work = np.asarray(work, float)
     cap = np.asarray(cap, float)
     n = len(arrival)
-    if n == 0:
-        return np.zeros(0)
+    if policy not in ("srpt", "ps", "fcfs"):
+        raise ValueError(f"unknown policy {policy!r}")
+    if not (len(work) == len(cap) == n):
+        raise ValueError("arrival, work and cap differ in length")
     if np.any(work < 0) or np.any(cap <= 0) or capacity <= 0:
         raise ValueError("work must be >= 0 and caps and capacity > 0")
+    if n == 0:
+        return np.zeros(0)
     order = np.argsort(arrival, kind="stable")
     rem = work.copy()
     done = np.full(n, np.nan)
@@ -469,8 +473,6 @@ def fluid_schedule(arrival, work, cap, capacity=1.0, policy="srpt"):
                     break
         else:
             key = (lambda j: (rem[j], arrival[j], j)) if policy == "srpt" else (lambda j: (arrival[j], j))
-            if policy not in ("srpt", "fcfs"):
-                raise ValueError(f"unknown policy {policy!r}")
             left = capacity
             for j in sorted(active, key=key):
                 rate[j] = min(cap[j], left)

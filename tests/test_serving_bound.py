@@ -60,6 +60,10 @@ def test_rejects_bad_inputs():
         fluid_schedule([0.0], [1.0], [0.0])
     with pytest.raises(ValueError):
         fluid_schedule([0.0], [1.0], [1.0], policy="lifo")
+    with pytest.raises(ValueError):
+        fluid_schedule([], [], [], policy="lifo")
+    with pytest.raises(ValueError):
+        fluid_schedule([0.0, 1.0], [1.0], [1.0, 1.0])
     assert len(fluid_schedule([], [], [])) == 0
 
 
