@@ -291,6 +291,8 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
         e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldStretchP>::value) {
         e = launch_trace_fast_stretch_packed(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldStretchPU>::value) {
+        e = launch_trace_fast_stretch_packed_uni(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldStretch>::value) {
         e = arith == QSL_ARITH_EXACT ? launch_trace_exact_stretch(J, twist, sched, n_host, st)
                                      : launch_trace_fast_stretch(J, twist, sched, n_host, st);
@@ -512,36 +514,40 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (prm->arith != QSL_ARITH_FAST || cells * (1 + STRETCH_BINS_PER_CELL) >= (1LL << 31)) return go(f);
     // fast arithmetic: the nodes interleaved into a stream-ordered float4
     // copy for the launch (one 16-byte load per corner; the same values),
-    // followed by the search tables (a 16-byte record per cell, an int2
-    // range per bin)
+    // followed, for the search, by its tables (a 16-byte record per cell, an
+    // int2 range per bin); the uniform formula needs none
     const int64_t nodes = (int64_t)nx * ny * nz;
-    const size_t bytes = (size_t)(nodes + cells) * sizeof(float4) + (size_t)cells * STRETCH_BINS_PER_CELL * sizeof(int2);
+    const int64_t tcells = uni ? 0 : cells;
+    const size_t bytes =
+        (size_t)(nodes + tcells) * sizeof(float4) + (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int2);
     float4* b4 = nullptr;
     QSL_CHECK_CUDA(cudaMallocAsync((void**)&b4, bytes, st), "node copy allocation");
-    float4* srec = b4 + nodes;
-    int2* sbin = reinterpret_cast<int2*>(srec + cells);
+    float4* srec = uni ? nullptr : b4 + nodes;
+    int2* sbin = uni ? nullptr : reinterpret_cast<int2*>(srec + cells);
     cudaError_t e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
-    if (e == cudaSuccess) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
+    if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {
         cudaFreeAsync(b4, st);
         return cuda_fail(e, "node copy");
     }
-    FieldStretchP fp;
-    fp.bx = Bx;
-    fp.by = By;
-    fp.bz = Bz;
-    fp.d = f.d;
-    fp.ax = x_arr;
-    fp.ay = y_arr;
-    fp.az = z_arr;
-    fp.uni_dev = nullptr;
-    fp.uni = f.uni;
-    fp.lo = fp.hi = fp.clo = fp.chi = fp.us = make_float3(0.f, 0.f, 0.f);
-    fp.b4 = b4;
-    fp.srec = srec;
-    fp.sbin = sbin;
-    fp.sbinv = make_float3(0.f, 0.f, 0.f);
-    const int rc = go(fp);
+    auto packed = [&](auto fp) {
+        fp.bx = Bx;
+        fp.by = By;
+        fp.bz = Bz;
+        fp.d = f.d;
+        fp.ax = x_arr;
+        fp.ay = y_arr;
+        fp.az = z_arr;
+        fp.uni_dev = nullptr;
+        fp.uni = f.uni;
+        fp.lo = fp.hi = fp.clo = fp.chi = fp.us = make_float3(0.f, 0.f, 0.f);
+        fp.b4 = b4;
+        fp.srec = srec;
+        fp.sbin = sbin;
+        fp.sbinv = make_float3(0.f, 0.f, 0.f);
+        return go(fp);
+    };
+    const int rc = uni ? packed(FieldStretchPU{}) : packed(FieldStretchP{});
     cudaFreeAsync(b4, st);
     return rc;
 }

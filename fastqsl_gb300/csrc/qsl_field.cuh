@@ -194,12 +194,16 @@ struct FieldH8C {
 // ay[ny], az[nz].  uni selects the reference's uniform-spacing index formula
 // instead of its search; lo/hi are the first and last coordinates (set at
 // kernel start from the coordinate arrays).
-// PACKED: the node values come from an interleaved float4 copy (b4: one
-// 16-byte load per corner instead of three 4-byte gathers; the same float
-// values, so the same results), and the search uses per-axis tables (srec,
-// sbin; built by launch_stretch_tables) that give the reference search's own
-// cell for every coordinate in two dependent loads instead of ~log2(n).
-template <bool PACKED>
+// M (mode): 0 = the caller's arrays, the search or the formula as uni says
+// at run time (the drop-in); 1 and 2 = packed: the node values come from an
+// interleaved float4 copy (b4: one 16-byte load per corner instead of three
+// 4-byte gathers; the same float values, so the same results), and the cell
+// search is fixed at compile time, so each inlined sample carries one search
+// only (the loop body is instruction-fetch bound): 1 = per-axis tables
+// (srec, sbin; built by launch_stretch_tables) that give the reference
+// search's own cell for every coordinate in two dependent loads instead of
+// ~log2(n); 2 = the uniform-spacing formula.
+template <int M>
 struct FieldStretchT {
     const float* bx;
     const float* by;
@@ -213,8 +217,8 @@ struct FieldStretchT {
     float3 lo, hi;        // first and last node coordinates (read at kernel start)
     float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
     float3 us;            // uniform-formula spacing (hi - lo) / n
-    const float4* b4;     // PACKED: Bx, By, Bz, 0 per node, x fastest
-    // PACKED search tables, axes x, y, z one after another (axis k starts at
+    const float4* b4;     // packed: Bx, By, Bz, 0 per node, x fastest
+    // search tables (M = 1), axes x, y, z one after another (axis k starts at
     // cell offset stretch_cell_offset(k)):
     //   srec[j]  the cell the reference's search gives for any coordinate in
     //            (a[j], a[j+1]] and its first coordinate and width:
@@ -226,7 +230,7 @@ struct FieldStretchT {
     const int2* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
-        if constexpr (PACKED) {
+        if constexpr (M != 0) {
             const FieldF4 s{b4, d};
             return s.corners(ix, iy, iz, c);
         } else {
@@ -236,8 +240,9 @@ struct FieldStretchT {
     }
     __device__ __forceinline__ const float* axis(int k) const { return k == 0 ? ax : (k == 1 ? ay : az); }
 };
-using FieldStretch = FieldStretchT<false>;
-using FieldStretchP = FieldStretchT<true>;
+using FieldStretch = FieldStretchT<0>;
+using FieldStretchP = FieldStretchT<1>;
+using FieldStretchPU = FieldStretchT<2>;
 
 constexpr int STRETCH_BINS_PER_CELL = 4;
 // first table cell of axis k (0, 1, 2) for node counts d
@@ -604,8 +609,8 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
 // coordinate and width.  The same cell, coordinate and width as
 // stretch_bisect followed by the two coordinate loads, for c clamped as
 // stretch_locate clamps it.
-template <bool P>
-__device__ __forceinline__ int stretch_table(const FieldStretchT<P>& f, int k, float c, float a0, float binv,
+template <int M>
+__device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, float c, float a0, float binv,
                                              float& ai, float& di) {
     const float* a = f.axis(k);
     const int n = f.d.n(k);
@@ -630,29 +635,27 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<P>& f, int k, f
 // (offsets applied in double and narrowed, once per kernel: clo, chi), then
 // the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122);
 // the fast arithmetic divides with the hardware reciprocal (div_fast).
-template <bool EXACT, bool P>
-__device__ __forceinline__ void stretch_locate(const FieldStretchT<P>& f, int k, float c, float a0, float an,
+template <bool EXACT, int M>
+__device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k, float c, float a0, float an,
                                                float clo, float chi, float du, float binv, int& i, float& r) {
     const float* a = f.axis(k);
     const int n = f.d.n(k);
     c = (c > a0) ? c : clo;
     c = (c < an) ? c : chi;
     float ai, di;
-    if (P && !f.uni) {
+    if constexpr (M == 1) {
         i = stretch_table(f, k, c, a0, binv, ai, di);
     } else {
-        // (a packed store never runs the search: its copy of the loop is
-        // left out of every inlined sample, which keeps the loop body small
-        // for the instruction cache)
-        i = (P || f.uni) ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
+        if constexpr (M == 2) i = stretch_uni(c, n, a0, du);
+        else i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
         ai = __ldg(a + i);
         di = __ldg(a + i + 1) - ai;
     }
     r = EXACT ? (c - ai) / di : div_fast(__fsub_rn(c, ai), di);
 }
 
-template <bool EXACT, bool P>
-__device__ __forceinline__ float3 sample_stretch(const FieldStretchT<P>& f, float3 p, bool unit) {
+template <bool EXACT, int M>
+__device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
     stretch_locate<EXACT>(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, f.sbinv.x, ix, rx);
@@ -686,6 +689,10 @@ __device__ __forceinline__ float3 sample<false, FieldStretch>(const FieldStretch
 }
 template <>
 __device__ __forceinline__ float3 sample<false, FieldStretchP>(const FieldStretchP& f, float3 p, bool unit) {
+    return sample_stretch<false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldStretchPU>(const FieldStretchPU& f, float3 p, bool unit) {
     return sample_stretch<false>(f, p, unit);
 }
 
@@ -753,6 +760,10 @@ __device__ __forceinline__ float3 sample_endpoint<false, FieldStretch>(const Fie
 }
 template <>
 __device__ __forceinline__ float3 sample_endpoint<false, FieldStretchP>(const FieldStretchP& f, float3 p) {
+    return sample_stretch<false>(f, p, false);
+}
+template <>
+__device__ __forceinline__ float3 sample_endpoint<false, FieldStretchPU>(const FieldStretchPU& f, float3 p) {
     return sample_stretch<false>(f, p, false);
 }
 

@@ -29,6 +29,9 @@ cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twis
                                       cudaStream_t st);
 cudaError_t launch_trace_fast_stretch_packed(const TraceJob<FieldStretchP>& J, bool twist, Schedule sched,
                                              long long n_host, cudaStream_t st);
+// trace_fast_stretch_packed_uni.cu
+cudaError_t launch_trace_fast_stretch_packed_uni(const TraceJob<FieldStretchPU>& J, bool twist, Schedule sched,
+                                                 long long n_host, cudaStream_t st);
 
 // trace_fast_<store>.cu
 cudaError_t launch_trace_fast_soa(const TraceJob<FieldSoA>& J, bool twist, Schedule sched, long long n_host,

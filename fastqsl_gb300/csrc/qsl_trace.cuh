@@ -234,13 +234,13 @@ __device__ __forceinline__ FieldSoA current_view(const F& f, const FieldSoA& c) 
 
 // Stretched grid (checkFlag, TraceBlineAdaptiveStretch.cu:309-331): the same
 // tests against the first and last node coordinates.
-template <bool P>
-__device__ __forceinline__ bool box_inside(const FieldStretchT<P>& f, float3 p) {
+template <int M>
+__device__ __forceinline__ bool box_inside(const FieldStretchT<M>& f, float3 p) {
     return (p.x >= f.lo.x) & (p.y > f.lo.y) & (p.z >= f.lo.z) & (p.x <= f.hi.x) & (p.y <= f.hi.y) &
            (p.z <= f.hi.z);
 }
-template <bool P>
-__device__ __forceinline__ int box_exit(const FieldStretchT<P>& f, float3 p) {
+template <int M>
+__device__ __forceinline__ int box_exit(const FieldStretchT<M>& f, float3 p) {
     const float3 a = f.lo, b = f.hi;
     if ((p.x >= a.x) & (p.y > a.y) & (p.z >= a.z) & (p.x <= b.x) & (p.y <= b.y) & (p.z <= b.z)) return 0;
     int r = 42;
@@ -253,12 +253,12 @@ __device__ __forceinline__ int box_exit(const FieldStretchT<P>& f, float3 p) {
     return r;
 }
 // the summed coordinate extents, in float as the reference (:337-339)
-template <bool P>
-__device__ __forceinline__ double len_scale(const FieldStretchT<P>& f) {
+template <int M>
+__device__ __forceinline__ double len_scale(const FieldStretchT<M>& f) {
     return (double)(((f.hi.x + f.hi.y) + f.hi.z) - ((f.lo.x + f.lo.y) + f.lo.z));
 }
-template <bool P>
-__device__ __forceinline__ void store_prepare(FieldStretchT<P>& f) {
+template <int M>
+__device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
     f.lo = v3(__ldg(f.ax), __ldg(f.ay), __ldg(f.az));
     f.hi = v3(__ldg(f.ax + f.d.nx - 1), __ldg(f.ay + f.d.ny - 1), __ldg(f.az + f.d.nz - 1));
     // per-sample constants of the cell search, formed once (the FP64 pipe
@@ -268,7 +268,7 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<P>& f) {
     f.us = v3((f.hi.x - f.lo.x) / __int2float_rd(f.d.nx), (f.hi.y - f.lo.y) / __int2float_rd(f.d.ny),
               (f.hi.z - f.lo.z) / __int2float_rd(f.d.nz));
     if (f.uni_dev) f.uni = *f.uni_dev ? 1 : 0;
-    if constexpr (P) {
+    if constexpr (M == 1) {
         // the bin width of the search tables (only picks the bin; the
         // tables' ranges absorb its rounding)
         f.sbinv = v3((float)(STRETCH_BINS_PER_CELL * (f.d.nx - 1)) / (f.hi.x - f.lo.x),
@@ -277,8 +277,8 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<P>& f) {
     }
 }
 // (the current density is always the caller's arrays: an unpacked view)
-template <bool P>
-__device__ __forceinline__ FieldStretch current_view(const FieldStretchT<P>& f, const FieldSoA& c) {
+template <int M>
+__device__ __forceinline__ FieldStretch current_view(const FieldStretchT<M>& f, const FieldSoA& c) {
     FieldStretch r;
     r.bx = c.bx;
     r.by = c.by;
@@ -534,7 +534,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     // only the drop-in stores (the caller's arrays) take their shape from the
     // device; the packed stores' dims stay kernel parameters
     if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value ||
-                  std::is_same<F, FieldStretchP>::value) {
+                  std::is_same<F, FieldStretchP>::value || std::is_same<F, FieldStretchPU>::value) {
         if (J.shape_dev) {
             f.d.nx = __ldg(J.shape_dev);
             f.d.ny = __ldg(J.shape_dev + 1);
