@@ -202,7 +202,9 @@ struct FieldH8C {
 // only (the loop body is instruction-fetch bound): 1 = per-axis tables
 // (srec, sbin; built by launch_stretch_tables) that give the reference
 // search's own cell for every coordinate in two dependent loads instead of
-// ~log2(n); 2 = the uniform-spacing formula.
+// ~log2(n); 2 = the uniform-spacing formula.  3 and 4 read the caller's
+// arrays with the search of 1 and 2 (the twist current density of a packed
+// launch, which stays in the caller's arrays).
 template <int M>
 struct FieldStretchT {
     const float* bx;
@@ -230,7 +232,7 @@ struct FieldStretchT {
     const int2* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
-        if constexpr (M != 0) {
+        if constexpr (M == 1 || M == 2) {
             const FieldF4 s{b4, d};
             return s.corners(ix, iy, iz, c);
         } else {
@@ -243,6 +245,9 @@ struct FieldStretchT {
 using FieldStretch = FieldStretchT<0>;
 using FieldStretchP = FieldStretchT<1>;
 using FieldStretchPU = FieldStretchT<2>;
+// the search a mode runs: 1 tables, 2 formula, 0 chosen at run time
+template <int M>
+constexpr int stretch_search_mode() { return M == 3 ? 1 : (M == 4 ? 2 : M); }
 
 constexpr int STRETCH_BINS_PER_CELL = 4;
 // first table cell of axis k (0, 1, 2) for node counts d
@@ -643,10 +648,10 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
     c = (c > a0) ? c : clo;
     c = (c < an) ? c : chi;
     float ai, di;
-    if constexpr (M == 1) {
+    if constexpr (stretch_search_mode<M>() == 1) {
         i = stretch_table(f, k, c, a0, binv, ai, di);
     } else {
-        if constexpr (M == 2) i = stretch_uni(c, n, a0, du);
+        if constexpr (stretch_search_mode<M>() == 2) i = stretch_uni(c, n, a0, du);
         else i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
         ai = __ldg(a + i);
         di = __ldg(a + i + 1) - ai;
@@ -693,6 +698,14 @@ __device__ __forceinline__ float3 sample<false, FieldStretchP>(const FieldStretc
 }
 template <>
 __device__ __forceinline__ float3 sample<false, FieldStretchPU>(const FieldStretchPU& f, float3 p, bool unit) {
+    return sample_stretch<false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldStretchT<3>>(const FieldStretchT<3>& f, float3 p, bool unit) {
+    return sample_stretch<false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldStretchT<4>>(const FieldStretchT<4>& f, float3 p, bool unit) {
     return sample_stretch<false>(f, p, unit);
 }
 

@@ -276,10 +276,12 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
                      (float)(STRETCH_BINS_PER_CELL * (f.d.nz - 1)) / (f.hi.z - f.lo.z));
     }
 }
-// (the current density is always the caller's arrays: an unpacked view)
+// The current density is always the caller's arrays: a view of them on the
+// store's grid that finds cells the way the store does (a packed store's
+// tables or formula, else the drop-in's run-time choice).
 template <int M>
-__device__ __forceinline__ FieldStretch current_view(const FieldStretchT<M>& f, const FieldSoA& c) {
-    FieldStretch r;
+__device__ __forceinline__ auto current_view(const FieldStretchT<M>& f, const FieldSoA& c) {
+    FieldStretchT<M == 1 ? 3 : (M == 2 ? 4 : 0)> r;
     r.bx = c.bx;
     r.by = c.by;
     r.bz = c.bz;
@@ -295,9 +297,9 @@ __device__ __forceinline__ FieldStretch current_view(const FieldStretchT<M>& f, 
     r.chi = f.chi;
     r.us = f.us;
     r.b4 = nullptr;
-    r.srec = nullptr;
-    r.sbin = nullptr;
-    r.sbinv = make_float3(0.f, 0.f, 0.f);
+    r.srec = f.srec;
+    r.sbin = f.sbin;
+    r.sbinv = f.sbinv;
     return r;
 }
 

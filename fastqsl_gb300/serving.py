@@ -34,6 +34,7 @@ thread with its job's settings; tests check alone == in the mix bit for bit).
 from __future__ import annotations
 
 import collections
+import gc
 import time
 from dataclasses import dataclass, field as dc_field
 
@@ -325,19 +326,28 @@ class QServer:
     # ---- a timed stream of requests ----
     def run_stream(self, requests, poll=2e-4):
         """Submits each request at its `arrival` time (seconds from now),
-        serving continuously; returns the requests in completion order."""
+        serving continuously; returns the requests in completion order.  The
+        cyclic garbage collector is held off while the stream runs (its
+        pauses would stall the scheduling loop) and run once at the end."""
         reqs = sorted(requests, key=lambda r: r.arrival)
-        t0 = time.perf_counter()
-        k = 0
-        self.done = []
-        while k < len(reqs) or not self.idle():
-            now = time.perf_counter()
-            while k < len(reqs) and t0 + reqs[k].arrival <= now:
-                self.submit(reqs[k], now=t0 + reqs[k].arrival)
-                k += 1
-            if not self.step():
-                nxt = t0 + reqs[k].arrival - time.perf_counter() if k < len(reqs) else poll
-                time.sleep(max(0.0, min(poll, nxt)))
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            t0 = time.perf_counter()
+            k = 0
+            self.done = []
+            while k < len(reqs) or not self.idle():
+                now = time.perf_counter()
+                while k < len(reqs) and t0 + reqs[k].arrival <= now:
+                    self.submit(reqs[k], now=t0 + reqs[k].arrival)
+                    k += 1
+                if not self.step():
+                    nxt = t0 + reqs[k].arrival - time.perf_counter() if k < len(reqs) else poll
+                    time.sleep(max(0.0, min(poll, nxt)))
+        finally:
+            if gc_on:
+                gc.enable()
+                gc.collect()
         return list(self.done)
 
 
