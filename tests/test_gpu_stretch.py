@@ -152,3 +152,38 @@ def test_native_fast_packed_equals_dropin_fast(cuda, uni, twist):
     for k in keys:
         a, b = got_n[k], got_d[k]
         assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]), k
+
+
+@pytest.mark.parametrize("shape", [(4, 3, 5), (2, 4, 4), (5, 2, 3), (4, 4, 4)])
+def test_native_tables_equal_dropin_search_on_small_grids(cuda, shape):
+    """Axes of 2-5 nodes with irregular spacing: the reference's search takes
+    its special cases there (with 4 nodes it answers the cell above for the
+    first interval); the native entry's tables must give the same cells.
+    Seeds at random points and exactly on node coordinates; every output
+    bit for bit against the drop-in (which runs the search itself)."""
+    from fastqsl_gb300 import api, synthetic as S
+    rng = np.random.default_rng(sum(shape))
+    ext = (12.0, 10.0, 10.0)
+    lo = (-6.0, -5.0, 0.0)
+    coords = []
+    for n, e, a in zip(shape, ext, lo):
+        w = rng.uniform(0.3, 3.0, n - 1)
+        coords.append((a + np.concatenate([[0.0], np.cumsum(w)]) * (e / w.sum())).astype(np.float32))
+    spec = S.bipole4_stretch(11, shape)
+    Bx, By, Bz = S.make_field_coords(spec, *coords)
+    m = 600
+    pts = [rng.uniform(c[0], c[-1], m).astype(np.float32) for c in coords]
+    # a third of the seeds on node coordinates (interval ends of the search)
+    for d in range(3):
+        pts[d][: m // 3] = rng.choice(coords[d], m // 3)
+    xs, ys, zs = pts
+    got_d = run_dropin_stretch(Bx, By, Bz, coords, False, xs, ys, zs, 0.01, 1.0, arith="fast")
+    prm = P.reference_stretch(arith=P.ARITH_FAST)
+    out = api.trace_stretch(*[torch.from_numpy(np.asfortranarray(b)) for b in (Bx, By, Bz)],
+                            [torch.from_numpy(c).cuda() for c in coords], _dev(xs), _dev(ys), _dev(zs), prm,
+                            s_len=0.01, uni=False)
+    torch.cuda.synchronize()
+    got_n = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    for k in F32 + I32 + ["LineLen"]:
+        a, b = got_n[k], got_d[k]
+        assert np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)]), k
