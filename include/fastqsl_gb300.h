@@ -325,9 +325,14 @@ int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, con
                                 const float *tol_coef, int64_t capacity, qsl_stream_t stream);
 
 /* Native form: host scalars and settings; Bx/By/Bz of shape nx x ny x nz (x
- * fastest) and the coordinates on the device; uni as above.  sched may be
- * NULL (static one-line-per-thread grid) or give the schedule, order map and
- * sample counter (occupancy is ignored). */
+ * fastest) and the coordinates (increasing) on the device; uni as above.
+ * sched may be NULL (static one-line-per-thread grid) or give the schedule,
+ * order map, sample counter and occupancy (6: the 6-blocks-per-SM variant of
+ * the fast kernels; 0: the default).  In fast arithmetic the call allocates,
+ * stream-ordered on `stream` (cudaMallocAsync, freed after the launch), an
+ * interleaved float4 copy of the nodes (16 B per node) and, for the search,
+ * per-axis search tables (48 B per cell of each axis); the outputs equal the
+ * drop-in's (fast arithmetic) bit for bit. */
 int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz,
                       const float *x_arr, const float *y_arr, const float *z_arr, int uni,
                       const qsl_trace_params *prm, const qsl_trace_io *io, int64_t n, float s_len, float tol_coef,
