@@ -59,8 +59,9 @@ static cudaError_t launch_fast(const TraceJob<F>& J, bool twist, Schedule sched,
     }
 }
 
+// (held to 3 blocks per SM: 168 registers; the twist form would take ~210)
 template <int GRAD, bool TWIST, class F>
-__global__ void __launch_bounds__(kTraceBlock) k_scott_fast(const ScottJob<F> J) {
+__global__ void __launch_bounds__(kTraceBlock, 3) k_scott_fast(const ScottJob<F> J) {
     scott_kernel_body<false, GRAD, TWIST>(J);
 }
 

@@ -143,6 +143,56 @@ __device__ __forceinline__ Vec9 scott_step(const F& f, const Vec9& s, float h, f
                         mul9(C::b6, k6)));
 }
 
+// The same Fehlberg step for the fast arithmetic with the six stages in a
+// rolled loop, so that the right-hand side (seven samples for the central
+// differences) is in the loop body once instead of six times: the unrolled
+// step does not fit the instruction cache.
+// After stage st, its k is added into the inputs of the stages still to come,
+// held in a shift register of five 9-vectors (slot i = stage st + 1 + i), so
+// every index is static.  Coefficients as Fehlberg's (float).
+struct ScottTab {
+    float a[6][5];  // a[st][i] = A(st + 1 + i, st)
+    float b[6], e[6];
+};
+__device__ __forceinline__ Vec9 fma9(float a, const Vec9& x, const Vec9& y) {
+    return {v3(fmaf(a, x.p.x, y.p.x), fmaf(a, x.p.y, y.p.y), fmaf(a, x.p.z, y.p.z)),
+            v3(fmaf(a, x.u.x, y.u.x), fmaf(a, x.u.y, y.u.y), fmaf(a, x.u.z, y.u.z)),
+            v3(fmaf(a, x.v.x, y.v.x), fmaf(a, x.v.y, y.v.y), fmaf(a, x.v.z, y.v.z))};
+}
+static __constant__ ScottTab kScottTab = {
+    {{Fehlberg::a21, Fehlberg::a31, Fehlberg::a41, Fehlberg::a51, Fehlberg::a61},
+     {Fehlberg::a32, Fehlberg::a42, Fehlberg::a52, Fehlberg::a62, 0.f},
+     {Fehlberg::a43, Fehlberg::a53, Fehlberg::a63, 0.f, 0.f},
+     {Fehlberg::a54, Fehlberg::a64, 0.f, 0.f, 0.f},
+     {Fehlberg::a65, 0.f, 0.f, 0.f, 0.f},
+     {0.f, 0.f, 0.f, 0.f, 0.f}},
+    {Fehlberg::b1, 0.f, Fehlberg::b3, Fehlberg::b4, Fehlberg::b5, Fehlberg::b6},
+    {Fehlberg::e1, 0.f, Fehlberg::e3, Fehlberg::e4, Fehlberg::e5, Fehlberg::e6}};
+
+template <int GRAD, class F>
+__device__ __forceinline__ Vec9 scott_step_rolled(const F& f, const Vec9& s, float h, float& err, unsigned& ns) {
+    const Vec9 zero = {v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+    Vec9 slot[5] = {zero, zero, zero, zero, zero};
+    Vec9 sol = zero;
+    float3 e = v3(0.f, 0.f, 0.f);
+    Vec9 in = s;
+#pragma unroll 1
+    for (int st = 0; st < 6; ++st) {
+        const Vec9 k = mul9(h, scott_rhs<false, GRAD>(f, in, ns));
+#pragma unroll
+        for (int i = 0; i < 5; ++i) slot[i] = fma9(kScottTab.a[st][i], k, slot[i]);
+        sol = fma9(kScottTab.b[st], k, sol);
+        const float ce = kScottTab.e[st];
+        e = v3(fmaf(ce, k.p.x, e.x), fmaf(ce, k.p.y, e.y), fmaf(ce, k.p.z, e.z));
+        in = add9(s, slot[0]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) slot[i] = slot[i + 1];
+        slot[4] = zero;
+    }
+    err = norm(e);
+    return add9(s, sol);
+}
+
 // v / |v| with the host rsqrtf of the reference's helper_math (1/sqrtf) in
 // exact arithmetic, the hardware rsqrt otherwise.
 template <bool EXACT>
@@ -193,7 +243,13 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
         int flag = 0;
         while ((flag == 0) & (len < len_lim) & (steps < pr.max_steps)) {
             float err;
-            const Vec9 b = scott_step<EXACT, GRAD>(f, a, h * (float)sgn, err, ns);
+            Vec9 b;
+            // the rolled stages pay for the central differences' seven
+            // samples per stage (12.5 -> 10.7 ms on the Scott form); the
+            // analytic gradient's one fetch keeps the unrolled step (3.4 ms
+            // against 3.8 rolled)
+            if constexpr (EXACT || GRAD == GRAD_ANALYTIC) b = scott_step<EXACT, GRAD>(f, a, h * (float)sgn, err, ns);
+            else b = scott_step_rolled<GRAD>(f, a, h * (float)sgn, err, ns);
             float scale;
             if (EXACT) scale = pow_cr((float)((double)(tol / err) / 11.09), 0.2f);
             else scale = exp2f(0.2f * __log2f(tol / err * (float)(1.0 / 11.09)));
