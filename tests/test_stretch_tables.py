@@ -1,0 +1,102 @@
+"""The stretched tracer's search tables (field_store.cu: k_stretch_tables;
+qsl_field.cuh: stretch_table) restated in float32 on the CPU against the
+reference's bisection (GetIndexBiSearch, TraceBlineAdaptiveStretch.cu:42-64):
+for every coordinate the tables give the cell the bisection gives, including
+its answers that are not the containing cell (the cell below near the top of
+its last interval, the cell above for the first interval of a 4-node axis).
+The GPU tests hold the kernels to the same answers bit for bit; this pins
+the scheme itself on many more axes and coordinates."""
+import numpy as np
+import pytest
+
+f32 = np.float32
+BINS_PER_CELL = 4
+
+
+def reference_bisect(c, a):
+    """GetIndexBiSearch: halve [i0, i1] while it spans more than 3 nodes, then
+    mid or mid - 1 on one comparison; clamped into [0, n-2]."""
+    n = len(a)
+    i0, i1, mid = 0, n - 1, n // 2
+    while i1 - i0 > 3:
+        if c > a[mid]:
+            i0 = mid
+        else:
+            i1 = mid
+        mid = (i0 + i1) // 2
+    r = mid if c > a[mid] else mid - 1
+    return max(min(r, n - 2), 0)
+
+
+def cell_below(c, a):
+    """Largest j in [0, n-2] with a[j] < c (0 if none), in double."""
+    lo, hi = 0, len(a) - 2
+    while lo < hi:
+        mid = (lo + hi + 1) >> 1
+        if float(a[mid]) < c:
+            lo = mid
+        else:
+            hi = mid - 1
+    return lo
+
+
+def build_tables(a):
+    n = len(a)
+    nb = BINS_PER_CELL * (n - 1)
+    rec = [reference_bisect(a[j + 1], a) for j in range(n - 1)]
+    a0, w = float(a[0]), (float(a[-1]) - float(a[0])) / nb
+    bins = []
+    for b in range(nb):
+        lo, hi = cell_below(a0 + (b - 0.01) * w, a), cell_below(a0 + (b + 1.01) * w, a)
+        bins.append((lo, max(lo, hi)))
+    binv = f32(f32(nb) / f32(a[-1] - a[0]))
+    return rec, bins, binv
+
+
+def table_lookup(c, a, rec, bins, binv):
+    nb = len(bins)
+    b = int(np.trunc(f32(f32(c - a[0]) * binv)))
+    lo, hi = bins[min(max(b, 0), nb - 1)]
+    while lo < hi:
+        mid = (lo + hi + 1) >> 1
+        if c > a[mid]:
+            lo = mid
+        else:
+            hi = mid - 1
+    return rec[lo]
+
+
+def axes(rng):
+    for n in (2, 3, 4, 5, 7, 8, 16, 33, 128, 256):
+        yield np.cumsum(rng.uniform(0.1, 3.0, n)).astype(f32)              # irregular
+        yield (np.cumsum(1.05 ** np.arange(n)) - 50.0).astype(f32)       # geometric
+        yield np.linspace(-7.0, 9.0, n).astype(f32)                      # uniform
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_tables_give_the_reference_search_cell(seed):
+    rng = np.random.default_rng(seed)
+    checked = 0
+    for a in axes(rng):
+        a = np.unique(a)
+        if len(a) < 2:
+            continue
+        rec, bins, binv = build_tables(a)
+        clo, chi = f32(float(a[0]) + 1e-6), f32(float(a[-1]) - 1e-6)
+        cs = np.concatenate([rng.uniform(float(a[0]), float(a[-1]), 400).astype(f32), a,
+                             np.nextafter(a, f32(np.inf)), np.nextafter(a, f32(-np.inf))])
+        for c in cs:
+            c = f32(c)
+            c = c if c > a[0] else clo          # the kernel's clamp (stretch_locate)
+            c = c if c < a[-1] else chi
+            assert table_lookup(c, a, rec, bins, binv) == reference_bisect(c, a), (len(a), float(c))
+            checked += 1
+    assert checked > 10000
+
+
+def test_four_node_axis_takes_the_cell_above():
+    # the case the tables must reproduce: 4 nodes, a point in the first cell
+    a = np.array([0.0, 1.0, 2.0, 3.0], f32)
+    assert reference_bisect(f32(0.5), a) == 1
+    rec, bins, binv = build_tables(a)
+    assert table_lookup(f32(0.5), a, rec, bins, binv) == 1
