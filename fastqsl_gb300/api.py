@@ -247,6 +247,13 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     results equal the drop-in's bit for bit.  Defaults to the reference
     stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""
     from .params import reference_stretch
+    for c in coords:
+        # coordinates given on the host are checked here (on the device they
+        # are taken as they are: a check would synchronise)
+        if not (isinstance(c, torch.Tensor) and c.is_cuda):
+            a = np.asarray(c.cpu() if isinstance(c, torch.Tensor) else c, dtype=np.float64)
+            if a.ndim != 1 or a.size < 2 or not np.all(np.diff(a) > 0):
+                raise ValueError("each coordinate array must be 1-D, with at least 2 strictly increasing entries")
     lib = _lib.load()
     if params is None:
         params = reference_stretch()

@@ -100,3 +100,16 @@ def test_four_node_axis_takes_the_cell_above():
     assert reference_bisect(f32(0.5), a) == 1
     rec, bins, binv = build_tables(a)
     assert table_lookup(f32(0.5), a, rec, bins, binv) == 1
+
+
+@pytest.mark.parametrize("bad", [[0.0, 1.0, 1.0], [0.0, 2.0, 1.0], [0.0]])
+def test_trace_stretch_rejects_bad_host_coordinates(bad):
+    """The native entry needs strictly increasing node coordinates (the
+    search and its tables assume them); host arrays are checked before any
+    device work."""
+    import torch
+    from fastqsl_gb300 import api
+    b = torch.zeros(3, 3, 3)
+    x = torch.zeros(4)
+    with pytest.raises(ValueError):
+        api.trace_stretch(b, b, b, [np.array(bad, f32), np.arange(3.0), np.arange(3.0)], x, x, x)
