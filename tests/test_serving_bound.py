@@ -80,3 +80,24 @@ def test_ideal_bound_from_isolated_solves():
     # of work to it (1.01), the second waited for the first (2.01)
     assert b["srpt"][1] == pytest.approx(np.percentile([1.01, 2.01, 1.0], 99), rel=1e-9)
     assert b["ps"][0] >= 1.0
+
+
+def test_bench_request_mix_is_beyond_the_serving_bar_for_any_scheduler():
+    """The serving sweep's request stream (96 requests, 10^4-4x10^6 seeds
+    log-uniform, seed 7) under a linear cost model: isolated time = Q-pixels x
+    a per-tolerance cost, at least 3 ms (small requests cannot fill the GPU).
+    At 80 % load even the ideal preemptive SRPT scheduler's p99 is far above
+    2x isolated: the largest requests queue behind each other whatever the
+    order.  At 50 % load it is lower but still above 2x."""
+    from fastqsl_gb300.serving import make_requests
+    shape, names = (384, 384, 256), [f"f{k}" for k in range(8)]
+    burst = make_requests(shape, names, 96, None, seed=7)
+    cost = {1e-3: 0.6, 1e-4: 1.0, 1e-5: 1.7}
+    rate_px = 80e6  # Q-pixels/s of the saturated GPU at tol 1e-4
+    iso = {r.rid: max(r.qpixels / rate_px * cost[r.tol], 0.003) for r in burst}
+    span = sum(r.qpixels / rate_px * cost[r.tol] for r in burst)  # saturated: the work itself
+    p99 = {}
+    for f in (0.5, 0.8):
+        reqs = make_requests(shape, names, 96, f * 96 / span, seed=7)
+        p99[f] = ideal_bound(reqs, iso, span, policies=("srpt",))["srpt"][1]
+    assert p99[0.8] > 4.0 and p99[0.5] > 2.0 and p99[0.8] > p99[0.5]
