@@ -9,12 +9,18 @@ tolerance 1e-4 and steps in [1e-3, 1] cell, pseudo-lines for the pixels
 whose field lies within ~0.6 deg of the plane, FP64 Q assembly.
 
 Forms measured on that workload:
-  value      — fp16 8^3-brick field store + persistent lane-refill tracer
-  plain_fp32 — the plain FP32 kernel: reference SoA field, one line per
-               thread (static grid), no work queue
+  value      — the fp16 brick store (8^3-cell bricks of x-pair records, a
+               float scale per brick; FP32 interpolation of the fp16 node
+               values), seeds traced in 8x8 tiles taken through every plane
+               of the stack (column order), one line per thread in static
+               lockstep, resident blocks per SM from the autotuner
+  plain_fp32 — the plain FP32 kernel: SoA float32 field in the caller's
+               layout, seeds in row order, one line per thread, compiler's
+               register choice; and float32 stores under the headline's own
+               schedule, so the fp16 store's share of the gain shows alone
 Inputs are resident in HBM during the timed region and larger than L2
-(field 805 MB fp32 / 764 MB fp16 bricks; outputs ~0.9 GB), so no L2 flush is
-needed between steps.
+(field 805 MB float32, 1.36 GB as fp16 x-pair bricks; outputs ~0.9 GB), so
+no L2 flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -94,6 +100,51 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def spread_planes(n):
+    """n z-plane indices spread evenly over the sub-box's stack."""
+    n = max(1, min(SUB["nz"], int(n)))
+    return sorted({int(round(v)) for v in np.linspace(0, SUB["nz"] - 1, n)})
+
+
+def sm_count():
+    import ctypes
+    from fastqsl_gb300 import _lib
+    sms = ctypes.c_int(0)
+    _lib.check(_lib.load().qsl_device_sm_count(ctypes.byref(sms)), "qsl_device_sm_count")
+    return int(sms.value)
+
+
+def l1_probe(device, reps=5):
+    """The L1 ceiling of 16-byte lane loads (qsl_l1_probe): GB/s with each
+    warp request spread over 1-32 128-byte lines, 16 resident blocks of 128
+    threads per SM, from a 32 KiB buffer that stays in L1; best of `reps`."""
+    import torch
+    from fastqsl_gb300 import _lib
+    lib = _lib.load()
+    buf = torch.zeros(32 << 10, dtype=torch.uint8, device=device)
+    sink = torch.zeros(1, dtype=torch.int32, device=device)
+    blocks = 16 * sm_count()
+    iters = 2048
+    st = torch.cuda.current_stream(device)
+    out = {}
+    for spread in (1, 2, 4, 8, 16, 32):
+        run = lambda: _lib.check(lib.qsl_l1_probe(buf.data_ptr(), buf.numel(), spread, blocks, iters,  # noqa
+                                                  sink.data_ptr(), st.cuda_stream), "qsl_l1_probe")
+        run()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            run()
+            e1.record(st)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            best = t if best is None else min(best, t)
+        out[str(spread)] = blocks * 128 * 8 * iters * 16 / (best / 1e3) / 1e9
+    return {"coalesced_gbs": out["4"], "by_spread": out}
+
+
 def cube_seeds(device, planes=None):
     if planes is None and NPLANES[0] != SUB["nz"]:
         planes = list(range(PLANE0[0], PLANE0[0] + NPLANES[0]))
@@ -106,6 +157,9 @@ def cube_seeds(device, planes=None):
 
 
 STORE_TYPES = {"h8c": "FieldH8C", "h4b": "FieldH4B", "f4": "FieldF4", "soa": "FieldSoA"}
+# --arith: FP32 interpolation (default) or the fp16-x-weight sampler of the
+# brick store (opt-in)
+ARITHS = {"fast": 1, "w16": 2}
 
 
 def make_field(device):
@@ -120,7 +174,7 @@ def run_ours(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     (bx, by, bz), spec = make_field(dev)
-    prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=P.ARITH_FAST)
+    prm = P.absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=ARITHS[args.arith])
     xs, ys, zz, npl = cube_seeds(dev)
     n0, n1 = SUB["ny"] + 2, SUB["nx"] + 2
     qpix = SUB["nx"] * SUB["ny"] * npl
@@ -168,6 +222,7 @@ def run_ours(args, rank, world):
     Q = plan.Q
 
     res = {"ms": ms, "qpix": qpix, "k_ms": k_ms, "samples_main": samples_main, "samples_all": samples_all,
+           "sm_count": sm_count(), "l1_probe": l1_probe(dev),
            "clocks": clk.summary(), "autotune": {"tile": list(tuned["tile"]), "occupancy": tuned["occupancy"],
                                                  "sample_ms": tuned["table"]}}
     if rank != 0:
@@ -196,6 +251,29 @@ def run_ours(args, rank, world):
         e1.record(stream)
         torch.cuda.synchronize()
         res["ours_trace_ms"] = e0.elapsed_time(e1) / reps
+
+        def timed_trace(st, p, occ):
+            api.trace(st, xs, ys, zz, p, s_len=S_LEN, schedule=plan.schedule, out=out, order=plan.order,
+                      chunk=plan.chunk, occupancy=occ)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                api.trace(st, xs, ys, zz, p, s_len=S_LEN, schedule=plan.schedule, out=out, order=plan.order,
+                          chunk=plan.chunk, occupancy=occ)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        # float32 stores under the headline's own schedule (tile/column order,
+        # static lockstep): the fp16 store's gain by itself
+        f4 = api.FieldStore(bx, by, bz, layout="f4")
+        res["same_schedule_f4_ms"] = {str(o): timed_trace(f4, prm.copy(arith=P.ARITH_FAST), o) for o in (0, 6, 8)}
+        f4.close()
+        res["same_schedule_soa_ms"] = {str(o): timed_trace(soa, prm.copy(arith=P.ARITH_FAST), o) for o in (0, 8)}
+        if args.layout == "h4b":
+            # the other x-lerp form of the brick store under the same schedule
+            other = P.ARITH_FAST_W16 if prm.arith == P.ARITH_FAST else P.ARITH_FAST
+            res["other_arith_trace_ms"] = timed_trace(store, prm.copy(arith=other), plan.occupancy_for(store))
         # the reference kernel's design on this GPU: one line per thread in
         # seed order, SoA float32 field, the reference's rounding (corner
         # weights in double), work-queue grid; same settings, one run
@@ -244,21 +322,27 @@ def run_ours(args, rank, world):
 
     # ---- accuracy against the FP64 oracle on a seeded sample of cells ----
     if not args.skip_accuracy:
-        res["accuracy"] = accuracy_sample(bx, by, bz, Q.cpu().numpy(), prm, args.acc_cells)
+        cubes = {args.arith: Q.cpu().numpy()}
+        if args.layout == "h4b":
+            # the brick store's other x-lerp form, on the same cells
+            oname = "w16" if args.arith == "fast" else "fast"
+            plan.run(store, xs, ys, zz, prm.copy(arith=ARITHS[oname]), s_len=S_LEN, stride=1.0)
+            cubes[oname] = plan.Q.cpu().numpy()
+        res["accuracy"] = accuracy_sample(bx, by, bz, cubes, prm, args.acc_cells)
     store.close()
     return res, Q
 
 
-def accuracy_sample(bx, by, bz, Q, prm, ncells):
-    """|dlog10 Q| of the GPU cube against the FP64 oracle on `ncells` seeded
-    cells: each sampled cell's Q is recomputed from its 5-seed stencil (and
-    its pseudo-lines when flagged) traced in FP64 on the host."""
+def accuracy_sample(bx, by, bz, cubes, prm, ncells):
+    """|dlog10 Q| of GPU cubes (name -> Q array) against the FP64 oracle on
+    `ncells` seeded cells: each sampled cell's Q is recomputed from its 5-seed
+    stencil (and its pseudo-lines when flagged) traced in FP64 on the host."""
     import oracle
     from fastqsl_gb300 import params as P
     from oracle import qassembly as QA
     rng = np.random.default_rng(1234)
     s = SUB
-    npl = Q.shape[0]
+    npl = next(iter(cubes.values())).shape[0]
     ci = rng.integers(0, npl, ncells)
     cj = rng.integers(0, s["ny"], ncells)
     ck = rng.integers(0, s["nx"], ncells)
@@ -279,12 +363,15 @@ def accuracy_sample(bx, by, bz, Q, prm, ncells):
     tr = lambda a, b, c: oracle.trace_all("port64", B[0], B[1], B[2], a, b, c, s_len=S_LEN,  # noqa: E731
                                           params=prm64)
     Qr = QA.qmap_pipeline(tr, xs, ys, zs, ncells, 3, 3, 1.0)[:, 0, 0]
-    Qg = Q[ci, cj, ck]
-    both = ~np.isnan(Qr) & ~np.isnan(Qg)
-    d = np.abs(np.log10(Qg[both]) - np.log10(Qr[both]))
-    return {"cells": int(ncells), "nan_agree": float((np.isnan(Qr) == np.isnan(Qg)).mean()),
-            "median_dlog10Q": float(np.median(d)) if d.size else None,
-            "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None}
+    out = {}
+    for name, Q in cubes.items():
+        Qg = Q[ci, cj, ck]
+        both = ~np.isnan(Qr) & ~np.isnan(Qg)
+        d = np.abs(np.log10(Qg[both]) - np.log10(Qr[both]))
+        out[name] = {"cells": int(ncells), "nan_agree": float((np.isnan(Qr) == np.isnan(Qg)).mean()),
+                     "median_dlog10Q": float(np.median(d)) if d.size else None,
+                     "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None}
+    return out
 
 
 _HOST_FIELD = []
@@ -321,21 +408,26 @@ def cpu_baseline(planes, threads=None):
             "sample": f"{npl} of {SUB['nz']} z-planes of the same cube ({qpix} Q-pixels), {dt:.1f} s"}
 
 
-def batched_graph(device, n_fields=64, seed=11, reps=3):
+def batched_graph(device, n_fields=64, seed=11, reps=3, acc_fields=8, acc_pixels=40):
     """64 independent fields (4-32 charges; 64^3, 128^3, 192x192x128 or 256^3;
     fp16 bricks or float32 nodes, interleaved), each with an arbitrarily oriented cutting
     plane of 10^3-10^6 seeds (log-uniform), RK4 or RKF45; the whole Q pipeline
-    of all 64 captured once into a CUDA graph and replayed."""
+    of all 64 captured once into a CUDA graph and replayed.  Accuracy: on
+    `acc_fields` of the fields (every 8th), `acc_pixels` seeded interior
+    pixels each against the FP64 oracle (each pixel's 3x3 seed stencil on its
+    cutting plane, and its pseudo-lines when flagged)."""
     import torch
     from fastqsl_gb300 import api, params as P, synthetic as S
     rng = np.random.default_rng(seed)
     sizes = [(64, 64, 64), (128, 128, 128), (192, 192, 128), (256, 256, 256)]
-    specs, stores = [], []
+    specs, stores, keep = [], [], {}
+    acc_idx = set(range(0, n_fields, max(1, n_fields // acc_fields))[:acc_fields])
     for k in range(n_fields):
         shape = sizes[int(rng.integers(len(sizes)))]
         spec = S.charges_random(seed * 100 + k, shape, int(rng.integers(4, 33)))
         B = S.make_field(spec, device=device, as_numpy=False)
-        fs = api.FieldStore(*B, layout="h4b" if rng.random() < 0.5 else "f4")
+        layout = "h4b" if rng.random() < 0.5 else "f4"
+        fs = api.FieldStore(*B, layout=layout)
         stores.append(fs)
         total = float(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
         n0 = max(3, int(np.sqrt(total)))
@@ -347,6 +439,10 @@ def batched_graph(device, n_fields=64, seed=11, reps=3):
         t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
         specs.append(dict(field=fs, xs=t(xs), ys=t(ys), zs=t(zs), n0=n0, n1=n1, nplanes=1, params=prm,
                           s_len=0.25 if rkf else 0.1, stride=stride, cross_dir=tuple(float(c) for c in nrm)))
+        if k in acc_idx:
+            keep[k] = dict(B=[b.cpu().numpy() for b in B], xs=xs, ys=ys, zs=zs, layout=layout, shape=shape,
+                           integrator="rkf45" if rkf else "rk4")
+        del B
     qb = api.QBatch(specs, device=device)
     qb.capture()
     torch.cuda.synchronize()
@@ -361,9 +457,53 @@ def batched_graph(device, n_fields=64, seed=11, reps=3):
     lines = sum(sp["n0"] * sp["n1"] for sp in specs)
     out = {"fields": n_fields, "seeds": int(lines), "q_pixels": int(qpix), "graph_ms": ms,
            "qpixels_per_s": qpix / (ms / 1e3)}
+    Qs = {k: qb.jobs[k]["Q"][0].cpu().numpy() for k in keep}
     for fs in stores:
         fs.close()
+    del qb
+    out["accuracy_vs_fp64"] = batched_accuracy(specs, keep, Qs, acc_pixels)
     return out
+
+
+def batched_accuracy(specs, keep, Qs, npix, seed=5):
+    """|dlog10 Q| of sampled batched-graph pixels against the FP64 oracle:
+    per sampled field `npix` seeded interior pixels, each recomputed from its
+    3x3 stencil of seeds on the field's cutting plane (and its pseudo-lines
+    when flagged) traced in FP64 with the job's own integrator settings."""
+    import oracle
+    from fastqsl_gb300 import params as P
+    from oracle import qassembly as QA
+    rng = np.random.default_rng(seed)
+    per, d_all, nan_all = {}, [], []
+    for k, kv in sorted(keep.items()):
+        sp = specs[k]
+        n0, n1 = sp["n0"], sp["n1"]
+        Q = Qs[k]
+        ci = rng.integers(0, n0 - 2, npix)
+        cj = rng.integers(0, n1 - 2, npix)
+        gx, gy, gz = (a.reshape(n0, n1) for a in (kv["xs"], kv["ys"], kv["zs"]))
+        sx = np.concatenate([gx[i:i + 3, j:j + 3].ravel() for i, j in zip(ci, cj)])
+        sy = np.concatenate([gy[i:i + 3, j:j + 3].ravel() for i, j in zip(ci, cj)])
+        sz = np.concatenate([gz[i:i + 3, j:j + 3].ravel() for i, j in zip(ci, cj)])
+        prm64 = sp["params"].copy(arith=P.ARITH_EXACT)
+        B = kv["B"]
+        tr = lambda a, b, c: oracle.trace_all("port64", B[0], B[1], B[2], a, b, c,  # noqa: E731
+                                              cross_dir=sp["cross_dir"], s_len=sp["s_len"], params=prm64)
+        Qr = QA.qmap_pipeline(tr, sx, sy, sz, npix, 3, 3, sp["stride"], cross_dir=sp["cross_dir"])[:, 0, 0]
+        Qg = Q[ci, cj]
+        both = ~np.isnan(Qr) & ~np.isnan(Qg)
+        d = np.abs(np.log10(Qg[both]) - np.log10(Qr[both]))
+        nan_agree = np.isnan(Qr) == np.isnan(Qg)
+        per[str(k)] = {"layout": kv["layout"], "shape": "x".join(map(str, kv["shape"])),
+                       "integrator": kv["integrator"], "nan_agree": float(nan_agree.mean()),
+                       "median_dlog10Q": float(np.median(d)) if d.size else None}
+        d_all.append(d)
+        nan_all.append(nan_agree)
+    d = np.concatenate(d_all) if d_all else np.zeros(0)
+    return {"fields": len(keep), "pixels": int(sum(len(a) for a in nan_all)),
+            "nan_agree": float(np.concatenate(nan_all).mean()) if nan_all else None,
+            "median_dlog10Q": float(np.median(d)) if d.size else None,
+            "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None, "per_field": per}
 
 
 def forms(device, planes=16):
@@ -475,17 +615,69 @@ def forms(device, planes=16):
     return res
 
 
-def serving_sweep(device, count=96):
-    """8 resident 384x384x256 fields; Poisson streams of Q-map requests
-    (10^4-4x10^6 seeds, tol 1e-3/1e-4/1e-5) at fractions of the batched
-    (whole-batch launches, all requests at once) saturated rate, served with
-    windowed bulk traces; p50/p99 latency against each request's isolated
-    solve."""
+def serving_accuracy(alone, device, server, nreq=4, npix=30, seed=9):
+    """|dlog10 Q| of `nreq` isolated serving results (the first requests of
+    the stream, each on its own resident field) against the FP64 oracle:
+    `npix` seeded interior pixels each, recomputed from the pixel's 3x3 seed
+    stencil on the request's plane (and its pseudo-lines when flagged) with
+    the request's tolerance; the field is regenerated from its seeded spec
+    for the host."""
+    import oracle
+    from fastqsl_gb300 import params as P, serving, synthetic as S
+    from oracle import qassembly as QA
+    rng = np.random.default_rng(seed)
+    d_all, nan_all, per = [], [], {}
+    for rid in sorted(alone)[:nreq]:
+        r, Q = alone[rid]
+        k = int(r.field[1:])
+        B = [b.cpu().numpy() for b in S.make_field(S.charges_tube(k, (384, 384, 256), n_charges=8),
+                                                    device=device, as_numpy=False)]
+        xs, ys, zs, nrm = serving.seeds_on_device(r, device)
+        g = [a.cpu().numpy().reshape(r.nplanes, r.n0, r.n1) for a in (xs, ys, zs)]
+        cp = rng.integers(0, r.nplanes, npix)
+        ci = rng.integers(0, r.n0 - 2, npix)
+        cj = rng.integers(0, r.n1 - 2, npix)
+        st = [np.concatenate([a[p, i:i + 3, j:j + 3].ravel() for p, i, j in zip(cp, ci, cj)]) for a in g]
+        prm = P.absolute_rkf45(tol=r.tol, h_min=server.h_min, h_max=server.h_max, arith=P.ARITH_EXACT)
+        tr = lambda a, b, c: oracle.trace_all("port64", B[0], B[1], B[2], a, b, c, cross_dir=nrm,  # noqa: E731
+                                              s_len=server.s_len, params=prm)
+        Qr = QA.qmap_pipeline(tr, *st, npix, 3, 3, r.spacing, cross_dir=nrm)[:, 0, 0]
+        Qg = Q[cp, ci, cj]
+        both = ~np.isnan(Qr) & ~np.isnan(Qg)
+        d = np.abs(np.log10(Qg[both]) - np.log10(Qr[both]))
+        per[str(rid)] = {"seeds": r.seeds, "tol": r.tol, "median_dlog10Q": float(np.median(d)) if d.size else None}
+        d_all.append(d)
+        nan_all.append(np.isnan(Qr) == np.isnan(Qg))
+    d = np.concatenate(d_all) if d_all else np.zeros(0)
+    return {"requests": len(per), "pixels": int(sum(len(a) for a in nan_all)),
+            "nan_agree": float(np.concatenate(nan_all).mean()) if nan_all else None,
+            "median_dlog10Q": float(np.median(d)) if d.size else None,
+            "p99_dlog10Q": float(np.quantile(d, 0.99)) if d.size else None, "per_request": per}
+
+
+def serving_sweep(device, count=512):
+    """8 resident 384x384x256 fields; Poisson streams of `count` Q-map
+    requests (tol 1e-3/1e-4/1e-5) at fractions of the batched (whole-batch
+    launches, all requests at once) saturated rate, served with windowed bulk
+    traces; p50/p99 latency against each request's isolated solve, beside
+    what an ideal fluid scheduler reaches on the same stream.  Two mixes: the
+    serving configuration's 10^4-4x10^6 seeds (log-uniform), and small
+    requests of 10^4-3x10^4 seeds, where even the ideal scheduler's p99 at
+    80 % load is within 2x isolated only because no request fills the GPU
+    alone."""
     from fastqsl_gb300 import serving
     fields = serving.make_fields(n_fields=8, shape=(384, 384, 256), device=device)
     srv = serving.QServer(fields, hbm_budget=48 << 30, streams=3, max_batch=16)
     whole = serving.QServer(fields, hbm_budget=48 << 30, streams=3, max_batch=16, chunk_lines=0)
-    out = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8), batched_server=whole)
+    alone = {}
+    out = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8), batched_server=whole,
+                        alone_out=alone)
+    out["mix"] = "1e4-4e6 seeds, log-uniform"
+    out["accuracy_vs_fp64"] = serving_accuracy(alone, device, srv)
+    small = serving.sweep(srv, (384, 384, 256), count=count, fractions=(0.5, 0.8), batched_server=whole,
+                          seeds_range=(1e4, 3e4))
+    small["mix"] = "1e4-3e4 seeds, log-uniform"
+    out["small_requests"] = small
     for fs in fields.values():
         fs.close()
     return out
@@ -498,7 +690,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--layout", default="h4b", choices=["h8c", "h4b", "f4", "soa"])
+    ap.add_argument("--arith", default="fast", choices=list(ARITHS),
+                    help="fast: FP32 interpolation; w16: fp16 x weights (h4b only)")
     ap.add_argument("--cpu-planes", type=int, default=32)
+    ap.add_argument("--ref-planes", type=int, default=8, help="z-planes per step of --impl reference")
     ap.add_argument("--acc-cells", type=int, default=2000)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
@@ -530,19 +725,33 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        per = []
-        for _ in range(args.warmup):
-            cpu_baseline(list(range(1)), None)
-        for _ in range(args.steps):
-            per.append(cpu_baseline(list(range(args.cpu_planes)), None))
-        v = float(np.mean([p["value"] for p in per]))
-        qpix = SUB["nx"] * SUB["ny"] * SUB["nz"]
+        # each step is a bounded sample of the cube: `--ref-planes` z-planes
+        # spread evenly over the 128-plane stack, shifted from step to step,
+        # timed whole; the rate and ms_per_step are those of that sample
+        npl = max(1, min(SUB["nz"], args.ref_planes))
+        gap = SUB["nz"] // npl
+
+        def planes_of(k):
+            return sorted({(j * gap + (k * 5) % gap) % SUB["nz"] for j in range(npl)})
+
+        for k in range(args.warmup):
+            cpu_baseline([planes_of(k)[0]], None)
+        per, wall = [], []
+        for k in range(args.steps):
+            t = time.perf_counter()
+            per.append(cpu_baseline(planes_of(k), None))
+            wall.append(time.perf_counter() - t)
+        qpix_step = SUB["nx"] * SUB["ny"] * npl
+        v = qpix_step * len(per) / float(sum(wall))
         line = {"metric": METRIC, "value": v, "unit": "Q-pixels/s", "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": qpix / v * 1e3,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(wall)) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
-                                                 "sampled_planes_per_step": args.cpu_planes},
-                "cpu_baseline": {**per[-1], "value": v},
+                "data": "synthetic",
+                "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
+                           "step": f"{npl} of the {SUB['nz']} z-planes ({qpix_step} Q-pixels), spread evenly "
+                                   f"over the stack and shifted each step"},
+                "cpu_baseline": {**per[-1], "value": v,
+                                 "sample": f"{npl} z-planes per step ({qpix_step} Q-pixels), {args.steps} steps"},
                 "e2e": {"value": v, "unit": "Q-pixels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -558,61 +767,89 @@ def main():
     from fastqsl_gb300 import replicas
     value = replicas.whole_job_rate(res["qpix"], ms, world)
     fp16 = args.layout in ("h4b", "h8c")
-    bytes_per_sample = 48 if fp16 else 96
-    achieved = res["samples_main"] * bytes_per_sample / (res["k_ms"] / 1e3) / 1e9
+    k_s = res["k_ms"] / 1e3
+    # algorithmic bytes per field sample: 8 corners x 3 components (fp16: 48 B,
+    # float32: 96 B); the bytes the sampler's loads move through L1 per
+    # sample: four 16-byte x-pair records (h4b), 32 + 16 B (h8c), eight
+    # 16-byte nodes (f4), 24 4-byte words (soa)
+    alg_bytes = 48 if fp16 else 96
+    l1_bytes = {"h4b": 64, "h8c": 48, "f4": 128, "soa": 96}[args.layout]
+    l1 = res["l1_probe"]
+    l1_achieved = res["samples_main"] * l1_bytes / k_s / 1e9
+    hbm_achieved = res["samples_main"] * alg_bytes / k_s / 1e9
+    acc = res.get("accuracy", {})
     line = {
-        "metric": METRIC, "value": value, "unit": "Q-pixels/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "Q-pixels/s",
+        "accuracy_vs_fp64": acc.get(args.arith) if acc else None,
+        "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (fp16 field storage)" if fp16 else "f32",
         "data": "synthetic",
         "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
                    "field": "x".join(map(str, FIELD_SHAPE)), "qcube": "256x256x128", "layout": args.layout,
-                   "schedule": "static lockstep, 8x8 seed tiles, 8 blocks/SM", "h": [1e-3, 1.0],
-                   "planes": NPLANES[0], "l2": "inputs larger than L2 (no flush)"},
+                   "interpolation": "FP32 weights and lerps of fp16 node values" if args.arith == "fast"
+                   else "fp16 x weights (opt-in sampler)",
+                   "h": [1e-3, 1.0], "planes": NPLANES[0], "l2": "inputs larger than L2 (no flush)"},
         "gpu_launches": None,
         "clocks": res["clocks"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     # DRAM bytes per launch: ncu's dram__bytes_read.sum + write.sum
-                     # of the full-size main trace (one-pass capture: 1.18 GB read +
-                     # 0.70 GB written for 14.82 G samples,
-                     # profiles/trace_h4b_cube_traffic.md), per this launch's samples
-                     "traffic": (1.884e9 / 14.816e9) * res["samples_main"] if args.layout == "h4b" else None,
-                     "kernel": f"k_trace_fast<static, {STORE_TYPES[args.layout]}> (main trace)",
-                     "note": f"algorithmic bytes = {bytes_per_sample} B x {res['samples_main']} field samples per "
-                             f"launch / {res['k_ms']:.2f} ms; peak {peak_kind}"},
+        "roofline": {
+            "bound": "l1", "achieved": l1_achieved, "peak": l1["coalesced_gbs"], "unit": "GB/s",
+            "frac": l1_achieved / l1["coalesced_gbs"],
+            # DRAM bytes per launch: ncu's dram__bytes_read.sum + write.sum of
+            # the full-size main trace (one-pass capture: 1.18 GB read + 0.70 GB
+            # written for 14.82 G samples), per this launch's samples
+            "traffic": (1.884e9 / 14.816e9) * res["samples_main"] if args.layout == "h4b" else None,
+            "kernel": f"k_trace_fast<static, {STORE_TYPES[args.layout]}> (main trace)",
+            "note": (f"L1 bytes the field gathers load = {l1_bytes} B x {res['samples_main']} field samples per "
+                     f"launch / {res['k_ms']:.2f} ms (CUDA events on the launch stream); peak = qsl_l1_probe in "
+                     f"this run: 16-byte lane loads from an L1-resident buffer, coalesced (4 lines per warp "
+                     f"request); the tracer's requests are scattered gathers, so its L1 wavefronts per byte "
+                     f"exceed the probe's"),
+            "l1_probe_gbs_by_lines_per_request": l1["by_spread"],
+            "hbm": {"achieved": hbm_achieved, "peak": peak, "unit": "GB/s", "frac": hbm_achieved / peak,
+                    "peak_kind": peak_kind,
+                    "note": f"algorithmic {alg_bytes} B per sample; above 1 because the gathers hit L1/L2, "
+                            f"DRAM traffic is the 'traffic' figure"},
+        },
     }
-    # Secondary roofline in FP32 flops: 75 per normalised field sample (18
-    # weights, 24 FMA, 9 to normalise) plus 130 per RKF45 step for the
-    # combine and error estimate, one step per 6 samples.  The peak is
-    # nominal (152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz); no measured
-    # FP32 figure exists for this GPU.
+    # FP32 flop view: 75 flops per normalised field sample (18 weights, 24 FMA,
+    # 9 to normalise) plus 130 per RKF45 step for the combine and error
+    # estimate, one step per 6 samples.  Nominal peak from the device's SM
+    # count (128 FP32 lanes x 2 flops per SM per clock at 2.07 GHz); no
+    # measured FP32 figure exists for this GPU.
     flops = res["samples_main"] * (75.0 + 130.0 / 6.0)
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
-    line["roofline"]["flops"] = {"achieved": flops / (res["k_ms"] / 1e3) / 1e12, "peak": fp32_peak,
-                                 "unit": "TFLOP/s", "frac": flops / (res["k_ms"] / 1e3) / 1e12 / fp32_peak,
-                                 "peak_kind": "nominal"}
+    fp32_peak = res["sm_count"] * 128 * 2 * 2.07e9 / 1e12
+    line["roofline"]["flops"] = {"achieved": flops / k_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": flops / k_s / 1e12 / fp32_peak, "peak_kind": "nominal",
+                                 "sm_count": res["sm_count"]}
     line["roofline"]["limiter"] = ("SM issue and the L1 data pipe together (ncu on 32 mid-cube planes: "
-                                   "issue active 80.9 %, L1 LSU wavefronts 80.7 % of peak); the field "
-                                   "gathers hit L1 (96.7 %) and L2, so the HBM frac exceeds 1")
+                                   "issue active ~81 %, L1 LSU wavefronts ~81 % of peak)")
     # launches per step: main trace, qcalc, flag_count, tile_scan, cook_write,
     # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
     line["gpu_launches"] = 8 * args.steps
     line["config"]["autotune"] = res["autotune"]
     line["config"]["schedule"] = (f"static lockstep, {res['autotune']['tile'][0]}x{res['autotune']['tile'][1]} "
-                                  f"seed tiles, occupancy {res['autotune']['occupancy']} "
+                                  f"seed tiles in column order, occupancy {res['autotune']['occupancy']} "
                                   f"({'default' if args.no_autotune else 'autotuned'})")
+    if acc:
+        line["accuracy_vs_fp64_all_forms"] = acc
     if "plain_trace_ms" in res:
-        line["plain_fp32"] = {"trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
-                              "speedup": res["plain_trace_ms"] / res["ours_trace_ms"],
-                              "reference_design_trace_ms": res.get("exact_trace_ms"),
-                              "speedup_vs_reference_design": res["exact_trace_ms"] / res["ours_trace_ms"]
-                              if res.get("exact_trace_ms") else None}
+        line["plain_fp32"] = {
+            "trace_ms": res["plain_trace_ms"], "ours_trace_ms": res["ours_trace_ms"],
+            "speedup": res["plain_trace_ms"] / res["ours_trace_ms"],
+            "plain": "SoA float32 field, seeds in row order, compiler's registers, same fast stepper",
+            "same_schedule_f4_trace_ms": res["same_schedule_f4_ms"],
+            "same_schedule_soa_trace_ms": res["same_schedule_soa_ms"],
+            "speedup_vs_same_schedule_f32": min(res["same_schedule_f4_ms"].values()) / res["ours_trace_ms"],
+            "reference_design_trace_ms": res.get("exact_trace_ms"),
+            "speedup_vs_reference_design": res["exact_trace_ms"] / res["ours_trace_ms"]
+            if res.get("exact_trace_ms") else None}
+        if "other_arith_trace_ms" in res:
+            line["plain_fp32"]["other_arith"] = {"arith": "w16" if args.arith == "fast" else "fast",
+                                                 "trace_ms": res["other_arith_trace_ms"]}
     if "e2e_ms" in res:
         line["e2e"] = {"value": res["qpix"] / (res["e2e_ms"] / 1e3), "unit": "Q-pixels/s",
                        "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]}
-    if "accuracy" in res:
-        line["accuracy_vs_fp64"] = res["accuracy"]
     if not args.skip_batched:
         import torch
         line["batched_graph"] = batched_graph(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
@@ -623,7 +860,7 @@ def main():
         import torch
         line["serving"] = serving_sweep(torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0))))
     if not args.skip_cpu:
-        line["cpu_baseline"] = cpu_baseline(list(range(args.cpu_planes)))
+        line["cpu_baseline"] = cpu_baseline(spread_planes(args.cpu_planes))
     line["samples_per_step"] = res["samples_all"]
     print(json.dumps(line))
 

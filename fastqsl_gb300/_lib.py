@@ -29,7 +29,8 @@ class TraceIO(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "inp_x", "inp_y", "inp_z", "start_x", "start_y", "start_z", "flag_start",
         "end_x", "end_y", "end_z", "flag_end", "B_this_x", "B_this_y", "B_this_z", "B_flag",
-        "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist")]
+        "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z", "LineLen", "twist",
+        "status_start", "status_end")]
 
 
 class BatchJob(ctypes.Structure):
@@ -109,6 +110,7 @@ _SIGS = {
     "qsl_cook_pseudo_line_noalloc": (c_int, [_P] * 7 + [c_i64, c_int, c_int, c_int, c_float] + [_P] * 7 + [_P]),
     "qsl_qcut": (c_int, [_P] * 10 + [c_i64, _P, c_i64, c_double, _P, _P, _P]),
     "qsl_qmerge": (c_int, [_P, _P, _P, c_i64, _P, c_i64, c_int, c_int, _P, _P, _P]),
+    "qsl_l1_probe": (c_int, [_P, c_i64, c_int, c_int, c_int, _P, _P]),
 }
 
 

@@ -180,11 +180,17 @@ class FieldUploader:
         self._last = slot
 
 
-def alloc_trace_outputs(n, device="cuda", twist=False):
+def alloc_trace_outputs(n, device="cuda", twist=False, status=False):
+    """The per-seed output arrays of a trace.  status=True adds int32
+    'status_start' / 'status_end' (qsl_line_status of each direction:
+    params.LINE_FACE ... LINE_REJECT_LIMIT)."""
     out = {k: torch.zeros(n, dtype=torch.float32, device=device) for k in TRACE_F32}
     out.update({k: torch.zeros(n, dtype=torch.int32, device=device) for k in TRACE_I32})
     out["LineLen"] = torch.zeros(n, dtype=torch.float64, device=device)
     out["twist"] = torch.zeros(n, dtype=torch.float64, device=device) if twist else None
+    if status:
+        out["status_start"] = torch.zeros(n, dtype=torch.int32, device=device)
+        out["status_end"] = torch.zeros(n, dtype=torch.int32, device=device)
     return out
 
 
@@ -194,12 +200,14 @@ def _io(xs, ys, zs, out):
     for k in TRACE_F32 + TRACE_I32 + ["LineLen"]:
         setattr(io, k, ptr(out[k]))
     io.twist = ptr(out.get("twist"))
+    io.status_start = ptr(out.get("status_start"))
+    io.status_end = ptr(out.get("status_end"))
     return io
 
 
 def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_len=0.125, tol_coef=1.0,
           cross_dir=(0.0, 0.0, 1.0), curB=None, schedule="queue", out=None, n=None, n_dev=None, samples=None,
-          queue=None, order=None, chunk=0, occupancy=0, stream=None):
+          queue=None, order=None, chunk=0, occupancy=0, stream=None, status=False):
     """Traces every seed (xs, ys, zs: float32 CUDA vectors) both ways.
     Returns the output dict (allocated unless `out` is given).  `n_dev`: a
     device counter holding the seed count (outputs must then hold the largest
@@ -208,13 +216,15 @@ def trace(field: FieldStore, xs, ys, zs, params: TraceParams | None = None, s_le
     traces seed order[k] (see tile_order).  `chunk`: lines per warp refill.
     `curB`: the current density for the twist integral, as three x-fastest
     float32 device arrays or as a FieldStore of the field's layout and shape
-    (qsl_trace_cur: each current sample costs a field sample)."""
+    (qsl_trace_cur: each current sample costs a field sample).  `status`:
+    also return each direction's qsl_line_status ('status_start',
+    'status_end'; with `out` given, it is written when `out` holds them)."""
     lib = _lib.load()
     if params is None:
         params = absolute_rkf45()
     n = int(xs.shape[0]) if n is None else int(n)
     if out is None:
-        out = alloc_trace_outputs(n, xs.device, twist=curB is not None)
+        out = alloc_trace_outputs(n, xs.device, twist=curB is not None, status=status)
     cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
     if curB is not None and out.get("twist") is None:
         out["twist"] = torch.zeros(out["LineLen"].shape[0], dtype=torch.float64, device=xs.device)
@@ -251,9 +261,12 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
         # coordinates given on the host are checked here (on the device they
         # are taken as they are: a check would synchronise)
         if not (isinstance(c, torch.Tensor) and c.is_cuda):
-            a = np.asarray(c.cpu() if isinstance(c, torch.Tensor) else c, dtype=np.float64)
+            # on the float32 values the device uses: two distinct doubles
+            # can round to one float
+            a = np.asarray(c.cpu() if isinstance(c, torch.Tensor) else c, dtype=np.float64).astype(np.float32)
             if a.ndim != 1 or a.size < 2 or not np.all(np.diff(a) > 0):
-                raise ValueError("each coordinate array must be 1-D, with at least 2 strictly increasing entries")
+                raise ValueError("each coordinate array must be 1-D, with at least 2 strictly increasing entries "
+                                 "(as float32)")
     lib = _lib.load()
     if params is None:
         params = reference_stretch()

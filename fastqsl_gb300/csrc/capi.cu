@@ -70,6 +70,7 @@ void qsl_params_reference_rk4(qsl_trace_params* p) {
     p->max_steps = 100000;
     p->boundary_twist = 1;
     p->arith = QSL_ARITH_EXACT;
+    p->max_rejects = 0;
 }
 
 void qsl_params_reference_rkf45(qsl_trace_params* p) {
@@ -83,6 +84,7 @@ void qsl_params_reference_rkf45(qsl_trace_params* p) {
     p->max_steps = 500000;
     p->boundary_twist = 0;
     p->arith = QSL_ARITH_EXACT;
+    p->max_rejects = 0;
 }
 
 }  // extern "C"
@@ -231,6 +233,7 @@ static FieldH4B h4b_of(const qsl_field* f) {
     return FieldH4B{f->bricks, f->scale, f->d, f->nbx, f->nby, (unsigned)(BRICK_U4 * f->nbx - 64),
                     (unsigned)((unsigned long long)BRICK_U4 * f->nbx * f->nby - 576)};
 }
+static FieldH4BW h4bw_of(const qsl_field* f) { return FieldH4BW{h4b_of(f)}; }
 static FieldH8C h8c_of(const qsl_field* f) { return FieldH8C{f->cells, f->d, f->nbx, f->nby}; }
 
 // ---------------------------------------------------------------------------
@@ -245,6 +248,8 @@ static TraceOut make_out(const qsl_trace_io* io) {
     o.bend_x = io->B_end_x; o.bend_y = io->B_end_y; o.bend_z = io->B_end_z;
     o.line_len = io->LineLen;
     o.twist = io->twist;
+    o.status_start = io->status_start;
+    o.status_end = io->status_end;
     return o;
 }
 
@@ -258,7 +263,8 @@ static bool io_ok(const qsl_trace_io* io) {
 static bool params_ok(const qsl_trace_params* p) {
     return p && (p->integrator == QSL_RK4 || p->integrator == QSL_RKF45) &&
            (p->tol_law == QSL_TOL_REFERENCE || p->tol_law == QSL_TOL_ABSOLUTE) &&
-           (p->arith == QSL_ARITH_EXACT || p->arith == QSL_ARITH_FAST) && p->max_steps >= 0 &&
+           (p->arith == QSL_ARITH_EXACT || p->arith == QSL_ARITH_FAST || p->arith == QSL_ARITH_FAST_W16) &&
+           p->max_steps >= 0 && p->max_rejects >= 0 &&
            p->max_steps <= 0x7fffffff && p->reject_factor > 0.0 && p->reject_factor < 1.0 && p->len_ratio >= 0.0;
 }
 
@@ -289,6 +295,8 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
         e = launch_trace_fast_f4(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldH4B>::value) {
         e = launch_trace_fast_h4b(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldH4BW>::value) {
+        e = launch_trace_fast_h4bw(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldStretchP>::value) {
         e = launch_trace_fast_stretch_packed(J, twist, sched, n_host, st);
     } else if constexpr (std::is_same<F, FieldStretchPU>::value) {
@@ -337,6 +345,7 @@ extern "C++" {
 static void store_view(const qsl_field_t* f, FieldSoA& s) { s = soa_of(f); }
 static void store_view(const qsl_field_t* f, FieldF4& s) { s = f4_of(f); }
 static void store_view(const qsl_field_t* f, FieldH4B& s) { s = h4b_of(f); }
+static void store_view(const qsl_field_t* f, FieldH4BW& s) { s = h4bw_of(f); }
 static void store_view(const qsl_field_t* f, FieldH8C& s) { s = h8c_of(f); }
 }
 
@@ -372,6 +381,8 @@ static int trace_impl(const qsl_field_t* field, const qsl_field_t* cur_field, co
     }
     if (field->layout != LAYOUT_SOA && prm->arith == QSL_ARITH_EXACT)
         return fail(QSL_ERR_INVALID, "exact arithmetic needs the SoA layout");
+    if (field->layout != LAYOUT_H4B && prm->arith == QSL_ARITH_FAST_W16)
+        return fail(QSL_ERR_INVALID, "fp16 x weights (QSL_ARITH_FAST_W16) need the h4b layout");
     const float cd[3] = {cross_dir_h ? cross_dir_h[0] : 0.f, cross_dir_h ? cross_dir_h[1] : 0.f,
                          cross_dir_h ? cross_dir_h[2] : 1.f};
     cudaStream_t st = (cudaStream_t)stream;
@@ -403,7 +414,7 @@ static int trace_impl(const qsl_field_t* field, const qsl_field_t* cur_field, co
     switch (field->layout) {
         case LAYOUT_SOA: return go(soa_of(field));
         case LAYOUT_F4: return go(f4_of(field));
-        case LAYOUT_H4B: return go(h4b_of(field));
+        case LAYOUT_H4B: return prm->arith == QSL_ARITH_FAST_W16 ? go(h4bw_of(field)) : go(h4b_of(field));
         default: return go(h8c_of(field));
     }
 }
@@ -478,6 +489,8 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (!Bx || !By || !Bz || !x_arr || !y_arr || !z_arr) return fail(QSL_ERR_INVALID, "null field or coordinates");
     if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
     if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
+    if (prm->arith == QSL_ARITH_FAST_W16)
+        return fail(QSL_ERR_INVALID, "fp16 x weights (QSL_ARITH_FAST_W16) are a qsl_trace option of the h4b layout");
     if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
     if (n == 0) return QSL_OK;
     if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
@@ -881,6 +894,8 @@ int qsl_trace_scott(const qsl_field_t* field, const qsl_trace_params* prm, const
     if (!field) return fail(QSL_ERR_INVALID, "field is null");
     if (!params_ok(prm) || prm->integrator != QSL_RKF45)
         return fail(QSL_ERR_INVALID, "bad trace params (the Scott tracer is RKF45)");
+    if (prm->arith == QSL_ARITH_FAST_W16)
+        return fail(QSL_ERR_INVALID, "fp16 x weights (QSL_ARITH_FAST_W16) are a qsl_trace option of the h4b layout");
     if (grad_mode != QSL_GRAD_FD && grad_mode != QSL_GRAD_ANALYTIC) return fail(QSL_ERR_INVALID, "bad grad_mode");
     if (prm->arith == QSL_ARITH_EXACT && (grad_mode != QSL_GRAD_FD || field->layout != LAYOUT_SOA))
         return fail(QSL_ERR_INVALID, "exact arithmetic needs the SoA layout and QSL_GRAD_FD");

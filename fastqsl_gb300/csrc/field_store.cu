@@ -24,10 +24,12 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
 //  * cell j: the reference's search at c = a[j+1] (its comparisons c > a[m]
 //    come out the same for every c in (a[j], a[j+1]], and it never compares
 //    with a[0], so a coordinate pinned at a[0] gets cell 0's answer too);
-//  * bin b: the cells of its edges moved out by 1 % of a bin (in double),
-//    each the largest j <= n-2 with a[j] below the edge (0 if none).  A
-//    coordinate the kernel puts in bin b lies within those edges, so its
-//    interval is in the range.
+//  * bin b: the cells of its edges moved out by 1 % of a bin plus the float
+//    rounding of the kernel's bin index ((c - a0) * binv, a few ulp of a
+//    value up to nb: 4e-7 nb bins covers it), in double, each the largest
+//    j <= n-2 with a[j] below the edge (0 if none).  A coordinate the
+//    kernel puts in bin b lies within those edges, so its interval is in the
+//    range, on axes of any length.
 __device__ __forceinline__ int stretch_cell_below(double c, int n, const float* __restrict__ a) {
     int lo = 0, hi = n - 2;  // largest j in [0, n-2] with a[j] < c, else 0
     while (lo < hi) {
@@ -59,8 +61,9 @@ __global__ void k_stretch_tables(const float* __restrict__ ax, const float* __re
             const int b = t - cells - STRETCH_BINS_PER_CELL * c0;
             const int nb = STRETCH_BINS_PER_CELL * (n - 1);
             const double a0 = __ldg(a), w = ((double)__ldg(a + n - 1) - a0) / nb;
-            const int lo = stretch_cell_below(a0 + (b - 0.01) * w, n, a);
-            const int hi = stretch_cell_below(a0 + (b + 1.01) * w, n, a);
+            const double wid = 0.01 + 4e-7 * (double)nb;
+            const int lo = stretch_cell_below(a0 + (b - wid) * w, n, a);
+            const int hi = stretch_cell_below(a0 + (b + 1 + wid) * w, n, a);
             sbin[t - cells] = make_int2(lo, hi < lo ? lo : hi);
         }
     }

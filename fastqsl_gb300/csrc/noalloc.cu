@@ -26,11 +26,34 @@ constexpr long long kScratchBytes = QSL_NOALLOC_SCRATCH_BYTES;
 __device__ __align__(256) unsigned char g_cook_scratch[kScratchBytes];
 
 // Host code cannot use g_cook_scratch's name as a device address; its
-// address on each device is looked up once, with that device current.
+// address on each device is looked up once, with that device current, and
+// again whenever the device's current context is a different one (after
+// cudaDeviceReset the module is loaded anew and the array may move).  The
+// context handle comes from the driver's cuCtxGetCurrent, reached through the
+// runtime's entry-point query so the library needs no link to libcuda.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_addr[kMaxDevices];
+void* g_scratch_ctx[kMaxDevices];
 bool g_scratch_ready[kMaxDevices];
+
+typedef int (*ctx_get_current_t)(void**);
+
+void* current_context() {
+    static ctx_get_current_t fn = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (ctx_get_current_t)f;
+        looked = true;
+    }
+    void* ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
 
 int scratch_on_current_device(void** out) {
     int dev = -1;
@@ -38,7 +61,7 @@ int scratch_on_current_device(void** out) {
     if (e != cudaSuccess) return qsl::set_error(QSL_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return qsl::set_error(QSL_ERR_INVALID, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ready[dev]) {
+    if (!g_scratch_ready[dev] || g_scratch_ctx[dev] != current_context()) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_cook_scratch);
         if (e != cudaSuccess || p == nullptr) {
@@ -47,6 +70,9 @@ int scratch_on_current_device(void** out) {
             return qsl::set_error(QSL_ERR_CUDA, msg);
         }
         g_scratch_addr[dev] = p;
+        // taken after the lookup, which makes the device's primary context
+        // current if no context was
+        g_scratch_ctx[dev] = current_context();
         g_scratch_ready[dev] = true;
     }
     *out = g_scratch_addr[dev];

@@ -27,7 +27,7 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
     const bool tw_on = TWIST && J.s.twist_on != 0;
     store_prepare(f);
     float len_lim;
-    if constexpr (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldF4>::value ||
+    if constexpr (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldH4BW>::value || std::is_same<F, FieldF4>::value ||
                   std::is_same<F, FieldH8C>::value)
         len_lim = J.lim.len_lim;
     else
@@ -41,7 +41,8 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
             const float3 be = sample_endpoint<false>(f, L.out);
             ns += 1;
             o.end_x[i] = L.out.x; o.end_y[i] = L.out.y; o.end_z[i] = L.out.z;
-            o.flag_end[i] = L.flag;
+            o.flag_end[i] = lane_flag(L.flag);
+            if (o.status_end) o.status_end[i] = lane_status(L.flag);
             o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
             o.line_len[i] = (double)L.len;
             if (TWIST && tw_on) o.twist[i] = L.tw;
@@ -53,7 +54,8 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
         const float3 b0 = sample_endpoint<false>(f, p0);
         ns += 2;
         o.start_x[i] = L.out.x; o.start_y[i] = L.out.y; o.start_z[i] = L.out.z;
-        o.flag_start[i] = L.flag;
+        o.flag_start[i] = lane_flag(L.flag);
+        if (o.status_start) o.status_start[i] = lane_status(L.flag);
         o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
         o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
         o.line_len[i] = o.line_len[i] + (double)L.len;

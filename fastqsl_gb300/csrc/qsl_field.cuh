@@ -150,6 +150,10 @@ struct FieldH4B {
         return __ldg(scale + brick);
     }
 };
+// The same brick store sampled with fp16 x weights (QSL_ARITH_FAST_W16, an
+// opt-in of qsl_trace): a distinct type so that its kernels are compiled
+// apart and the default sampler keeps FP32 weights.
+struct FieldH4BW : FieldH4B {};
 
 // fp16 cell records.  Record (64 bytes, 32-byte aligned) as 16 32-bit words:
 // w[0..3] Bx, w[4..7] By, w[8..11] Bz, where word k of a component is the
@@ -227,7 +231,8 @@ struct FieldStretchT {
     //            {a[i], a[i+1] - a[i], i as int bits, 0}
     //   sbin[b]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins over [a[0],
     //            a[n-1]] per axis: the lowest and highest cell a coordinate
-    //            of the bin (widened by 1 % of a bin) can lie in
+    //            of the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
+    //            float rounding of the bin index) can lie in
     const float4* srec;
     const int2* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
@@ -392,17 +397,69 @@ __device__ __forceinline__ float3 sample_unit_raw<FieldF4>(const FieldF4& f, flo
 }
 
 // ---------------------------------------------------------------------------
-// Fast sampling of the fp16 brick store without fp16->fp32 conversions.
+// Fast sampling of the fp16 stores: FP32 interpolation of fp16 node values.
+//
+// The x-lerp of a corner pair (a, b) is a + r (b - a) in FP32 with the FP32
+// fraction r: a widened exactly and b - a rounded once to f32, both by the
+// mixed-precision multiply-add (fma.rn.f32.f16 with an f16 one: the product
+// is exact, the sum rounded once; it issues on the FMA pipe, where
+// cvt.f32.f16 and sub.rn.f32.f16 go to the narrower fp16 pipe, measured
+// 0.5 % slower), then one f32 multiply-add, the (Bx, By) pair on the packed
+// f32x2 pipe.  The y and z lerps run on packed f32 pairs as well.  Every
+// weight and every operation is FP32; only the stored node values are fp16.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void xdiff_h4(uint2 lo, uint2 hi, float2& axy, float& az, float2& dxy, float& dz) {
+    // the widening and the difference as mixed-precision multiply-adds by
+    // an f16 one (a x 1 + 0 = a exactly; b x 1 - a rounded once = b - a)
+    asm("{\n\t"
+        ".reg .f16 a0, a1, a2, a3, b0, b1, b2, b3, one;\n\t"
+        ".reg .f32 n0, n1, n2;\n\t"
+        "mov.b16 one, 0x3C00;\n\t"
+        "mov.b32 {a0, a1}, %6;\n\t"
+        "mov.b32 {a2, a3}, %7;\n\t"
+        "mov.b32 {b0, b1}, %8;\n\t"
+        "mov.b32 {b2, b3}, %9;\n\t"
+        "fma.rn.f32.f16 %0, a0, one, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %1, a1, one, 0f00000000;\n\t"
+        "fma.rn.f32.f16 %2, a2, one, 0f00000000;\n\t"
+        "neg.f32 n0, %0;\n\t"
+        "neg.f32 n1, %1;\n\t"
+        "neg.f32 n2, %2;\n\t"
+        "fma.rn.f32.f16 %3, b0, one, n0;\n\t"
+        "fma.rn.f32.f16 %4, b1, one, n1;\n\t"
+        "fma.rn.f32.f16 %5, b2, one, n2;\n\t"
+        "}"
+        : "=f"(axy.x), "=f"(axy.y), "=f"(az), "=f"(dxy.x), "=f"(dxy.y), "=f"(dz)
+        : "r"(lo.x), "r"(lo.y), "r"(hi.x), "r"(hi.y));
+}
+
+// a + r (b - a) of one fp16 pair (low half a, high half b) in FP32.
+__device__ __forceinline__ float xmix_f32(unsigned pair, float r) {
+    float a, d;
+    asm("{\n\t"
+        ".reg .f16 l, h, one;\n\t"
+        ".reg .f32 n;\n\t"
+        "mov.b16 one, 0x3C00;\n\t"
+        "mov.b32 {l, h}, %2;\n\t"
+        "fma.rn.f32.f16 %0, l, one, 0f00000000;\n\t"
+        "neg.f32 n, %0;\n\t"
+        "fma.rn.f32.f16 %1, h, one, n;\n\t"
+        "}"
+        : "=f"(a), "=f"(d)
+        : "r"(pair));
+    return fmaf(d, r, a);
+}
+
+// ---------------------------------------------------------------------------
+// The fp16-weight sampler of the brick store (opt-in, QSL_ARITH_FAST_W16).
 //
 // The x-lerp of each corner pair reads the fp16 components directly with the
 // mixed-precision multiply-add (fma.rn.f32.f16: the f16 x f16 product is exact
-// and the sum is rounded once to f32); the y and z lerps run on packed f32
-// pairs (fma.rn.f32x2) for (Bx, By) and scalar f32 for Bz.  The x weights
-// enter as fp16: in the brick store (1 - r, r) each rounded to fp16 (their
-// sum is 1 within 2^-11, which a normalised sample does not see), in the
-// cell-record store r rounded to the 2^-11 grid first so that both weights
-// are exact and sum to 1 (the fp16 node values themselves carry a relative
-// rounding of up to 2^-12).
+// and the sum is rounded once to f32), with the x weights (1 - r, r) each
+// rounded to fp16 (their sum is 1 within 2^-11, which a normalised sample
+// does not see): the x fraction is quantised to ~2^-11.  Fewer instructions
+// per sample than the FP32 form; its own error figures are stated wherever
+// it is measured.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void xlerp_h4(uint2 lo, uint2 hi, unsigned w, float& x, float& y, float& z) {
     asm("{\n\t"
@@ -430,16 +487,14 @@ __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float o, float r) {
 }
 
 // The trilinear value at p in brick units (times the brick's scale = B).
+// W16 = false: FP32 x-lerps (xdiff_h4); true: fp16 x weights (xlerp_h4).
+template <bool W16>
 __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsigned& brick_out) {
     int ix, iy, iz;
     float rx, ry, rz;
     locate_fast(p.x, f.d.nx, ix, rx);
     locate_fast(p.y, f.d.ny, iy, ry);
     locate_fast(p.z, f.d.nz, iz, rz);
-    // the x weights (1 - rx, rx) rounded to fp16 each (they sum to 1 within
-    // 2^-11; a normalised sample does not see their sum)
-    const __half2 wh = __floats2half2_rn(1.f - rx, rx);
-    const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
     // the record index, with the z term (the only one that can pass 2^32) in
     // 64 bits
     const unsigned part = (unsigned)ix + 640u * (unsigned)(ix >> 3) + 8u * (unsigned)iy + f.ky * (unsigned)(iy >> 3) +
@@ -451,9 +506,32 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
     // e[(dy << 1) | dz]: x-lerped corner pairs
     float2 exy[4];
     float ez[4];
+    if constexpr (W16) {
+        // the x weights (1 - rx, rx) rounded to fp16 each
+        const __half2 wh = __floats2half2_rn(1.f - rx, rx);
+        const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-        xlerp_h4(make_uint2(u[q].x, u[q].y), make_uint2(u[q].z, u[q].w), w, exy[q].x, exy[q].y, ez[q]);
+        for (int q = 0; q < 4; ++q)
+            xlerp_h4(make_uint2(u[q].x, u[q].y), make_uint2(u[q].z, u[q].w), w, exy[q].x, exy[q].y, ez[q]);
+    } else {
+        float2 az[2], dz[2];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float2 axy, dxy;
+            float a, d;
+            xdiff_h4(make_uint2(u[q].x, u[q].y), make_uint2(u[q].z, u[q].w), axy, a, dxy, d);
+            exy[q] = __ffma2_rn(dxy, make_float2(rx, rx), axy);
+            if (q & 1) { az[q >> 1].y = a; dz[q >> 1].y = d; }
+            else { az[q >> 1].x = a; dz[q >> 1].x = d; }
+        }
+        // the Bz lerps of two corner pairs at a time on the packed pipe
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float2 e = __ffma2_rn(dz[k], make_float2(rx, rx), az[k]);
+            ez[2 * k] = e.x;
+            ez[2 * k + 1] = e.y;
+        }
+    }
     const float oy = 1.f - ry, oz = 1.f - rz;
     const float2 g0 = lerp2(exy[0], exy[2], oy, ry), g1 = lerp2(exy[1], exy[3], oy, ry);
     // the two z-column y-lerps as one packed pair
@@ -465,10 +543,10 @@ __device__ __forceinline__ float3 h4b_interp(const FieldH4B& f, float3 p, unsign
     return v3(rxy.x, rxy.y, fmaf(gz.y, rz, gz.x * oz));
 }
 
-template <>
-__device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, float3 p, bool unit) {
+template <bool W16>
+__device__ __forceinline__ float3 h4b_sample(const FieldH4B& f, float3 p, bool unit) {
     unsigned brick;
-    float3 r = h4b_interp(f, p, brick);
+    float3 r = h4b_interp<W16>(f, p, brick);
     if (unit) {
         const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
         const float2 xy = __fmul2_rn(make_float2(r.x, r.y), make_float2(inv, inv));
@@ -479,32 +557,31 @@ __device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, flo
     }
     return r;
 }
-
-template <>
-__device__ __forceinline__ float3 sample_unit_raw<FieldH4B>(const FieldH4B& f, float3 p, float3& raw) {
+template <bool W16>
+__device__ __forceinline__ float3 h4b_sample_unit_raw(const FieldH4B& f, float3 p, float3& raw) {
     unsigned brick;
-    const float3 r = h4b_interp(f, p, brick);
+    const float3 r = h4b_interp<W16>(f, p, brick);
     const float s = __ldg(f.scale + brick);
     raw = v3(r.x * s, r.y * s, r.z * s);
     const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
     return v3(r.x * inv, r.y * inv, r.z * inv);
 }
 
-// (1 - r) lo + r hi of one fp16 pair (w = the fp16 pair (1 - r, r)), the
-// products exact and the sum rounded once.
-__device__ __forceinline__ float xmix(unsigned pair, unsigned w) {
-    float d;
-    asm("{\n\t"
-        ".reg .f16 l, h, wo, wr;\n\t"
-        ".reg .f32 t;\n\t"
-        "mov.b32 {l, h}, %1;\n\t"
-        "mov.b32 {wo, wr}, %2;\n\t"
-        "fma.rn.f32.f16 t, l, wo, 0f00000000;\n\t"
-        "fma.rn.f32.f16 %0, h, wr, t;\n\t"
-        "}"
-        : "=f"(d)
-        : "r"(pair), "r"(w));
-    return d;
+template <>
+__device__ __forceinline__ float3 sample<false, FieldH4B>(const FieldH4B& f, float3 p, bool unit) {
+    return h4b_sample<false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample_unit_raw<FieldH4B>(const FieldH4B& f, float3 p, float3& raw) {
+    return h4b_sample_unit_raw<false>(f, p, raw);
+}
+template <>
+__device__ __forceinline__ float3 sample<false, FieldH4BW>(const FieldH4BW& f, float3 p, bool unit) {
+    return h4b_sample<true>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample_unit_raw<FieldH4BW>(const FieldH4BW& f, float3 p, float3& raw) {
+    return h4b_sample_unit_raw<true>(f, p, raw);
 }
 
 // 32-byte read-only load (one L1 sector); p must be 32-byte aligned.
@@ -515,8 +592,8 @@ __device__ __forceinline__ void ldg_v8(const void* p, unsigned (&v)[8]) {
 }
 
 // Fast sample of the cell-record store: the same arithmetic as the fp16
-// brick store's fast sample (x fraction on the 2^-11 grid, fp16 x-lerps by
-// mixed-precision FMA, packed y/z lerps), with Bx/By in one 32-byte load
+// brick store's fast sample (FP32 x-lerps of the fp16 pairs, packed y/z
+// lerps), with Bx/By in one 32-byte load
 // (WIDE) or two 16-byte loads, and Bz in one 16-byte load.  The 32-byte load
 // is used in code inlined into kernels only: ptxas 13.0 fails (segmentation
 // fault) on it inside an out-of-line device function called from several
@@ -528,9 +605,6 @@ __device__ __forceinline__ float3 sample_h8c(const FieldH8C& f, float3 p, bool u
     locate_fast(p.x, f.d.nx, ix, rx);
     locate_fast(p.y, f.d.ny, iy, ry);
     locate_fast(p.z, f.d.nz, iz, rz);
-    const float rq = rintf(rx * 2048.f) * (1.f / 2048.f);
-    const __half2 wh = __floats2half2_rn(1.f - rq, rq);  // exact: both on the 2^-11 grid
-    const unsigned w = *reinterpret_cast<const unsigned*>(&wh);
     const uint4* r = f.record(ix, iy, iz);
     uint4 bx, by;
     if (WIDE) {
@@ -543,9 +617,12 @@ __device__ __forceinline__ float3 sample_h8c(const FieldH8C& f, float3 p, bool u
         by = __ldg(r + 1);
     }
     const uint4 bz = __ldg(r + 2);
-    const float2 e0 = make_float2(xmix(bx.x, w), xmix(by.x, w)), e1 = make_float2(xmix(bx.y, w), xmix(by.y, w)),
-                 e2 = make_float2(xmix(bx.z, w), xmix(by.z, w)), e3 = make_float2(xmix(bx.w, w), xmix(by.w, w));
-    const float ez0 = xmix(bz.x, w), ez1 = xmix(bz.y, w), ez2 = xmix(bz.z, w), ez3 = xmix(bz.w, w);
+    const float2 e0 = make_float2(xmix_f32(bx.x, rx), xmix_f32(by.x, rx)),
+                 e1 = make_float2(xmix_f32(bx.y, rx), xmix_f32(by.y, rx)),
+                 e2 = make_float2(xmix_f32(bx.z, rx), xmix_f32(by.z, rx)),
+                 e3 = make_float2(xmix_f32(bx.w, rx), xmix_f32(by.w, rx));
+    const float ez0 = xmix_f32(bz.x, rx), ez1 = xmix_f32(bz.y, rx), ez2 = xmix_f32(bz.z, rx),
+                ez3 = xmix_f32(bz.w, rx);
     const float oy = 1.f - ry, oz = 1.f - rz;
     const float2 g0 = lerp2(e0, e2, oy, ry), g1 = lerp2(e1, e3, oy, ry);
     const float gz0 = fmaf(ez2, ry, ez0 * oy), gz1 = fmaf(ez3, ry, ez1 * oy);

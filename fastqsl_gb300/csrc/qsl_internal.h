@@ -42,6 +42,9 @@ cudaError_t launch_trace_fast_h4b(const TraceJob<FieldH4B>& J, bool twist, Sched
                                   cudaStream_t st);
 cudaError_t launch_trace_fast_h8c(const TraceJob<FieldH8C>& J, bool twist, Schedule sched, long long n_host,
                                   cudaStream_t st);
+// trace_fast_h4bw.cu
+cudaError_t launch_trace_fast_h4bw(const TraceJob<FieldH4BW>& J, bool twist, Schedule sched, long long n_host,
+                                   cudaStream_t st);
 
 // Scott tracer (one line per thread); exact arithmetic uses GRAD_FD
 cudaError_t launch_scott_exact(const ScottJob<FieldSoA>& J, bool twist, long long n_grid, cudaStream_t st);

@@ -283,8 +283,21 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
                     if (fabsf(q1 - q2) > 0.f) {
                         qmid = (flag % 2 == 1) ? 0.f : (float)f.d.n(d);
                         e = div9(add9(mul9(q2 - qmid, a), mul9(qmid - q1, b)), q2 - q1);
-                        const float3 ua = sample<EXACT>(f, a.p, true);
-                        ns += 1;
+                        // the exit segment's length divides by the field's
+                        // component along the exit axis (B_P1, :448): with
+                        // the twist on, B at the point past the face as the
+                        // reference sets it (:425); with the twist off the
+                        // reference leaves B_P1 unset and the unit field at
+                        // the last inside point stands in (as in
+                        // TraceBlineAdaptive.cu:404).  The length gates the
+                        // second direction (the budget is shared).
+                        float3 ua;
+                        if (TWIST && tw_on) {
+                            ua = bp1;
+                        } else {
+                            ua = sample<EXACT>(f, a.p, true);
+                            ns += 1;
+                        }
                         len = len + (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(ua, d)));
                     } else {
                         e = a;

@@ -34,6 +34,8 @@ struct TraceOut {
     float *bend_x, *bend_y, *bend_z;
     double* line_len;
     double* twist;
+    int* status_start;  // optional qsl_line_status per direction
+    int* status_end;
 };
 
 // Scalars the reference passes as one-element device arrays are read from
@@ -336,11 +338,18 @@ struct Lane {
     float lc;      // Kahan compensation of len (fast arithmetic)
     double tw;     // accumulated twist
     int steps;     // accepted steps
+    int rej;       // trial steps rejected in a row
     int dir;       // +1 forward, -1 backward
     long long line;
     float3 out;    // footpoint of this direction when finished
-    int flag;
+    int flag;      // reference flag; bits 8.. hold the qsl_line_status when finished
 };
+
+// The reference flag and the qsl_line_status of a finished direction
+// (packed into Lane::flag so that the status costs no register in the loop).
+__device__ __forceinline__ int lane_flag(int packed) { return packed & 0xff; }
+__device__ __forceinline__ int lane_status(int packed) { return packed >> 8; }
+__device__ __forceinline__ int pack_flag(int flag, int status) { return flag | (status << 8); }
 
 template <bool EXACT>
 __device__ __forceinline__ void len_add(Lane<EXACT>& L, double x_exact, float x_fast) {
@@ -366,6 +375,7 @@ __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lan
     L.lc = 0.f;
     L.tw = 0.0;
     L.steps = 0;
+    L.rej = 0;
     L.flag = 0;
     L.out = L.p;
     L.tol = 0.f;
@@ -403,9 +413,10 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
                                           unsigned& ns) {
     const qsl_trace_params& pr = J.prm;
     const bool more_steps = EXACT ? ((long long)L.steps < pr.max_steps) : (L.steps < J.lim.max_steps);
-    if (!((L.len < len_lim) & more_steps)) {
+    const bool more_len = L.len < len_lim;
+    if (!(more_len & more_steps)) {
         L.out = L.p;
-        L.flag = 0;
+        L.flag = pack_flag(0, more_len ? QSL_LINE_MAX_STEPS : QSL_LINE_MAX_LENGTH);
         return true;
     }
     const float hd = L.h * (float)L.dir;
@@ -421,6 +432,11 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
             scale = pow_cr((float)((double)(L.tol / err) / 11.09), 0.2f);
             if ((double)scale < 0.618) {
                 L.h = (float)((double)L.h * pr.reject_factor);
+                if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
+                    L.out = L.p;
+                    L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
+                    return true;
+                }
                 return false;
             }
         } else {
@@ -429,9 +445,15 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
             scale = ex2_approx(0.2f * __log2f(__fdividef(L.tol, err) * (float)(1.0 / 11.09)));
             if (scale < 0.618f) {
                 L.h = L.h * J.lim.reject;
+                if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
+                    L.out = L.p;
+                    L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
+                    return true;
+                }
                 return false;
             }
         }
+        L.rej = 0;
         float h = L.h * scale;
         if (EXACT) {
             if ((double)h > pr.h_max) h = (float)pr.h_max;
@@ -507,7 +529,8 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
         } else {
             L.out = p2;
         }
-        L.flag = flag;
+        const bool finite = isfinite(p2.x) & isfinite(p2.y) & isfinite(p2.z);
+        L.flag = pack_flag(flag, flag <= 6 ? QSL_LINE_FACE : (finite ? QSL_LINE_EDGE : QSL_LINE_NAN));
         L.p = p2;
         L.steps++;
         return true;
@@ -563,7 +586,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     // kernel parameter (a register would be re-formed from the double
     // product at every step once the loop runs short of registers)
     typename Lane<EXACT>::len_t len_lim;
-    if constexpr (!EXACT && (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldF4>::value ||
+    if constexpr (!EXACT && (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldH4BW>::value || std::is_same<F, FieldF4>::value ||
                              std::is_same<F, FieldH8C>::value))
         len_lim = J.lim.len_lim;
     else
@@ -638,7 +661,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
                 const float3 be = sample_endpoint<EXACT>(f, pe);
                 ns += 1;
                 o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
-                o.flag_end[i] = L.flag;
+                o.flag_end[i] = lane_flag(L.flag);
+                if (o.status_end) o.status_end[i] = lane_status(L.flag);
                 o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
                 o.line_len[i] = (double)L.len;
                 if (TWIST && tw_on) o.twist[i] = L.tw;
@@ -650,7 +674,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
                 const float3 b0 = sample_endpoint<EXACT>(f, p0);
                 ns += 2;
                 o.start_x[i] = ps.x; o.start_y[i] = ps.y; o.start_z[i] = ps.z;
-                o.flag_start[i] = L.flag;
+                o.flag_start[i] = lane_flag(L.flag);
+                if (o.status_start) o.status_start[i] = lane_status(L.flag);
                 o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
                 o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
                 o.line_len[i] = o.line_len[i] + (double)L.len;

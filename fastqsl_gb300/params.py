@@ -10,6 +10,9 @@ the presets below reproduce them:
   rejection, length limit 3*(nx+ny+nz), 500000 steps.
 * Scott — ``fastqslpy/cu/TraceBlineScott.cu:10-14``: length limit
   2*(nx+ny+nz), 10000 steps shared by both directions, tol 1e-3*tol_coef.
+* ``max_rejects`` (no counterpart in the reference, 0 in its presets): the
+  number of rejected trial steps in a row that ends a direction.
+
 * Stretched-grid RKF45 — ``fastqslpy/cu/TraceBlineAdaptiveStretch.cu:10-12,
   336-371``: the RKF45 settings with length limit 2 x the summed coordinate
   extents, no step limit (capped here at 2^31 - 1), exit-segment twist term
@@ -23,6 +26,23 @@ TOL_REFERENCE = 0
 TOL_ABSOLUTE = 1
 ARITH_EXACT = 0
 ARITH_FAST = 1
+# qsl_trace on the fp16 brick store only: fp16 x weights (opt-in, see
+# QSL_ARITH_FAST_W16 in include/fastqsl_gb300.h)
+ARITH_FAST_W16 = 2
+
+# qsl_line_status: how one direction of a line ended
+LINE_FACE = 0
+LINE_EDGE = 1
+LINE_NAN = 2
+LINE_MAX_STEPS = 3
+LINE_MAX_LENGTH = 4
+LINE_REJECT_LIMIT = 5
+
+# Rejected trial steps in a row that end a direction in the absolute-
+# tolerance preset: 64 rejections shrink the step by 0.618^64 ~ 4e-14, far
+# below what a float position can resolve, so a controller that has not
+# accepted by then never will (the reference presets keep 0, no limit).
+MAX_REJECTS = 64
 
 
 class TraceParams(ctypes.Structure):
@@ -37,6 +57,7 @@ class TraceParams(ctypes.Structure):
         ("max_steps", ctypes.c_int64),
         ("boundary_twist", ctypes.c_int32),
         ("arith", ctypes.c_int32),
+        ("max_rejects", ctypes.c_int32),
     ]
 
     def copy(self, **kw):
@@ -71,10 +92,11 @@ def reference_stretch(arith=ARITH_EXACT) -> TraceParams:
     return TraceParams(RKF45, TOL_REFERENCE, 1e-3, 0.1, 100.0, 0.618, 2.0, 2**31 - 1, 1, arith)
 
 
-def absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=ARITH_FAST) -> TraceParams:
+def absolute_rkf45(tol=1e-4, h_min=1e-3, h_max=1.0, arith=ARITH_FAST, max_rejects=MAX_REJECTS) -> TraceParams:
     """RKF45 with an absolute local tolerance and explicit step bounds (the
-    benchmark settings: tol 1e-4, h in [1e-3, 1])."""
-    return TraceParams(RKF45, TOL_ABSOLUTE, tol, h_min, h_max, 0.618, 3.0, 500000, 0, arith)
+    benchmark settings: tol 1e-4, h in [1e-3, 1]); a direction ends where
+    `max_rejects` trial steps in a row were rejected (status REJECT_LIMIT)."""
+    return TraceParams(RKF45, TOL_ABSOLUTE, tol, h_min, h_max, 0.618, 3.0, 500000, 0, arith, max_rejects)
 
 
 def fixed_rk4(max_steps=100000, len_ratio=2.0, arith=ARITH_EXACT) -> TraceParams:

@@ -503,9 +503,81 @@ def fluid_schedule(arrival, work, cap, capacity=1.0, policy="srpt"):
     return done
 
 
-def ideal_bound(requests, isolated, saturated_span, policies=("srpt", "ps")):
+def _deadlines_feasible(arrival, work, cap, deadline, capacity):
+    """Whether the fluid server (capacity per second, job i at most cap[i]
+    per second, preemption free) can finish every job i between arrival[i]
+    and deadline[i]: a transportation problem between jobs and the intervals
+    of time their windows share, solved as a maximum flow (source -> job:
+    its work; job -> interval inside its window: cap x length; interval ->
+    sink: capacity x length).  Amounts are counted in integer units with
+    every capacity rounded up and every work rounded down, so the test can
+    only err towards feasible (a bound built on it stays a lower bound)."""
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import maximum_flow
+    n = len(arrival)
+    pts = np.unique(np.concatenate([arrival, deadline]))
+    lo, hi = pts[:-1], pts[1:]
+    length = hi - lo
+    m = len(length)
+    # integer unit: the total work spread over ~2^30 units
+    unit = max(float(work.sum()), 1e-300) / float(1 << 30)
+    src, snk = 0, 1 + n + m
+    rows, cols, caps = [], [], []
+    for i in range(n):
+        k0 = int(np.searchsorted(pts, arrival[i], side="left"))
+        k1 = int(np.searchsorted(pts, deadline[i], side="left"))
+        if k1 <= k0:
+            continue
+        ks = np.arange(k0, k1)
+        rows.append(np.full(len(ks), 1 + i))
+        cols.append(1 + n + ks)
+        caps.append(np.ceil(cap[i] * length[ks] / unit))
+    rows.append(np.zeros(n, np.int64))
+    cols.append(1 + np.arange(n))
+    need = np.floor(work / unit)
+    caps.append(need)
+    rows.append(1 + n + np.arange(m))
+    cols.append(np.full(m, snk))
+    caps.append(np.ceil(capacity * length / unit))
+    r, c, v = np.concatenate(rows), np.concatenate(cols), np.concatenate(caps)
+    v = np.minimum(v, 2**31 - 1).astype(np.int32)
+    g = csr_matrix((v, (r.astype(np.int32), c.astype(np.int32))), shape=(snk + 1, snk + 1))
+    g.sum_duplicates()
+    return maximum_flow(g, src, snk).flow_value >= int(need.sum())
+
+
+def min_max_stretch(arrival, work, cap, isolated, capacity=1.0, rel=1e-3):
+    """A lower bound, within `rel`, on the largest ratio of response time to
+    isolated time that any schedule of the jobs on the fluid server reaches
+    (fluid_schedule's model): the smallest s for which every job i can
+    finish by arrival[i] + s * isolated[i] (bisection on s over the
+    feasibility test; s >= 1, and no schedule beats s by more than `rel`).
+    Minimising the largest ratio is not what SRPT does (it minimises the
+    mean response time), so this is the floor for a worst-request figure."""
+    arrival = np.asarray(arrival, float)
+    work = np.asarray(work, float)
+    cap = np.asarray(cap, float)
+    iso = np.asarray(isolated, float)
+    if len(arrival) == 0:
+        return 1.0
+    hi = max(1.0, float(np.max((fluid_schedule(arrival, work, cap, capacity, "srpt") - arrival) / iso)))
+    lo = 1.0
+    if _deadlines_feasible(arrival, work, cap, arrival + lo * iso, capacity):
+        return lo
+    while hi - lo > rel * lo:
+        mid = 0.5 * (lo + hi)
+        if _deadlines_feasible(arrival, work, cap, arrival + mid * iso, capacity):
+            hi = mid
+        else:
+            lo = mid
+    return lo
+
+
+def ideal_bound(requests, isolated, saturated_span, policies=("srpt", "ps"), min_max=False):
     """p50/p99 of latency / isolated solve that an ideal fluid scheduler
-    (free preemption, perfect sharing of the GPU) reaches on `requests`.
+    (free preemption, perfect sharing of the GPU) reaches on `requests`
+    under each policy, and with `min_max` the smallest worst-request ratio
+    any schedule reaches (min_max_stretch).
 
     A request's work is its Q-pixels times the GPU time per Q-pixel of the
     most efficient isolated solve at its tolerance (the largest requests fill
@@ -527,22 +599,41 @@ def ideal_bound(requests, isolated, saturated_span, policies=("srpt", "ps")):
     for pol in policies:
         ratio = (fluid_schedule(arrival, work, cap, capacity, pol) - arrival) / iso
         out[pol] = [float(np.percentile(ratio, 50)), float(np.percentile(ratio, 99))]
+    if min_max:
+        out["min_max"] = min_max_stretch(arrival, work, cap, iso, capacity)
     return out
 
 
-def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6),
-          batched_server: QServer | None = None):
+def sweep(server: QServer, fields_shape, count=512, fractions=(0.5, 0.8), seed=7, seeds_range=(1e4, 4e6),
+          batched_server: QServer | None = None, keep_alone=8, alone_out: dict | None = None):
     """Isolated solve of every request, the saturated throughput (all
     requests at once), then Poisson streams at fractions of the saturated
     request rate.  With `batched_server` (e.g. one launching whole batches,
     chunk_lines=0) the saturated rate the fractions refer to is that
     server's, and `server`'s own saturated throughput is reported beside it.
-    Returns a dict of latency_stats per point."""
+    Returns a dict of latency_stats per point, each with the ideal fluid
+    scheduler's figures on the same stream built from the measured isolated
+    solves (SRPT and processor-sharing p50/p99, and the smallest worst-request
+    ratio any schedule reaches) beside this server's worst ratio.  The first
+    `keep_alone` requests' isolated results are compared with their results
+    in every stream ('alone_vs_mix_identical', bit for bit, NaN where NaN);
+    with `alone_out` they are also returned there ({rid: (request, Q)})."""
     names = sorted(server.fields)
     burst = make_requests(fields_shape, names, count, None, seed=seed, seeds_range=seeds_range)
-    iso = {r.rid: solve_alone(server, r)[0] for r in burst}
+    iso, alone = {}, {}
+    for r in burst:
+        iso[r.rid], q = solve_alone(server, r)
+        if r.rid < keep_alone:
+            alone[r.rid] = q
+            if alone_out is not None:
+                alone_out[r.rid] = (r, q)
+
+    def same_as_alone(done):
+        hit = [r for r in done if r.rid in alone]
+        ok = sum(1 for r in hit if np.array_equal(r.result, alone[r.rid], equal_nan=True))
+        return f"{ok}/{len(hit)}"
     done = (batched_server or server).run_stream(burst)
-    sat = latency_stats(done, iso)
+    sat = dict(latency_stats(done, iso), alone_vs_mix_identical=same_as_alone(done))
     span = max(r.t_done for r in done) - min(r.t_submit for r in done)
     sat_rate = count / span
     res = {"saturated": sat, "isolated_p50_s": float(np.median(list(iso.values())))}
@@ -554,7 +645,11 @@ def sweep(server: QServer, fields_shape, count=48, fractions=(0.5, 0.8), seed=7,
         done = server.run_stream(reqs)
         st = dict(latency_stats(done, iso), offered_req_per_s=f * sat_rate)
         # what an ideal fluid scheduler reaches on the same stream: [p50, p99]
-        st["ideal_fluid_p50_p99_over_isolated"] = ideal_bound(reqs, iso, span)
+        ideal = ideal_bound(reqs, iso, span, min_max=True)
+        st["ideal_min_max_over_isolated"] = ideal.pop("min_max")
+        st["ideal_fluid_p50_p99_over_isolated"] = ideal
+        st["max_over_isolated"] = float(max(r.latency / iso[r.rid] for r in done))
+        st["alone_vs_mix_identical"] = same_as_alone(done)
         for c in range(len(server.classes)):
             rr = [r.latency / iso[r.rid] for r in done if r.meta["class"] == c]
             if rr:

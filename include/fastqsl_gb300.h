@@ -54,8 +54,14 @@ enum qsl_arith {
      * fused multiply-add: corner weights in FP64, IEEE divide and sqrt. */
     QSL_ARITH_EXACT = 0,
     /* FP32 with fused multiply-add, FP32 corner weights and rsqrt
-     * normalisation. */
-    QSL_ARITH_FAST = 1
+     * normalisation.  On the fp16 stores the node values are widened exactly
+     * and every lerp is FP32. */
+    QSL_ARITH_FAST = 1,
+    /* qsl_trace on the QSL_LAYOUT_H4B store only: QSL_ARITH_FAST with the x
+     * weights (1 - r, r) rounded to fp16 and the x-lerps done by the
+     * mixed-precision f16 x f16 + f32 multiply-add (fewer instructions per
+     * sample; the x fraction is quantised to ~2^-11).  Rejected elsewhere. */
+    QSL_ARITH_FAST_W16 = 2
 };
 
 /* Integrator settings.  qsl_params_reference_rk4/_rkf45 fill the values the
@@ -71,7 +77,23 @@ typedef struct qsl_trace_params {
     int64_t max_steps;       /* accepted steps per direction; ref 500000 (RKF45), 100000 (RK4) */
     int32_t boundary_twist;  /* add the exit-segment twist term (RK4 reference does, TraceBline.cu:362-365) */
     int32_t arith;           /* qsl_arith */
+    int32_t max_rejects;     /* RKF45: this many rejected trial steps in a row end the direction where
+                                it is (flag 0, status QSL_LINE_REJECT_LIMIT); 0 = no limit, as in the
+                                reference, whose controller then only stops when the step size
+                                underflows and the position turns non-finite (flag 42) */
 } qsl_trace_params;
+
+/* How one direction of a line ended (the optional status_start / status_end
+ * outputs of qsl_trace_io; the reference reports only the flag, which is 0
+ * for every limit and 42 for edges, corners and non-finite positions alike). */
+enum qsl_line_status {
+    QSL_LINE_FACE = 0,         /* left through a face: flag 1..6 */
+    QSL_LINE_EDGE = 1,         /* left through an edge or corner: flag 42, finite position */
+    QSL_LINE_NAN = 2,          /* the position became non-finite (NaN/Inf field or step): flag 42 */
+    QSL_LINE_MAX_STEPS = 3,    /* stopped by max_steps: flag 0 */
+    QSL_LINE_MAX_LENGTH = 4,   /* stopped by the length limit: flag 0 */
+    QSL_LINE_REJECT_LIMIT = 5  /* stopped by max_rejects: flag 0 */
+};
 
 void qsl_params_reference_rk4(qsl_trace_params *p_h);
 void qsl_params_reference_rkf45(qsl_trace_params *p_h);
@@ -182,6 +204,8 @@ typedef struct qsl_trace_io {
     float *B_end_x, *B_end_y, *B_end_z;
     double *LineLen;
     double *twist; /* needed when curB is given */
+    int *status_start, *status_end; /* optional (null = not written): qsl_line_status of the
+                                       backward / forward direction */
 } qsl_trace_io;
 
 /* Scheduling of a trace launch (host struct; pointers are device pointers). */
@@ -459,7 +483,10 @@ int qsl_cook_pseudo_line(const int *B_flag, const float *x_start, const float *y
  * qsl_cook_noalloc_max_pixels() (about 358 million pixels) and larger
  * requests return QSL_ERR_TOO_LARGE.  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls on a device
+ * make that first call before any stream capture.  A call that finds a
+ * different current context on the device (after cudaDeviceReset) looks the
+ * address up again, so make the first call after a reset outside a capture
+ * too.  All calls on a device
  * share the one array: calls whose work overlaps on the GPU (other streams,
  * other host threads) race and must be serialised by the caller.  The
  * entry allocates nothing: no cudaMalloc, cudaFree or allocating library
@@ -485,6 +512,17 @@ int qsl_qcut(const float *start_x, const float *start_y, const float *start_z, c
 int qsl_qmerge(const int64_t *pix, const float *Qcut32, const double *Qcut64, int64_t count,
                const unsigned long long *count_dev, int64_t max_count, int n0, int n1, float *Qfinal32,
                double *Qfinal64, qsl_stream_t stream);
+
+/* Measurement helper with no reference counterpart: the L1 ceiling of the
+ * tracers' 16-byte field gathers.  Launches `blocks` blocks of 128 threads;
+ * each thread issues 8 * iters 16-byte read-only loads from `buf`
+ * (buf_bytes: a power of two from 4 KiB, small enough to stay in L1; the
+ * caller zeroes it), each warp request spread over `spread` 128-byte lines
+ * (1, 2, 4 = coalesced 512 bytes, 8, 16 or 32).  The caller times the launch
+ * on `stream`; bytes loaded = blocks * 128 * 8 * iters * 16.  `sink`: one
+ * device word the kernel may write. */
+int qsl_l1_probe(const void *buf, int64_t buf_bytes, int spread, int blocks, int iters, unsigned *sink,
+                 qsl_stream_t stream);
 
 #ifdef __cplusplus
 }

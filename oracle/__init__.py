@@ -139,8 +139,13 @@ SCOTT_KEYS_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
                   "B_this_x", "B_this_y", "B_this_z", "q_0", "q_perp"]
 
 
-def scott_all(impl, Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=None, curB=None, threads=None):
-    """Scott deviation-vector tracer (restated; see qsl_port.c header)."""
+def scott_all(impl, Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=None, curB=None, threads=None,
+              cross_dir=(0, 0, 1)):
+    """Scott deviation-vector tracer: the restatement (impl 'port32',
+    'port32cr', 'port64'; see qsl_port.c header) or 'ref_scott', the
+    reference's whole-line routine built from the copy with its tolerance
+    initialised (oracle/build_ref.sh; its settings are compiled in, `params`
+    is ignored, and it reports no line length)."""
     flat, shape = _field_ptrs(Bx, By, Bz)
     xs, ys, zs = _f32(xs), _f32(ys), _f32(zs)
     n = xs.size
@@ -151,6 +156,26 @@ def scott_all(impl, Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=Non
     out["twist"] = np.zeros(n, np.float64)
     twist_on = curB is not None
     cur = [np.asfortranarray(a, dtype=np.float32).ravel(order="F") for a in curB] if twist_on else [None] * 3
+    if impl == "ref_scott":
+        lib = ref_lib("scott")
+        if threads:
+            lib.qref_set_threads(int(threads))
+        cd = np.array(cross_dir, dtype=np.float32)
+        rc = lib.qref_scott_all(*[_p(a, _f32p) for a in flat], _p(shape, _i32p),
+                                *[(_p(a, _f32p) if a is not None else None) for a in cur], _p(out["twist"], _f64p),
+                                ctypes.c_int(int(twist_on)), _p(xs, _f32p), _p(ys, _f32p), _p(zs, _f32p),
+                                _p(cd, _f32p),
+                                _p(out["start_x"], _f32p), _p(out["start_y"], _f32p), _p(out["start_z"], _f32p),
+                                _p(out["flag_start"], _i32p),
+                                _p(out["end_x"], _f32p), _p(out["end_y"], _f32p), _p(out["end_z"], _f32p),
+                                _p(out["flag_end"], _i32p),
+                                _p(out["B_this_x"], _f32p), _p(out["B_this_y"], _f32p), _p(out["B_this_z"], _f32p),
+                                _p(out["q_0"], _f32p), _p(out["q_perp"], _f32p),
+                                ctypes.c_float(s_len), ctypes.c_ulonglong(n), ctypes.c_float(tol_coef))
+        if rc != 0:
+            raise RuntimeError(f"reference scott_all failed: {rc}")
+        del out["LineLen"]
+        return out
     lib = port_lib()
     fn = getattr(lib, _PREFIX[impl] + "scott_all")
     samples = ctypes.c_int64(0)

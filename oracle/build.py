@@ -20,7 +20,9 @@ ROOT = os.path.dirname(HERE)
 BUILD = os.path.join(HERE, "_build")
 PORT_SO = os.path.join(BUILD, "libqsl_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("QSL_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $QSL_REFERENCE_ROOT, else a directory named
+# `reference` beside this repository
+REFERENCE_ROOT = os.environ.get("QSL_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference"))
 
 # -fno-strict-aliasing: on aarch64, GCC 13 at -O2 produced wrong stretched-
 # grid samples of the port (differing from -O0, -O1 and every x86 build;

@@ -413,6 +413,7 @@ static dir_result trace_direction(fld *f, fld *cur, int twist_on, const qsl_trac
         tol = tol * tol_coef;
     }
 
+    int rej = 0; /* trial steps rejected in a row (max_rejects > 0 ends the direction there) */
     while ((flag == 0) & (len < len_lim) & (steps < pr->max_steps)) {
         v3 p2;
         if (rkf) {
@@ -421,8 +422,10 @@ static dir_result trace_direction(fld *f, fld *cur, int twist_on, const qsl_trac
             R scale = RPOW((R)((tol / err) / 11.09), (R)0.2);
             if (scale < 0.618) {
                 h = (R)(h * pr->reject_factor);
+                if (pr->max_rejects > 0 && ++rej >= pr->max_rejects) break;
                 continue;
             }
+            rej = 0;
             h = h * scale;
             if (h > pr->h_max) h = (R)pr->h_max;
             if (h < pr->h_min) h = (R)pr->h_min;
@@ -758,7 +761,14 @@ static scott_result trace_scott(fld *f, fld *cur, int twist_on, const qsl_trace_
                     if (RFABS(q1 - q2) > 0) {
                         qmid = (flag % 2 == 1) ? (R)0 : (R)n[d];
                         e = div9(add9(mul9(q2 - qmid, a), mul9(qmid - q1, b)), q2 - q1);
-                        v3 ua = sample_b(f, a.p, 1);
+                        /* the exit segment's length divides by the field's
+                         * component along the exit axis, B_P1 in the
+                         * reference (:448): with the twist on it is B at the
+                         * point past the face (:425); with it off the
+                         * reference leaves B_P1 unset, and the unit field at
+                         * the last inside point stands in (as in
+                         * TraceBlineAdaptive.cu:404) */
+                        v3 ua = twist_on ? bp1 : sample_b(f, a.p, 1);
                         len = len + RFABS(qmid - q1) / (1e-4 + RFABS(comp3(ua, d)));
                     } else {
                         e = a;

@@ -173,10 +173,10 @@ QREF_API int qref_trace_all(const float *Bx, const float *By, const float *Bz, c
 #endif
 
 #if REF_KERNEL == 3
-/* Scott-method building blocks (TraceBlineScott.cu:204-290).  The whole-line
- * routine TraceBlineScott reads an uninitialised tolerance
- * (TraceBlineScott.cu:352,378), so only these per-step functions are pinned
- * against the reference; the oracle restates the line loop. */
+/* Scott-method building blocks (TraceBlineScott.cu:204-290), and the
+ * whole-line routine TraceBlineScott (:334-519) from the copy of the file
+ * whose uninitialised tolerance (:352,378) build_ref.sh sets to
+ * TOL*tol_coef. */
 static float9 load9(const float *v)
 {
     float9 r;
@@ -212,6 +212,53 @@ QREF_API float qref_rkf45_scott(const float *Bx, const float *By, const float *B
     float err = RKF45_Scott((float *)Bx, (float *)By, (float *)Bz, shape_of(shape), load9(v9), &o, h);
     store9(o, out9);
     return err;
+}
+
+/* TraceBlineScott for seeds [0, n), as one thread of TraceAllBlineScott
+ * (:521-595) runs it, with its per-seed locals initialised here: the
+ * reference kernel leaves the exit flags unset when a line ends on the shared
+ * step limit, and the footpoints and q unset when a line ends on an edge or
+ * corner (flag 42), so those lines keep flag 0 and the footpoint/q outputs
+ * of such lines are whatever the routine left in its locals (the caller
+ * masks them).  B_this as the kernel computes it (:583-585).  The line
+ * length is not reported: the routine adds a term with B_P1, which it
+ * sets only when the twist is on (:448), so with the twist off it is not
+ * defined. */
+QREF_API int qref_scott_all(const float *Bx, const float *By, const float *Bz, const int *shape,
+                            const float *curBx, const float *curBy, const float *curBz, double *twist,
+                            int twist_flag, const float *inp_x, const float *inp_y, const float *inp_z,
+                            const float *cross_dir, float *start_x, float *start_y, float *start_z,
+                            int *flag_start, float *end_x, float *end_y, float *end_z, int *flag_end,
+                            float *B_this_x, float *B_this_y, float *B_this_z, float *q_0, float *q_perp,
+                            float s_len, unsigned long long n, float tol_coef)
+{
+    bool flag = twist_flag != 0;
+    if (flag && (!curBx || !curBy || !curBz || !twist)) return -1;
+    const float *cx = flag ? curBx : Bx, *cy = flag ? curBy : By, *cz = flag ? curBz : Bz;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long long i = 0; i < (long long)n; ++i) {
+        set_single_thread_launch();
+        int3 s3 = shape_of(shape);
+        float cd[3] = {cross_dir[0], cross_dir[1], cross_dir[2]};
+        float p0[3] = {inp_x[i], inp_y[i], inp_z[i]};
+        double tw = 0, len = 0;
+        bool f = flag;
+        int fs = 0, fe = 0;
+        float q0 = 0.f, qp = 0.f;
+        float9 pv = TraceBlineScott((float *)Bx, (float *)By, (float *)Bz, s3, (float *)cx, (float *)cy,
+                                    (float *)cz, &tw, &f, p0, cd, s_len, &fs, &fe, &q0, &qp, &len, tol_coef);
+        start_x[i] = pv.x.x; start_y[i] = pv.x.y; start_z[i] = pv.x.z;
+        end_x[i] = pv.z.x; end_y[i] = pv.z.y; end_z[i] = pv.z.z;
+        flag_start[i] = fs;
+        flag_end[i] = fe;
+        if (flag) twist[i] = tw;
+        B_this_x[i] = Interp3d((float *)Bx, s3, p0[0], p0[1], p0[2]);
+        B_this_y[i] = Interp3d((float *)By, s3, p0[0], p0[1], p0[2]);
+        B_this_z[i] = Interp3d((float *)Bz, s3, p0[0], p0[1], p0[2]);
+        q_0[i] = q0;
+        q_perp[i] = qp;
+    }
+    return 0;
 }
 #endif
 

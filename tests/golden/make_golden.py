@@ -1,6 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the REFERENCE itself.
 
-Run in a checkout where the reference exists (default /root/reference):
+Run where the reference checkout exists ($QSL_REFERENCE_ROOT, default: a
+directory named `reference` beside this repository):
 
     python oracle/build.py            # builds oracle/_ref from the reference sources
     python tests/golden/make_golden.py
@@ -9,7 +10,9 @@ What runs:
 * tracing — the reference's own kernels (fastqslpy/cu/TraceBline.cu,
   TraceBlineAdaptive.cu, TraceBlineScott.cu, TraceBlineAdaptiveStretch.cu),
   compiled for the host by
-  oracle/build_ref.sh (unmodified sources, -ffp-contract=off);
+  oracle/build_ref.sh (unmodified sources, -ffp-contract=off, except one
+  line of TraceBlineScott.cu in a copy: its uninitialised tolerance set to
+  TOL*tol_coef);
 * Q assembly — the reference's own fastqslpy/FastQSL.py (QCalcPlane,
   CookPseudoLine, ResReshape) imported with NumPy standing in for CuPy, and
   the pseudo-line Q cells of demo/Q_RKF45CuPy.ipynb (cells 9-11) executed
@@ -36,7 +39,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from fastqsl_gb300 import synthetic as S  # noqa: E402
 
-REF = os.environ.get("QSL_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("QSL_REFERENCE_ROOT", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def reference_fastqsl():
@@ -86,6 +89,32 @@ def stretch_case(name, seed, z_ratio, uni, twist=False, s_len=0.01, tol_coef=1.0
     meta = dict(kind="stretch", spec="bipole4_stretch", seed=seed, z_ratio=z_ratio, uni=uni, s_len=s_len,
                 tol_coef=tol_coef, twist=twist, fingerprint=S.field_fingerprint(Bx, By, Bz))
     save(name, meta=json.dumps(meta), inp_x=xs, inp_y=ys, inp_z=zs, xa=xa, ya=ya, za=za, **out)
+
+
+def scott_case(name, seed, twist):
+    """Whole-line TraceBlineScott (TraceBlineScott.cu:334-519) of the
+    reference, built from the copy with its tolerance initialised
+    (oracle/build_ref.sh), on bipole4_64: 40 x 36 seeds, all on z = 0
+    without the twist (the reference's second direction is defined there:
+    one direction of a bottom-plane seed is skipped), and with the twist
+    every third seed at z = 6.5 and one below z = 0 (with the twist on every
+    quantity the routine reads is set)."""
+    spec = S.bipole4_64(seed)
+    Bx, By, Bz = S.make_field(spec)
+    xs, ys, zs, shp = S.plane_seeds((2, 61), (2, 61), 40, 36, 0.0)
+    if twist:
+        zs[::3] = 6.5
+        zs[5] = -1.0
+    cur = (By * np.float32(0.3) + Bz, Bz - Bx, Bx * np.float32(0.5) + By) if twist else None
+    out = oracle.scott_all("ref_scott", Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, curB=cur)
+    meta = dict(kind="scott", spec="bipole4_64", seed=seed, s_len=0.25, tol_coef=1.0, twist=twist,
+                fingerprint=S.field_fingerprint(Bx, By, Bz))
+    save(name, meta=json.dumps(meta), inp_x=xs, inp_y=ys, inp_z=zs, **out)
+
+
+def scott_cases():
+    scott_case("scott_bipole4_64.npz", 2, False)
+    scott_case("scott_twist_bipole4_64.npz", 1, True)
 
 
 def curl_case():
@@ -251,6 +280,8 @@ def main():
         return stretch_cases()
     if sys.argv[1:] == ["curl"]:
         return curl_case()
+    if sys.argv[1:] == ["scott"]:
+        return scott_cases()
     trace_case("trace_rk4_bipole4_64.npz", "rk4", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 0.0, 0.1, 1.0)
     trace_case("trace_rkf45_bipole4_64.npz", "rkf45", S.bipole4_64, 0, ((0, 63), (0, 63), 64, 64), 1e-4,
                0.125, 0.5)
@@ -259,6 +290,7 @@ def main():
     trace_case("trace_rk4_twist_bipole4_64.npz", "rk4", S.bipole4_64, 1, ((2, 61), (2, 61), 40, 40), 0.0,
                0.1, 1.0, twist=True)
     probes_case()
+    scott_cases()
     qmap_case()
     stretch_cases()
     curl_case()

@@ -49,6 +49,18 @@ TRACE_CASES = {
     "trace_rk4_twist_bipole4_64.npz": ("rk4", True),
 }
 
+# whole-line TraceBlineScott fixtures: name -> twist on
+SCOTT_CASES = {"scott_bipole4_64.npz": False, "scott_twist_bipole4_64.npz": True}
+
+
+def scott_live(g):
+    """Seeds whose two directions both ended on a face (flags 1-6): the
+    reference routine leaves its footpoints and q unset on a line stopped by
+    the shared step limit, ended on an edge (flag 42), or skipped (z < 0)."""
+    fs, fe = g["flag_start"], g["flag_end"]
+    return (fs >= 1) & (fs <= 6) & (fe >= 1) & (fe <= 6)
+
+
 FOOT_KEYS = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
              "B_start_x", "B_start_y", "B_start_z", "B_end_x", "B_end_y", "B_end_z"]
 
@@ -68,3 +80,40 @@ def magtool_case(name="magtool_charges5.npz"):
     fp = [float(np.sum(B[0], dtype=np.float64)), float(np.sum(B[2], dtype=np.float64))]
     assert np.allclose(fp, g["fingerprint"], rtol=0, atol=1e-9 * max(1.0, abs(fp[0]))), "field generator changed"
     return g, B
+
+
+def fp16_exact_field(B, brick=8):
+    """A field the fp16 stores hold exactly: every 8^3-cell brick's largest
+    |component| (over its 9^3 nodes) raised to a power of two at that node,
+    then every node rounded to 11 significant bits of the largest such scale
+    among the bricks that hold it.  Dividing by a power-of-two scale and
+    rounding to fp16 then changes no value, so the brick store (per-brick
+    scale) and the cell-record store (per-cell power-of-two scale) see the
+    float32 field's own node values, and a trace on them differs from one on
+    the float32 field only by arithmetic."""
+    B = [np.array(b, np.float64) for b in B]
+    nx, ny, nz = B[0].shape
+    sls = [(slice(i, min(i + brick + 1, nx)), slice(j, min(j + brick + 1, ny)), slice(k, min(k + brick + 1, nz)))
+           for i in range(0, nx - 1, brick) for j in range(0, ny - 1, brick) for k in range(0, nz - 1, brick)]
+    for _ in range(50):
+        changed = 0
+        for sl in sls:
+            m = [np.abs(b[sl]).max() for b in B]
+            c = int(np.argmax(m))
+            if m[c] == 0:
+                continue
+            p = 2.0 ** np.ceil(np.log2(m[c]))
+            if p != m[c]:
+                blk = B[c][sl]
+                idx = np.unravel_index(np.argmax(np.abs(blk)), blk.shape)
+                blk[idx] = np.sign(blk[idx]) * p
+                changed += 1
+        if not changed:
+            break
+    E = np.full(B[0].shape, -200.0)
+    for sl in sls:
+        m = max(np.abs(b[sl]).max() for b in B)
+        if m > 0:
+            E[sl] = np.maximum(E[sl], np.log2(m))
+    q = 2.0 ** (E - 11)
+    return [np.asfortranarray((np.round(b / q) * q).astype(np.float32)) for b in B]

@@ -134,8 +134,9 @@ def test_notebook_workflow_through_dropin(cuda):
     assert np.median(d) <= 1e-6 and np.quantile(d, 0.99) <= 1e-2, (np.median(d), np.quantile(d, 0.99))
 
 
-@pytest.mark.parametrize("layout", ["f4", "soa", "h4b", "h8c"])
-def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
+@pytest.mark.parametrize("layout,arith", [("f4", P.ARITH_FAST), ("soa", P.ARITH_FAST), ("h4b", P.ARITH_FAST),
+                                          ("h8c", P.ARITH_FAST), ("h4b", P.ARITH_FAST_W16)])
+def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout, arith):
     from fastqsl_gb300 import api, synthetic as S
     from oracle import qassembly as QA
     spec = S.charges_random(21, (80, 72, 48), 6)
@@ -144,7 +145,7 @@ def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     zs = [0.0, 6.0, 13.5]
     stride = 1.5
     xs, ys, zz = api.plane_seed_grid(4.0, 4.0 + stride * (n1 - 1), n1, 4.0, 4.0 + stride * (n0 - 1), n0, zs)
-    prm = P.absolute_rkf45()
+    prm = P.absolute_rkf45(arith=arith)
     fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout=layout)
     plan = api.QMapPlan(n0, n1, len(zs))
     Q = plan.run(fs, xs, ys, zz, prm, s_len=0.25, stride=stride).cpu().numpy()
@@ -155,9 +156,10 @@ def test_qmap_pipeline_vs_fp64_oracle(cuda, oracle_port, layout):
     assert nan_same.mean() >= 0.99
     ok = ~np.isnan(Q) & ~np.isnan(Qref)
     d = np.abs(np.log10(Q[ok]) - np.log10(Qref[ok]))
-    # fp16 node values (h4b, h8c): the bar of the fp16 form is the median;
-    # its stated tail on this steep small field is within 5e-2
-    p99_bar = 5e-2 if layout in ("h4b", "h8c") else 1e-2
+    # every form with FP32 interpolation meets median <= 1e-3 and 99th
+    # percentile <= 1e-2; the opt-in fp16-x-weight sampler's tail on this
+    # steep small field is within 5e-2 (its stated bar)
+    p99_bar = 5e-2 if arith == P.ARITH_FAST_W16 else 1e-2
     assert np.median(d) <= 1e-3 and np.quantile(d, 0.99) <= p99_bar, (np.median(d), np.quantile(d, 0.99))
 
 

@@ -7,9 +7,9 @@
   cell) against the reference's host build, whose powf rounds differently
   in ~6e-4 of calls.
 * The fast FP32 kernels (SoA, interleaved float4, fp16 bricks) against the
-  oracle at the benchmark settings: flags identical for >= 99.8 % (>= 99 %
-  for fp16 storage), footpoints within 1e-3 cell for >= 99 % (2e-2 cell for
-  >= 90 % with fp16 storage).
+  oracle at the benchmark settings: flags identical for >= 99.8 %,
+  footpoints within 1e-3 cell for >= 99 % (2e-2 cell with fp16 storage; on
+  a field the fp16 stores hold exactly, 1e-3 cell as for float32).
 """
 import numpy as np
 import pytest
@@ -170,11 +170,52 @@ def test_native_layouts_match_oracle(cuda, oracle_port, layout, sched):
                     samples=samples)
     torch.cuda.synchronize()
     got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
-    if layout in ("h4b", "h8c"):  # fp16 node values
-        check_parity(got, ref, flag_frac=0.99, foot_frac=0.9, tol=2e-2)
+    if layout in ("h4b", "h8c"):
+        # fp16 node values (relative rounding up to 2^-12 of the brick's or
+        # cell's scale) move footpoints by more than the arithmetic does:
+        # within 2e-2 cell on >= 99 %; the arithmetic alone is held to the
+        # float32 bars in test_fp16_stores_arithmetic_parity
+        check_parity(got, ref, flag_frac=0.998, foot_frac=0.99, tol=2e-2)
     else:
         check_parity(got, ref, flag_frac=0.998, foot_frac=0.99)
     assert int(samples.item()) > 6 * len(xs)
+
+
+@pytest.mark.parametrize("layout,arith", [("f4", P.ARITH_FAST), ("h4b", P.ARITH_FAST), ("h8c", P.ARITH_FAST),
+                                          ("h4b", P.ARITH_FAST_W16)])
+def test_fp16_stores_arithmetic_parity(cuda, oracle_port, layout, arith):
+    """On a field the fp16 stores hold exactly (golden_util.fp16_exact_field)
+    the fp16 stores' FP32 interpolation traces like the float32 store: the
+    same bars as the interleaved float32 store (flags >= 99.8 %, footpoints
+    within 1e-3 cell on >= 99 %) against the FP32 oracle of the reference's
+    tracer on the same field.  The opt-in fp16-x-weight sampler quantises the
+    x fraction to ~2^-11 and is held to its own, looser bar (flags >= 99 %,
+    footpoints within 2e-2 cell on >= 98 %)."""
+    from fastqsl_gb300 import api, synthetic as S
+    B = G.fp16_exact_field(S.make_field(S.charges_random(3, (96, 96, 64), 8)))
+    xs, ys, zs, shp = S.plane_seeds((2, 93), (2, 93), 72, 72, 0.5)
+    ref = oracle_port.trace_all("port32", *B, xs, ys, zs, s_len=0.25, tol_coef=1.0,
+                                params=P.absolute_rkf45(arith=P.ARITH_EXACT))
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout=layout)
+    out = api.trace(fs, _dev(xs), _dev(ys), _dev(zs), P.absolute_rkf45(arith=arith), s_len=0.25, tol_coef=1.0,
+                    schedule="queue")
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+    if arith == P.ARITH_FAST_W16:
+        check_parity(got, ref, flag_frac=0.99, foot_frac=0.98, tol=2e-2)
+    else:
+        check_parity(got, ref, flag_frac=0.998, foot_frac=0.99)
+
+
+def test_w16_rejected_off_the_brick_store(cuda):
+    """fp16 x weights are a sampler of the brick store: other layouts refuse
+    them with a clear error."""
+    from fastqsl_gb300 import api, _lib, synthetic as S
+    B = S.make_field(S.bipole4_64(0))
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout="f4")
+    x = torch.full((4,), 10.0, device="cuda")
+    with pytest.raises(_lib.QslError, match="h4b"):
+        api.trace(fs, x, x, x, P.absolute_rkf45(arith=P.ARITH_FAST_W16))
 
 
 def test_edge_seeds(cuda, oracle_port):
@@ -254,13 +295,10 @@ def test_native_twist_vs_fp64_oracle(cuda, oracle_port, layout, packed):
     rl = np.abs(ll[same] - ref["LineLen"][same]) / np.maximum(ref["LineLen"][same], 1e-6)
     print(layout, packed, "twist rel err median %.2e p90 %.2e" % (med, p90), "len rel median %.2e p90 %.2e" % (
         np.median(rl), np.quantile(rl, 0.9)))
-    # fp16 bricks: the mixed-precision x-lerp samples on a 2^-11 grid of the
-    # x fraction; that noise in the RKF45 error estimate changes the step
-    # sequence, and the twist is a first-order sum over the steps (the
-    # reference's rule), so it moves by a fraction of its own discretisation
-    # error: the FP64 oracle's twist at tol 1e-4 differs from its twist at
-    # tol 1e-6 by 2.5e-2 (median) / 1.25e-1 (90th percentile) on this case
-    bar = (2e-2, 1.5e-1) if layout == "h4b" else (1e-4, 1e-3)
+    # fp16 bricks: the node values' rounding moves the step sequence a
+    # little, and the twist is a first-order sum over the steps (the
+    # reference's rule)
+    bar = (1e-3, 1e-2) if layout == "h4b" else (1e-4, 1e-3)
     assert med <= bar[0] and p90 <= bar[1], (med, p90)
 
 
@@ -285,3 +323,70 @@ def test_qmap_plan_twist_map(cuda):
     ref = api.trace(fs, xs, ys, zz, prm, s_len=0.25, schedule="static", curB=cs, occupancy=plan.occupancy_for(fs))
     assert plan.twist_map.shape == (2, n0, n1)
     assert torch.equal(plan.twist_map.reshape(-1), ref["twist"])
+
+
+def test_line_status(cuda):
+    """Each direction's qsl_line_status (the reference reports only flag 0 for
+    every limit and 42 for edges and non-finite positions alike):
+    * faces (flags 1-6) on an ordinary field, EDGE for a flag-42 exit at a
+      finite position (two coordinates crossing their faces in one step);
+    * MAX_STEPS (max_steps = 5) and MAX_LENGTH (a length limit of ~2 cells),
+      flag 0, footpoint where the line stopped;
+    * REJECT_LIMIT with a tolerance no step meets (1e-30) and max_rejects 5:
+      flag 0 and the seed itself as footpoint; with tol = 0 and no reject
+      limit the controller rejects until the step size underflows and the
+      position turns non-finite: NAN, flag 42;
+    * NAN for lines started in a cell with an infinite node value."""
+    from fastqsl_gb300 import api, synthetic as S
+    B = S.make_field(S.bipole4_64(0))
+    xs, ys, zs, _ = S.plane_seeds((4, 59), (4, 59), 24, 24, 0.5)
+    x, y, z = _dev(xs), _dev(ys), _dev(zs)
+    for layout, arith in (("soa", P.ARITH_EXACT), ("h4b", P.ARITH_FAST), ("f4", P.ARITH_FAST)):
+        fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout=layout)
+        base = P.absolute_rkf45(arith=arith)
+
+        def run(prm, sx=x, sy=y, sz=z):
+            o = api.trace(fs, sx, sy, sz, prm, s_len=0.25, status=True)
+            torch.cuda.synchronize()
+            return {k: v.cpu().numpy() for k, v in o.items() if v is not None}
+
+        o = run(base)
+        for f, st in (("flag_start", "status_start"), ("flag_end", "status_end")):
+            face = (o[f] >= 1) & (o[f] <= 6)
+            assert face.mean() > 0.9
+            assert (o[st][face] == P.LINE_FACE).all()
+            assert (o[st][o[f] == 42] == P.LINE_EDGE).all()
+        for prm, want in ((base.copy(max_steps=5), P.LINE_MAX_STEPS), (base.copy(len_ratio=0.01),
+                                                                        P.LINE_MAX_LENGTH)):
+            o = run(prm)
+            st = np.concatenate([o["status_start"], o["status_end"]])
+            fl = np.concatenate([o["flag_start"], o["flag_end"]])
+            assert ((st == want) == (fl == 0)).all()
+            assert (st == want).mean() > 0.4
+            assert np.isfinite(o["end_x"]).all() and np.isfinite(o["start_x"]).all()
+        o = run(base.copy(tol=1e-30, max_rejects=5))
+        for f, st, k in (("flag_start", "status_start", "start_x"), ("flag_end", "status_end", "end_x")):
+            assert (o[st] == P.LINE_REJECT_LIMIT).all() and (o[f] == 0).all()
+            np.testing.assert_array_equal(o[k], xs)
+        o = run(base.copy(tol=0.0, max_rejects=0))
+        assert (o["status_end"] == P.LINE_NAN).all() and (o["flag_end"] == 42).all()
+        fs.close()
+    # edge exit: B along (1, 1, 0), seeds on the diagonal near the x-max / y-max edge
+    one = np.ones((32, 32, 32), np.float32)
+    fs = api.FieldStore(torch.from_numpy(one), torch.from_numpy(one), torch.from_numpy(0 * one), layout="f4")
+    e = torch.tensor([29.5, 30.25], device="cuda")
+    o = api.trace(fs, e, e, torch.full_like(e, 7.0), P.absolute_rkf45(), s_len=0.25, status=True)
+    torch.cuda.synchronize()
+    assert (o["flag_end"].cpu() == 42).all() and (o["status_end"].cpu() == P.LINE_EDGE).all()
+    assert torch.isfinite(o["end_x"]).all()
+    fs.close()
+    # poisoned field: an infinite node in the seeds' cell
+    Bp = [b.copy() for b in B]
+    Bp[0][20, 20, 0] = np.inf
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in Bp], layout="f4")
+    p = torch.tensor([20.25, 19.5], device="cuda")
+    o = api.trace(fs, p, torch.tensor([20.5, 19.75], device="cuda"), torch.tensor([0.5, 0.25], device="cuda"),
+                  P.absolute_rkf45(), s_len=0.25, status=True)
+    torch.cuda.synchronize()
+    assert (o["status_end"].cpu() == P.LINE_NAN).all() and (o["flag_end"].cpu() == 42).all()
+    fs.close()

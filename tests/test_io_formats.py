@@ -8,7 +8,9 @@ import pytest
 
 from fastqsl_gb300 import io
 
-REF = os.environ.get("QSL_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $QSL_REFERENCE_ROOT, else `reference` beside the repository
+REF = os.environ.get("QSL_REFERENCE_ROOT", os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference"))
 
 
 def test_fits_roundtrip(tmp_path):

@@ -53,13 +53,13 @@ def test_reference_presets_match_python(lib):
 
 def test_params_struct_layout():
     from fastqsl_gb300 import params as P, _lib
-    # int32, int32, 5 doubles, int64, int32, int32
-    assert ctypes.sizeof(P.TraceParams) == 4 + 4 + 5 * 8 + 8 + 4 + 4
-    assert ctypes.sizeof(_lib.TraceIO) == 23 * 8
+    # int32, int32, 5 doubles, int64, int32, int32, int32, (pad to 8)
+    assert ctypes.sizeof(P.TraceParams) == 4 + 4 + 5 * 8 + 8 + 4 + 4 + 4 + 4
+    assert ctypes.sizeof(_lib.TraceIO) == 25 * 8
     assert ctypes.sizeof(_lib.ScottIO) == 18 * 8
     assert ctypes.sizeof(_lib.Sched) == 4 + 4 + 3 * 8 + 8
     # field, params, io, n, s_len, tol_coef, cross[3], (pad), curB[3], order, n_dev
-    assert ctypes.sizeof(_lib.BatchJob) == 8 + 64 + 184 + 8 + 4 + 4 + 12 + 4 + 24 + 8 + 8
+    assert ctypes.sizeof(_lib.BatchJob) == 8 + 72 + 200 + 8 + 4 + 4 + 12 + 4 + 24 + 8 + 8
 
 
 def test_version_and_errors_without_gpu(lib):

@@ -2,9 +2,10 @@
 by running the reference code; see tests/golden/make_golden.py).
 
 The FP32 restatement must reproduce the reference bit for bit, except in
-the two places where the reference reads uninitialised memory (footpoints of
+the places where the reference reads uninitialised memory (footpoints of
 directions stopped by a limit; the RK4 exit-segment twist term when the exit
-step is shorter than 1e-3)."""
+step is shorter than 1e-3; the Scott routine's outputs of lines it leaves
+unset)."""
 import numpy as np
 import pytest
 
@@ -61,6 +62,29 @@ def test_port32_matches_reference_probes(oracle_port):
     sc = [pr.rkf45_scott(v, h) for v, h in zip(v9, hs)]
     np.testing.assert_array_equal(np.stack([s[0] for s in sc]), g["rkf45_scott"])
     np.testing.assert_array_equal(np.array([s[1] for s in sc], np.float32), g["rkf45_scott_err"])
+
+
+@pytest.mark.parametrize("name", sorted(G.SCOTT_CASES))
+def test_port32_matches_reference_scott_lines(oracle_port, name):
+    """Whole Scott lines (TraceBlineScott.cu:334-519, the reference built with
+    its tolerance initialised): exit faces of every seed the reference
+    defines, footpoints, q_0, q_perp, B at the seed and (twist on) the twist
+    integral, bit for bit."""
+    g, meta = G.load(name)
+    Bx, By, Bz = G.field_for(meta)
+    cur = G.twist_current(Bx, By, Bz) if meta["twist"] else None
+    out = oracle_port.scott_all("port32", Bx, By, Bz, g["inp_x"], g["inp_y"], g["inp_z"], s_len=meta["s_len"],
+                                tol_coef=meta["tol_coef"], params=P.reference_scott(), curB=cur)
+    live = G.scott_live(g)
+    assert live.mean() > 0.85
+    defined = g["inp_z"] >= 0
+    for k in ["flag_start", "flag_end"]:
+        np.testing.assert_array_equal(out[k][defined], g[k][defined], err_msg=k)
+    for k in ["B_this_x", "B_this_y", "B_this_z"]:
+        np.testing.assert_array_equal(out[k][defined], g[k][defined], err_msg=k)
+    for k in ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "q_0", "q_perp"] + (
+            ["twist"] if meta["twist"] else []):
+        np.testing.assert_array_equal(out[k][live], g[k][live], err_msg=k)
 
 
 def test_qassembly_matches_reference(oracle_port):

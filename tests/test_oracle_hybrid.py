@@ -15,7 +15,9 @@ import pytest
 
 from oracle import qassembly as QA
 
-REF = os.environ.get("QSL_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: $QSL_REFERENCE_ROOT, else `reference` beside the repository
+REF = os.environ.get("QSL_REFERENCE_ROOT", os.path.join(
+    os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "reference"))
 NB = os.path.join(REF, "demo", "Q_RKF45MixCuPyDiffScott.ipynb")
 
 

@@ -40,14 +40,22 @@ def cell_below(c, a):
     return lo
 
 
+def stretch_bin_widening(nb):
+    """How far (in bins) each search-table bin is widened on both sides: 1 %
+    plus the float rounding of the kernel's bin index (c - a0) * binv, about
+    2.4e-7 * nb bins, with margin."""
+    return 0.01 + 4e-7 * nb
+
+
 def build_tables(a):
     n = len(a)
     nb = BINS_PER_CELL * (n - 1)
     rec = [reference_bisect(a[j + 1], a) for j in range(n - 1)]
     a0, w = float(a[0]), (float(a[-1]) - float(a[0])) / nb
+    wid = stretch_bin_widening(nb)
     bins = []
     for b in range(nb):
-        lo, hi = cell_below(a0 + (b - 0.01) * w, a), cell_below(a0 + (b + 1.01) * w, a)
+        lo, hi = cell_below(a0 + (b - wid) * w, a), cell_below(a0 + (b + 1 + wid) * w, a)
         bins.append((lo, max(lo, hi)))
     binv = f32(f32(nb) / f32(a[-1] - a[0]))
     return rec, bins, binv
@@ -102,7 +110,8 @@ def test_four_node_axis_takes_the_cell_above():
     assert table_lookup(f32(0.5), a, rec, bins, binv) == 1
 
 
-@pytest.mark.parametrize("bad", [[0.0, 1.0, 1.0], [0.0, 2.0, 1.0], [0.0]])
+@pytest.mark.parametrize("bad", [[0.0, 1.0, 1.0], [0.0, 2.0, 1.0], [0.0],
+                                 np.array([0.0, 1.0, 1.0 + 1e-9])])  # distinct doubles, one float
 def test_trace_stretch_rejects_bad_host_coordinates(bad):
     """The native entry needs strictly increasing node coordinates (the
     search and its tables assume them); host arrays are checked before any
@@ -112,4 +121,65 @@ def test_trace_stretch_rejects_bad_host_coordinates(bad):
     b = torch.zeros(3, 3, 3)
     x = torch.zeros(4)
     with pytest.raises(ValueError):
-        api.trace_stretch(b, b, b, [np.array(bad, f32), np.arange(3.0), np.arange(3.0)], x, x, x)
+        api.trace_stretch(b, b, b, [np.asarray(bad), np.arange(3.0), np.arange(3.0)], x, x, x)
+
+
+def _bisect_vec(c, a):
+    """reference_bisect over an array of coordinates."""
+    n = len(a)
+    i0, i1 = np.zeros(c.shape, np.int64), np.full(c.shape, n - 1)
+    mid = np.full(c.shape, n // 2)
+    while True:
+        act = (i1 - i0) > 3
+        if not act.any():
+            break
+        gt = c > a[mid]
+        i0, i1 = np.where(act & gt, mid, i0), np.where(act & ~gt, mid, i1)
+        mid = np.where(act, (i0 + i1) // 2, mid)
+    r = np.minimum(np.where(c > a[mid], mid, mid - 1), n - 2)
+    return np.maximum(r, 0)
+
+
+def _tables_vec(a, wid):
+    n = len(a)
+    nb = BINS_PER_CELL * (n - 1)
+    rec = _bisect_vec(a[1:], a)
+    a0, w = float(a[0]), (float(a[-1]) - float(a[0])) / nb
+    b = np.arange(nb)
+    below = lambda x: np.clip(np.searchsorted(a.astype(np.float64), x, side="left") - 1, 0, n - 2)  # noqa: E731
+    lo, hi = below(a0 + (b - wid) * w), below(a0 + (b + 1 + wid) * w)
+    return rec, lo, np.maximum(lo, hi), f32(f32(nb) / f32(a[-1] - a[0]))
+
+
+def _lookup_vec(c, a, rec, lo, hi, binv):
+    b = np.clip(np.trunc((f32(c - a[0]) * binv).astype(f32)).astype(np.int64), 0, len(lo) - 1)
+    lo, hi = lo[b].copy(), hi[b].copy()
+    while True:
+        act = lo < hi
+        if not act.any():
+            break
+        mid = (lo + hi + 1) >> 1
+        gt = c > a[np.minimum(mid, len(a) - 1)]
+        lo, hi = np.where(act & gt, mid, lo), np.where(act & ~gt, mid - 1, hi)
+    return rec[lo]
+
+
+def test_tables_on_a_long_axis():
+    """An irregular axis of ~120,000 nodes (480,000 bins) away from the
+    origin, probed at and beside every bin edge and node: there the float
+    rounding of the kernel's bin index ((c - a0) * binv) reaches several
+    hundredths of a bin, so a fixed 1 % widening of the bins misses the
+    reference search's cell for some coordinates (checked below); the
+    widening that grows with the bin count gives it for every one."""
+    rng = np.random.default_rng(10)
+    a = np.unique(np.cumsum(rng.uniform(0.3, 1.7, 120000)).astype(f32) + f32(rng.uniform(-1e4, 1e4)))
+    nb = BINS_PER_CELL * (len(a) - 1)
+    e = (float(a[0]) + (float(a[-1]) - float(a[0])) * np.arange(1, nb) / nb).astype(f32)
+    c = np.concatenate([e, np.nextafter(e, f32(np.inf)), np.nextafter(e, f32(-np.inf)), a[1:-1],
+                        np.nextafter(a[1:-1], f32(np.inf))])
+    c = np.clip(c, np.nextafter(a[0], f32(np.inf)), np.nextafter(a[-1], f32(-np.inf)))  # the kernel's clamp
+    ref = _bisect_vec(c, a)
+    got = _lookup_vec(c, a, *_tables_vec(a, stretch_bin_widening(nb)))
+    assert (got == ref).all(), int((got != ref).sum())
+    fixed = _lookup_vec(c, a, *_tables_vec(a, 0.01))
+    assert (fixed != ref).any()  # the case does exercise the rounding

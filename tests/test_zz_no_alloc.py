@@ -90,6 +90,25 @@ def test_noalloc_matches_workspace_entry_twice(lib):
             np.testing.assert_array_equal(a, b)
 
 
+def test_noalloc_allocates_nothing(lib):
+    """After a warm-up call (which looks up the scratch array's address), a
+    further call leaves the device's free memory exactly as it was."""
+    ins, n = _inputs(64, 80, 3, 9)
+    _call_noalloc(lib, ins, n, 64, 80, 1, 0.5)
+    from fastqsl_gb300.api import ptr, stream_handle
+    f, b, pix, cnt = _outputs(n)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    rc = lib.qsl_cook_pseudo_line_noalloc(*[ptr(t) for t in ins], n, 64, 80, 1, 0.5,
+                                          *[ptr(t) for t in f], *[ptr(t) for t in b], ptr(pix), ptr(cnt),
+                                          stream_handle())
+    assert rc == 0, lib.qsl_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert int(cnt[0].item()) > 0
+
+
 def test_noalloc_rejects_oversize(lib):
     from fastqsl_gb300.api import stream_handle
     big = int(lib.qsl_cook_noalloc_max_pixels()) + 1
