@@ -182,7 +182,8 @@ def run_ours(args, rank, world):
     plan = api.QMapPlan(n0, n1, npl, device=dev)
     from fastqsl_gb300 import autotune
     if args.no_autotune:
-        tuned = {"tile": (8, 8), "occupancy": plan.occupancy_for(store), "table": {}}
+        tuned = {"tile": (8, 8), "occupancy": plan.occupancy_for(store), "schedule": plan.schedule, "chunk": 0,
+                 "table": {}}
     else:
         tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=8)
     stream = torch.cuda.current_stream()
@@ -224,6 +225,7 @@ def run_ours(args, rank, world):
     res = {"ms": ms, "qpix": qpix, "k_ms": k_ms, "samples_main": samples_main, "samples_all": samples_all,
            "sm_count": sm_count(), "l1_probe": l1_probe(dev),
            "clocks": clk.summary(), "autotune": {"tile": list(tuned["tile"]), "occupancy": tuned["occupancy"],
+                                                 "schedule": tuned["schedule"], "chunk": tuned["chunk"],
                                                  "sample_ms": tuned["table"]}}
     if rank != 0:
         return res, None
@@ -444,6 +446,8 @@ def batched_graph(device, n_fields=64, seed=11, reps=3, acc_fields=8, acc_pixels
                            integrator="rkf45" if rkf else "rk4")
         del B
     qb = api.QBatch(specs, device=device)
+    from fastqsl_gb300 import autotune
+    tuned = autotune.tune_batch(qb)
     qb.capture()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -456,7 +460,7 @@ def batched_graph(device, n_fields=64, seed=11, reps=3, acc_fields=8, acc_pixels
     qpix = sum((sp["n0"] - 2) * (sp["n1"] - 2) for sp in specs)
     lines = sum(sp["n0"] * sp["n1"] for sp in specs)
     out = {"fields": n_fields, "seeds": int(lines), "q_pixels": int(qpix), "graph_ms": ms,
-           "qpixels_per_s": qpix / (ms / 1e3)}
+           "qpixels_per_s": qpix / (ms / 1e3), "autotune": tuned}
     Qs = {k: qb.jobs[k]["Q"][0].cpu().numpy() for k in keep}
     for fs in stores:
         fs.close()
@@ -828,9 +832,10 @@ def main():
     # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
     line["gpu_launches"] = 8 * args.steps
     line["config"]["autotune"] = res["autotune"]
-    line["config"]["schedule"] = (f"static lockstep, {res['autotune']['tile'][0]}x{res['autotune']['tile'][1]} "
-                                  f"seed tiles in column order, occupancy {res['autotune']['occupancy']} "
-                                  f"({'default' if args.no_autotune else 'autotuned'})")
+    at = res["autotune"]
+    sched = "static lockstep" if at["schedule"] == "static" else f"work queue, {at['chunk']} lines per refill"
+    line["config"]["schedule"] = (f"{sched}, {at['tile'][0]}x{at['tile'][1]} seed tiles in column order, "
+                                  f"occupancy {at['occupancy']} ({'default' if args.no_autotune else 'autotuned'})")
     if acc:
         line["accuracy_vs_fp64_all_forms"] = acc
     if "plain_trace_ms" in res:

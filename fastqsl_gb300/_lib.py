@@ -79,7 +79,7 @@ _SIGS = {
     "qsl_params_reference_scott": (None, [_P]),
     "qsl_batch_pack": (c_int, [_P, c_int, _P, c_i64, _P]),
     "qsl_batch_run": (c_int, [_P, _P, _P, _P]),
-    "qsl_batch_run_window": (c_int, [_P, _P, _P, c_i64, c_i64, c_int, _P]),
+    "qsl_batch_run_window": (c_int, [_P, _P, _P, c_i64, c_i64, c_int, c_int, _P]),
     "qsl_batch_create": (c_int, [_P, c_int, _P, _P]),
     "qsl_batch_launch": (c_int, [_P, _P, _P]),
     "qsl_batch_lines": (c_i64, [_P]),

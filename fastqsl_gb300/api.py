@@ -257,23 +257,25 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     results equal the drop-in's bit for bit.  Defaults to the reference
     stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""
     from .params import reference_stretch
+    # the native entry takes the coordinates on the host (the per-axis
+    # constants of the cell location are formed there); device arrays are
+    # copied back first
+    ax = []
     for c in coords:
-        # coordinates given on the host are checked here (on the device they
-        # are taken as they are: a check would synchronise)
-        if not (isinstance(c, torch.Tensor) and c.is_cuda):
-            # on the float32 values the device uses: two distinct doubles
-            # can round to one float
-            a = np.asarray(c.cpu() if isinstance(c, torch.Tensor) else c, dtype=np.float64).astype(np.float32)
-            if a.ndim != 1 or a.size < 2 or not np.all(np.diff(a) > 0):
-                raise ValueError("each coordinate array must be 1-D, with at least 2 strictly increasing entries "
-                                 "(as float32)")
+        a = c.detach().cpu().numpy() if isinstance(c, torch.Tensor) else np.asarray(c)
+        # checked on the float32 values the kernels use: two distinct doubles
+        # can round to one float
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).astype(np.float32))
+        if a.ndim != 1 or a.size < 2 or not np.all(np.diff(a) > 0):
+            raise ValueError("each coordinate array must be 1-D, with at least 2 strictly increasing entries "
+                             "(as float32)")
+        ax.append(a)
     lib = _lib.load()
     if params is None:
         params = reference_stretch()
     arrs = [as_xfast(b) for b in (Bx, By, Bz)]
     nx, ny, nz = (int(v) for v in arrs[0].shape)
-    ax = [torch.as_tensor(c).to(device=xs.device, dtype=torch.float32).contiguous() for c in coords]
-    if [a.numel() for a in ax] != [nx, ny, nz]:
+    if [a.size for a in ax] != [nx, ny, nz]:
         raise ValueError("coordinate arrays must have nx, ny, nz entries")
     n = int(xs.shape[0])
     if out is None:
@@ -285,7 +287,8 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
         out["twist"] = torch.zeros(n, dtype=torch.float64, device=xs.device)
     io = _io(xs, ys, zs, out)
     sc = _lib.Sched(SCHEDULES[schedule], 0, ptr(order), None, ptr(samples), int(occupancy))
-    _lib.check(lib.qsl_trace_stretch(*[ptr(a) for a in arrs], nx, ny, nz, *[ptr(a) for a in ax], int(bool(uni)),
+    _lib.check(lib.qsl_trace_stretch(*[ptr(a) for a in arrs], nx, ny, nz,
+                                     *[a.ctypes.data_as(ctypes.c_void_p) for a in ax], int(bool(uni)),
                                      ctypes.byref(params), ctypes.byref(io), n, float(s_len), float(tol_coef), cd,
                                      *cur, ctypes.byref(sc), stream_handle(stream)), "qsl_trace_stretch")
     return out
@@ -370,9 +373,10 @@ class QMapPlan:
     demo/Q_RKF45CuPy.ipynb cells 7-11."""
 
     # measured best per field layout on GB300 (trace of the 512x512x256 cube):
-    # register budget for 8 resident blocks/SM for the brick and float4
-    # stores, the compiler's choice for SoA
-    DEFAULT_OCCUPANCY = {"h8c": 8, "h4b": 8, "f4": 8, "soa": 0}
+    # register budget for 7 resident blocks/SM for the brick store (FP32
+    # interpolation), 8 for the cell-record and float4 stores, the compiler's
+    # choice for SoA
+    DEFAULT_OCCUPANCY = {"h8c": 8, "h4b": 7, "f4": 8, "soa": 0}
 
     def __init__(self, n0, n1, nplanes=1, device="cuda", pseudo=True, tile=(8, 8), chunk=256, schedule="static",
                  occupancy=None, hybrid=False):
@@ -574,12 +578,14 @@ class BatchPlan:
         self.info = info
         self.lines = int(info.lines)
 
-    def launch(self, samples=None, stream=None, max_blocks=0, lo=0, hi=-1):
+    def launch(self, samples=None, stream=None, max_blocks=0, lo=0, hi=-1, occupancy=0):
         """Lines [lo, hi) of the batch (hi < 0: all); max_blocks > 0: at most
         that many resident blocks (they loop over the lines), leaving the rest
-        of the GPU's block slots free."""
+        of the GPU's block slots free; occupancy: the kernels' register budget
+        in resident blocks per SM (6-10, 0 = 8)."""
         _lib.check(_lib.load().qsl_batch_run_window(self._dev.data_ptr(), ctypes.byref(self.info), ptr(samples),
-                                                    int(lo), int(hi), int(max_blocks), stream_handle(stream)),
+                                                    int(lo), int(hi), int(max_blocks), int(occupancy),
+                                                    stream_handle(stream)),
                    "qsl_batch_run")
 
     @property
@@ -640,6 +646,9 @@ class QBatch:
         self.main_batch = BatchPlan(main_jobs, stream=stream)
         self.sub_batch = BatchPlan(sub_jobs, stream=stream)
         self.graph = None
+        # register budget of the batched kernels (resident blocks per SM;
+        # autotune.tune_batch measures the choices; 0 = 8)
+        self.occupancy = 0
 
     @property
     def main_lines(self):
@@ -651,7 +660,7 @@ class QBatch:
 
     def run_main(self, stream=None, lo=0, hi=-1):
         """The batched main trace, or the window [lo, hi) of its lines."""
-        self.main_batch.launch(stream=stream, max_blocks=self.max_blocks, lo=lo, hi=hi)
+        self.main_batch.launch(stream=stream, max_blocks=self.max_blocks, lo=lo, hi=hi, occupancy=self.occupancy)
 
     def run_post(self, stream=None):
         """Everything after the main trace: Q, pseudo-lines, merge."""
@@ -672,7 +681,7 @@ class QBatch:
                                                 float(sp.get("stride", 1.0)), ptr(J["cut"][0]), ptr(J["cut"][1]),
                                                 ptr(J["cut"][2]), ptr(J["bz0s"]), ptr(J["bz0e"]), ptr(J["pix"]),
                                                 ptr(J["count"]), ptr(J["work"]), J["work_bytes"], st), "cook")
-        self.sub_batch.launch(stream=stream, max_blocks=self.max_blocks)
+        self.sub_batch.launch(stream=stream, max_blocks=self.max_blocks, occupancy=self.occupancy)
         for J in self.jobs:
             sp, s = J["sp"], J["sub"]
             jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0

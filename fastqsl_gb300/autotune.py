@@ -8,9 +8,18 @@ spread evenly over the stack) for each candidate
   warp a 8x4 patch; 16x16 a 16x2 strip; 4x8 a 4x8 patch),
 * resident-block budget — registers per thread sized for 0 (compiler's
   choice), 6, 7, 8, 9 or 10 blocks of 128 threads per SM,
+* schedule — static lockstep (one line per thread) against the device work
+  queue with 32, 128 or 512 lines per warp refill (lanes refill the moment
+  their line ends), on the best tile and budget,
 
 and keeps the fastest.  Results are cached per (device, store layout, field
-shape, integrator, plane shape).
+shape, integrator, plane shape).  tune_batch does the same for the batched
+kernels of a QBatch (resident-block budget 6-10, timed on windows of lines
+spread over the batch).
+
+The brick edge is not a tuning dimension: an x-pair brick row of 8 records
+is one 128-byte line, the unit the L1 charges per warp request, and the
+record index is formed with shifts by 3.
 """
 from __future__ import annotations
 
@@ -20,6 +29,8 @@ from . import api
 
 TILES = ((8, 8), (4, 8), (16, 16))
 OCCUPANCIES = (0, 6, 7, 8, 9, 10)
+QUEUE_CHUNKS = (32, 128, 512)
+BATCH_OCCUPANCIES = (6, 7, 8, 9, 10)
 
 _cache: dict = {}
 
@@ -30,11 +41,12 @@ def _key(field, params, n0, n1):
 
 
 def tune_trace(field, xs, ys, zs, params, n0, n1, nplanes, s_len=0.25, tol_coef=1.0, cross_dir=(0.0, 0.0, 1.0),
-               sample_planes=4, reps=2, tiles=TILES, occupancies=OCCUPANCIES, use_cache=True):
-    """Returns {'tile': (ty, tx), 'occupancy': k, 'ms': t, 'table': {...}}
-    for the fastest candidate on `sample_planes` planes evenly spaced over
-    the stack (lines from the bottom and the middle of a cube differ in
-    length and spread)."""
+               sample_planes=4, reps=2, tiles=TILES, occupancies=OCCUPANCIES, chunks=QUEUE_CHUNKS, use_cache=True):
+    """Returns {'tile': (ty, tx), 'occupancy': k, 'schedule': 'static' or
+    'queue', 'chunk': lines per refill, 'ms': t, 'table': {...}} for the
+    fastest candidate on `sample_planes` planes evenly spaced over the stack
+    (lines from the bottom and the middle of a cube differ in length and
+    spread)."""
     key = _key(field, params, n0, n1)
     if use_cache and key in _cache:
         return _cache[key]
@@ -46,23 +58,33 @@ def tune_trace(field, xs, ys, zs, params, n0, n1, nplanes, s_len=0.25, tol_coef=
     npl, n = len(picks), len(picks) * per
     sx, sy, sz = xs[idx].contiguous(), ys[idx].contiguous(), zs[idx].contiguous()
     out = api.alloc_trace_outputs(n, xs.device)
+    queue = torch.zeros(1, dtype=torch.int64, device=xs.device)
+
+    def timed(**kw):
+        api.trace(field, sx, sy, sz, **kw)  # warm-up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            api.trace(field, sx, sy, sz, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    base = dict(params=params, s_len=s_len, tol_coef=tol_coef, cross_dir=cross_dir, out=out)
     table = {}
+    orders = {}
     for tile in tiles:
-        order = api.tile_order(npl, n0, n1, tile[0], tile[1], xs.device)
+        orders[tile] = api.tile_order(npl, n0, n1, tile[0], tile[1], xs.device)
         for occ in occupancies:
-            kw = dict(params=params, s_len=s_len, tol_coef=tol_coef, cross_dir=cross_dir, schedule="static",
-                      out=out, order=order, occupancy=occ)
-            api.trace(field, sx, sy, sz, **kw)  # warm-up
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(reps):
-                api.trace(field, sx, sy, sz, **kw)
-            e1.record()
-            torch.cuda.synchronize()
-            table[(tile, occ)] = e0.elapsed_time(e1) / reps
-    (tile, occ), ms = min(table.items(), key=lambda kv: kv[1])
-    res = {"tile": tile, "occupancy": occ, "ms": ms, "table": {f"{t[0]}x{t[1]}/occ{o}": v for (t, o), v in
-                                                               table.items()}}
+            table[(tile, occ, "static", 0)] = timed(**base, schedule="static", order=orders[tile], occupancy=occ)
+    (tile, occ, _, _), _ = min(table.items(), key=lambda kv: kv[1])
+    for chunk in chunks:
+        table[(tile, occ, "queue", chunk)] = timed(**base, schedule="queue", order=orders[tile], occupancy=occ,
+                                                  chunk=chunk, queue=queue)
+    (tile, occ, sched, chunk), ms = min(table.items(), key=lambda kv: kv[1])
+    res = {"tile": tile, "occupancy": occ, "schedule": sched, "chunk": chunk, "ms": ms,
+           "table": {f"{t[0]}x{t[1]}/occ{o}" + (f"/queue{c}" if sc == "queue" else ""): v
+                     for (t, o, sc, c), v in table.items()}}
     _cache[key] = res
     return res
 
@@ -74,4 +96,39 @@ def tune_plan(plan, field, xs, ys, zs, params, s_len=0.25, tol_coef=1.0, cross_d
     ty, tx = res["tile"]
     plan.order = api.tile_order(plan.nplanes, plan.n0, plan.n1, ty, tx, xs.device)
     plan.occupancy = res["occupancy"]
+    plan.schedule = res["schedule"]
+    if res["schedule"] == "queue":
+        plan.chunk = res["chunk"]
     return res
+
+
+def tune_batch(qb, occupancies=BATCH_OCCUPANCIES, windows=8, window_lines=1 << 15, reps=2):
+    """Times the batched main trace of QBatch `qb` at each resident-block
+    budget on `windows` windows of lines spread evenly over its line space
+    (each window holds whole warps of a few jobs), sets the fastest as
+    qb.occupancy (before capture()) and returns {'occupancy': k, 'ms': t,
+    'table': {...}}."""
+    lines = int(qb.main_lines)
+    if lines <= 0:
+        return {"occupancy": qb.occupancy, "ms": 0.0, "table": {}}
+    w = max(32, min(window_lines, lines // windows) // 32 * 32)
+    starts = sorted({(k * lines // windows) // 32 * 32 for k in range(windows)})
+
+    def run(occ):
+        for lo in starts:
+            qb.main_batch.launch(max_blocks=qb.max_blocks, lo=lo, hi=min(lines, lo + w), occupancy=occ)
+
+    table = {}
+    for occ in occupancies:
+        run(occ)  # warm-up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            run(occ)
+        e1.record()
+        torch.cuda.synchronize()
+        table[occ] = e0.elapsed_time(e1) / reps
+    occ, ms = min(table.items(), key=lambda kv: kv[1])
+    qb.occupancy = occ
+    return {"occupancy": occ, "ms": ms, "table": {f"occ{o}": v for o, v in table.items()},
+            "sample": f"{len(starts)} windows of {w} lines"}

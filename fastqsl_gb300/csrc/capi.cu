@@ -236,6 +236,38 @@ static FieldH4B h4b_of(const qsl_field* f) {
 static FieldH4BW h4bw_of(const qsl_field* f) { return FieldH4BW{h4b_of(f)}; }
 static FieldH8C h8c_of(const qsl_field* f) { return FieldH8C{f->cells, f->d, f->nbx, f->nby}; }
 
+// The per-launch constants of a packed stretched store, formed on the host
+// from the host coordinates in the arithmetic store_prepare uses on the
+// device for the drop-in (so both give the same bits): first and last node
+// coordinates, the clamp bounds 1e-6 inside them (double, narrowed), the
+// uniform-formula spacing (hi - lo) / n and the search-table bins per unit
+// coordinate.
+template <int M>
+static void stretch_constants_host(FieldStretchT<M>& f, const float* ax, const float* ay, const float* az) {
+    const int n[3] = {f.d.nx, f.d.ny, f.d.nz};
+    const float* a[3] = {ax, ay, az};
+    float lo[3], hi[3], clo[3], chi[3], us[3], binv[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = a[k][0];
+        hi[k] = a[k][n[k] - 1];
+        clo[k] = (float)((double)lo[k] + 1e-6);
+        chi[k] = (float)((double)hi[k] - 1e-6);
+        us[k] = (hi[k] - lo[k]) / (float)n[k];
+        binv[k] = (float)(STRETCH_BINS_PER_CELL * (n[k] - 1)) / (hi[k] - lo[k]);
+    }
+    f.lo = make_float3(lo[0], lo[1], lo[2]);
+    f.hi = make_float3(hi[0], hi[1], hi[2]);
+    f.clo = make_float3(clo[0], clo[1], clo[2]);
+    f.chi = make_float3(chi[0], chi[1], chi[2]);
+    f.us = make_float3(us[0], us[1], us[2]);
+    f.sbinv = make_float3(binv[0], binv[1], binv[2]);
+}
+// the summed coordinate extents, as len_scale forms them on the device
+template <int M>
+static double stretch_len_scale_host(const FieldStretchT<M>& f) {
+    return (double)(((f.hi.x + f.hi.y) + f.hi.z) - ((f.lo.x + f.lo.y) + f.lo.z));
+}
+
 // ---------------------------------------------------------------------------
 // Tracing
 // ---------------------------------------------------------------------------
@@ -479,14 +511,14 @@ int qsl_trace_all_bline(int integrator, int arith, const float* Bx, const float*
 }
 
 // Stretched grid, native form: field arrays (x fastest) of shape nx x ny x nz
-// on the increasing node coordinates x_arr, y_arr, z_arr (device), host
+// on the increasing node coordinates x_arr_h, y_arr_h, z_arr_h (host), host
 // scalars and settings.
 int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx, int ny, int nz,
-                      const float* x_arr, const float* y_arr, const float* z_arr, int uni,
+                      const float* x_arr_h, const float* y_arr_h, const float* z_arr_h, int uni,
                       const qsl_trace_params* prm, const qsl_trace_io* io, int64_t n, float s_len, float tol_coef,
                       const float* cross_dir_h, const float* curBx, const float* curBy, const float* curBz,
                       const qsl_sched* sched_h, qsl_stream_t stream) {
-    if (!Bx || !By || !Bz || !x_arr || !y_arr || !z_arr) return fail(QSL_ERR_INVALID, "null field or coordinates");
+    if (!Bx || !By || !Bz || !x_arr_h || !y_arr_h || !z_arr_h) return fail(QSL_ERR_INVALID, "null field or coordinates");
     if (!dims_ok(nx, ny, nz)) return fail(QSL_ERR_INVALID, "bad field shape %d x %d x %d", nx, ny, nz);
     if (!params_ok(prm)) return fail(QSL_ERR_INVALID, "bad trace params");
     if (prm->arith == QSL_ARITH_FAST_W16)
@@ -494,6 +526,11 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (n < 0) return fail(QSL_ERR_INVALID, "negative seed count");
     if (n == 0) return QSL_OK;
     if (!io_ok(io)) return fail(QSL_ERR_INVALID, "null pointer in trace io");
+    const float* ah[3] = {x_arr_h, y_arr_h, z_arr_h};
+    const int na[3] = {nx, ny, nz};
+    for (int k = 0; k < 3; ++k)
+        for (int i = 0; i + 1 < na[k]; ++i)
+            if (!(ah[k][i] < ah[k][i + 1])) return fail(QSL_ERR_INVALID, "coordinates of axis %d not increasing", k);
     qsl_sched sc{QSL_SCHED_STATIC, 0, nullptr, nullptr, nullptr, 0};
     if (sched_h) sc = *sched_h;
     if (sc.schedule != QSL_SCHED_QUEUE && sc.schedule != QSL_SCHED_STATIC)
@@ -504,6 +541,28 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     const bool twist = curBx != nullptr;
     if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
     cudaStream_t st = (cudaStream_t)stream;
+    const int64_t cells = (int64_t)(nx - 1) + (ny - 1) + (nz - 1);
+    const bool packed_path = prm->arith == QSL_ARITH_FAST && cells * (1 + STRETCH_BINS_PER_CELL) < (1LL << 31);
+    // one stream-ordered buffer for the launch: the coordinates, then (fast
+    // arithmetic) the float4 node copy and the search tables
+    const int64_t nodes = (int64_t)nx * ny * nz;
+    const int64_t tcells = (packed_path && !uni) ? cells : 0;
+    const int64_t ncoord = (int64_t)nx + ny + nz;
+    const size_t coord_bytes = ((size_t)ncoord * sizeof(float) + 255) / 256 * 256;
+    const size_t bytes = coord_bytes + (packed_path ? (size_t)(nodes + tcells) * sizeof(float4) +
+                                                          (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int2)
+                                                    : 0);
+    char* buf = nullptr;
+    QSL_CHECK_CUDA(cudaMallocAsync((void**)&buf, bytes, st), "launch buffer allocation");
+    float* coord = reinterpret_cast<float*>(buf);
+    cudaError_t e = cudaSuccess;
+    for (int k = 0, off = 0; k < 3 && e == cudaSuccess; off += na[k], ++k)
+        e = cudaMemcpyAsync(coord + off, ah[k], (size_t)na[k] * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(buf, st);
+        return cuda_fail(e, "coordinate upload");
+    }
+    const float *x_arr = coord, *y_arr = coord + nx, *z_arr = coord + nx + ny;
     auto go = [&](auto store) {
         TraceJob<decltype(store)> J;
         J.f = store;
@@ -519,49 +578,49 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
         J.s.cross[1] = cross_dir_h ? cross_dir_h[1] : 0.f;
         J.s.cross[2] = cross_dir_h ? cross_dir_h[2] : 1.f;
         J.s.twist_on = twist ? 1 : 0;
+        if constexpr (!std::is_same<decltype(store), FieldStretch>::value)
+            J.lim.len_lim = (float)(prm->len_ratio * stretch_len_scale_host(J.f));
         return run_trace(J, prm->arith, twist, sc.schedule, n, sc.queue, st);
     };
-    const FieldStretch f{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
-                         make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    const int64_t cells = (int64_t)(nx - 1) + (ny - 1) + (nz - 1);
-    if (prm->arith != QSL_ARITH_FAST || cells * (1 + STRETCH_BINS_PER_CELL) >= (1LL << 31)) return go(f);
-    // fast arithmetic: the nodes interleaved into a stream-ordered float4
-    // copy for the launch (one 16-byte load per corner; the same values),
-    // followed, for the search, by its tables (a 16-byte record per cell, an
-    // int2 range per bin); the uniform formula needs none
-    const int64_t nodes = (int64_t)nx * ny * nz;
-    const int64_t tcells = uni ? 0 : cells;
-    const size_t bytes =
-        (size_t)(nodes + tcells) * sizeof(float4) + (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int2);
-    float4* b4 = nullptr;
-    QSL_CHECK_CUDA(cudaMallocAsync((void**)&b4, bytes, st), "node copy allocation");
+    int rc;
+    if (!packed_path) {
+        const FieldStretch f{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
+                             make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+        rc = go(f);
+        cudaFreeAsync(buf, st);
+        return rc;
+    }
+    // fast arithmetic: the nodes interleaved into a float4 copy for the
+    // launch (one 16-byte load per corner; the same values), followed, for
+    // the search, by its tables (a 16-byte record per cell, an int2 range per
+    // bin); the uniform formula needs none
+    float4* b4 = reinterpret_cast<float4*>(buf + coord_bytes);
     float4* srec = uni ? nullptr : b4 + nodes;
     int2* sbin = uni ? nullptr : reinterpret_cast<int2*>(srec + cells);
-    cudaError_t e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
+    e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
     if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {
-        cudaFreeAsync(b4, st);
+        cudaFreeAsync(buf, st);
         return cuda_fail(e, "node copy");
     }
     auto packed = [&](auto fp) {
         fp.bx = Bx;
         fp.by = By;
         fp.bz = Bz;
-        fp.d = f.d;
+        fp.d = Dims{nx, ny, nz};
         fp.ax = x_arr;
         fp.ay = y_arr;
         fp.az = z_arr;
         fp.uni_dev = nullptr;
-        fp.uni = f.uni;
-        fp.lo = fp.hi = fp.clo = fp.chi = fp.us = make_float3(0.f, 0.f, 0.f);
+        fp.uni = uni ? 1 : 0;
+        stretch_constants_host(fp, x_arr_h, y_arr_h, z_arr_h);
         fp.b4 = b4;
         fp.srec = srec;
         fp.sbin = sbin;
-        fp.sbinv = make_float3(0.f, 0.f, 0.f);
         return go(fp);
     };
-    const int rc = uni ? packed(FieldStretchPU{}) : packed(FieldStretchP{});
-    cudaFreeAsync(b4, st);
+    rc = uni ? packed(FieldStretchPU{}) : packed(FieldStretchP{});
+    cudaFreeAsync(buf, st);
     return rc;
 }
 
@@ -740,18 +799,18 @@ static void batch_layout(const BatchLists& L, qsl_batch_info* info) {
 // One launch per store type with jobs (a type without jobs launches nothing).
 static cudaError_t launch_slots(void* const jobs[], long long* const begin[], const int njobs[],
                                 const long long total[], const bool twist[], unsigned long long* samples,
-                                int max_blocks, long long lo, long long hi, cudaStream_t st) {
+                                int max_blocks, long long lo, long long hi, int occ, cudaStream_t st) {
     cudaError_t e = launch_trace_batch_soa((const TraceJob<FieldSoA>*)jobs[0], begin[0], njobs[0], total[0], twist[0],
-                                           samples, max_blocks, lo, hi, st);
+                                           samples, max_blocks, lo, hi, occ, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_f4((const TraceJob<FieldF4>*)jobs[1], begin[1], njobs[1], total[1], twist[1], samples,
-                                  max_blocks, lo, hi, st);
+                                  max_blocks, lo, hi, occ, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_h4b((const TraceJob<FieldH4B>*)jobs[2], begin[2], njobs[2], total[2], twist[2],
-                                   samples, max_blocks, lo, hi, st);
+                                   samples, max_blocks, lo, hi, occ, st);
     if (e == cudaSuccess)
         e = launch_trace_batch_h8c((const TraceJob<FieldH8C>*)jobs[3], begin[3], njobs[3], total[3], twist[3],
-                                   samples, max_blocks, lo, hi, st);
+                                   samples, max_blocks, lo, hi, occ, st);
     return e;
 }
 
@@ -775,9 +834,11 @@ int qsl_batch_pack(const qsl_batch_job* jobs_h, int njobs, void* table_h, int64_
 }
 
 int qsl_batch_run_window(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
-                         int64_t line_lo, int64_t line_hi, int max_blocks, qsl_stream_t stream) {
+                         int64_t line_lo, int64_t line_hi, int max_blocks, int occupancy, qsl_stream_t stream) {
     if (!table_dev || !info_h) return fail(QSL_ERR_INVALID, "null table or info");
     if (max_blocks < 0) return fail(QSL_ERR_INVALID, "max_blocks must be >= 0");
+    if (occupancy != 0 && (occupancy < 6 || occupancy > 10))
+        return fail(QSL_ERR_INVALID, "occupancy must be 0, 6, 7, 8, 9 or 10");
     char* t = (char*)table_dev;
     const qsl_batch_info& I = *info_h;
     void* jobs[kStoreTypes];
@@ -792,7 +853,7 @@ int qsl_batch_run_window(const void* table_dev, const qsl_batch_info* info_h, un
         total[k] = I.total[k];
         tw[k] = I.twist[k] != 0;
     }
-    QSL_CHECK_CUDA(launch_slots(jobs, begin, nj, total, tw, samples_dev, max_blocks, line_lo, line_hi,
+    QSL_CHECK_CUDA(launch_slots(jobs, begin, nj, total, tw, samples_dev, max_blocks, line_lo, line_hi, occupancy,
                                 (cudaStream_t)stream),
                    "batch run");
     return QSL_OK;
@@ -800,7 +861,7 @@ int qsl_batch_run_window(const void* table_dev, const qsl_batch_info* info_h, un
 
 int qsl_batch_run(const void* table_dev, const qsl_batch_info* info_h, unsigned long long* samples_dev,
                   qsl_stream_t stream) {
-    return qsl_batch_run_window(table_dev, info_h, samples_dev, 0, -1, 0, stream);
+    return qsl_batch_run_window(table_dev, info_h, samples_dev, 0, -1, 0, 0, stream);
 }
 
 int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream, qsl_batch_t** out) {
@@ -840,7 +901,7 @@ int qsl_batch_create(const qsl_batch_job* jobs_h, int njobs, qsl_stream_t stream
 
 int qsl_batch_launch(const qsl_batch_t* B, unsigned long long* samples_dev, qsl_stream_t stream) {
     if (!B) return fail(QSL_ERR_INVALID, "batch is null");
-    QSL_CHECK_CUDA(launch_slots(B->jobs, B->begin, B->njobs, B->total, B->twist, samples_dev, 0, 0, -1,
+    QSL_CHECK_CUDA(launch_slots(B->jobs, B->begin, B->njobs, B->total, B->twist, samples_dev, 0, 0, -1, 0,
                                 (cudaStream_t)stream),
                    "batch launch");
     return QSL_OK;

@@ -246,6 +246,16 @@ struct FieldStretchT {
         }
     }
     __device__ __forceinline__ const float* axis(int k) const { return k == 0 ? ax : (k == 1 ? ay : az); }
+    // one node's (Bx, By, Bz)
+    __device__ __forceinline__ float3 node(int ix, int iy, int iz) const {
+        const int64_t o = ix + (int64_t)d.nx * (iy + (int64_t)d.ny * iz);
+        if constexpr (M == 1 || M == 2) {
+            const float4 v = __ldg(b4 + o);
+            return v3(v.x, v.y, v.z);
+        } else {
+            return v3(__ldg(bx + o), __ldg(by + o), __ldg(bz + o));
+        }
+    }
 };
 using FieldStretch = FieldStretchT<0>;
 using FieldStretchP = FieldStretchT<1>;
@@ -743,12 +753,35 @@ __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, floa
     stretch_locate<EXACT>(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, f.sbinv.x, ix, rx);
     stretch_locate<EXACT>(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, f.sbinv.y, iy, ry);
     stretch_locate<EXACT>(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, f.sbinv.z, iz, rz);
-    float w[8];
-    if (EXACT) weights_exact(rx, ry, rz, w);
-    else weights_fast(rx, ry, rz, w);
-    float3 c[8];
-    f.corners(ix, iy, iz, c);
-    float3 r = blend<EXACT>(c, w);
+    float3 r;
+    if constexpr (EXACT) {
+        float w[8];
+        weights_exact(rx, ry, rz, w);
+        float3 c[8];
+        f.corners(ix, iy, iz, c);
+        r = blend<true>(c, w);
+    } else {
+        // fast arithmetic: x-lerps of the four corner pairs as each pair is
+        // loaded, then y, then z, so that at most a pair of corners is live
+        // (the eight corners and weights of a one-shot blend held the
+        // kernel's register count near 170); (Bx, By) on the packed pipe
+        const float ox = 1.f - rx, oy = 1.f - ry, oz = 1.f - rz;
+        float2 exy[4];
+        float ez[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float3 a = f.node(ix, iy + (q >> 1), iz + (q & 1));
+            const float3 b = f.node(ix + 1, iy + (q >> 1), iz + (q & 1));
+            exy[q] = __ffma2_rn(make_float2(b.x, b.y), make_float2(rx, rx),
+                                __fmul2_rn(make_float2(a.x, a.y), make_float2(ox, ox)));
+            ez[q] = fmaf(b.z, rx, a.z * ox);
+        }
+        const float2 g0 = __ffma2_rn(exy[2], make_float2(ry, ry), __fmul2_rn(exy[0], make_float2(oy, oy)));
+        const float2 g1 = __ffma2_rn(exy[3], make_float2(ry, ry), __fmul2_rn(exy[1], make_float2(oy, oy)));
+        const float gz0 = fmaf(ez[2], ry, ez[0] * oy), gz1 = fmaf(ez[3], ry, ez[1] * oy);
+        const float2 rxy = __ffma2_rn(g1, make_float2(rz, rz), __fmul2_rn(g0, make_float2(oz, oz)));
+        r = v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
+    }
     if (unit) {
         if (EXACT) {
             const float nb = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);

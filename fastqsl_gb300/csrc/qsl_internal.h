@@ -59,16 +59,16 @@ cudaError_t launch_scott_fast_h8c(const ScottJob<FieldH8C>& J, int grad, bool tw
 // Batched trace over a job table in device memory (trace_fast_<store>.cu)
 cudaError_t launch_trace_batch_soa(const TraceJob<FieldSoA>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, int max_blocks,
-                                   long long line_lo, long long line_hi, cudaStream_t st);
+                                   long long line_lo, long long line_hi, int occupancy, cudaStream_t st);
 cudaError_t launch_trace_batch_f4(const TraceJob<FieldF4>* jobs, const long long* begin, int njobs, long long total,
                                   bool twist, unsigned long long* samples, int max_blocks,
-                                   long long line_lo, long long line_hi, cudaStream_t st);
+                                   long long line_lo, long long line_hi, int occupancy, cudaStream_t st);
 cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, int max_blocks,
-                                   long long line_lo, long long line_hi, cudaStream_t st);
+                                   long long line_lo, long long line_hi, int occupancy, cudaStream_t st);
 cudaError_t launch_trace_batch_h8c(const TraceJob<FieldH8C>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, int max_blocks,
-                                   long long line_lo, long long line_hi, cudaStream_t st);
+                                   long long line_lo, long long line_hi, int occupancy, cudaStream_t st);
 
 // curl.cu (compiled with -fmad=false)
 cudaError_t launch_curl(const float* bx, const float* by, const float* bz, const float* ax, const float* ay,

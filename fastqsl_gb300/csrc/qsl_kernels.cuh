@@ -79,20 +79,27 @@ static cudaError_t launch_scott(const ScottJob<F>& J, int grad, bool twist, long
     return cudaGetLastError();
 }
 
-// Batched trace: one line per thread, 8 resident blocks/SM (the register
-// budget measured best for the lockstep tracer).
-template <bool TWIST, class F>
-__global__ void __launch_bounds__(kTraceBlock, 8) k_trace_batch(const TraceJob<F>* __restrict__ jobs,
-                                                                 const long long* __restrict__ begin, int njobs,
-                                                                 unsigned long long* samples, long long line_lo,
-                                                                 long long line_hi) {
+// Batched trace: one line per thread; MINB resident blocks per SM the
+// register allocation must allow (6-10; the autotuner picks, 8 by default).
+template <bool TWIST, class F, int MINB>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace_batch(const TraceJob<F>* __restrict__ jobs,
+                                                                    const long long* __restrict__ begin, int njobs,
+                                                                    unsigned long long* samples, long long line_lo,
+                                                                    long long line_hi) {
     batch_kernel_body<TWIST>(jobs, begin, njobs, samples, line_lo, line_hi);
+}
+
+template <class F, int MINB>
+static void launch_batch_minb(int grid, const TraceJob<F>* jobs, const long long* begin, int njobs, bool twist,
+                              unsigned long long* samples, long long line_lo, long long line_hi, cudaStream_t st) {
+    if (twist) k_trace_batch<true, F, MINB><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
+    else k_trace_batch<false, F, MINB><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
 }
 
 template <class F>
 static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin, int njobs, long long total,
                                 bool twist, unsigned long long* samples, int max_blocks, long long line_lo,
-                                long long line_hi, cudaStream_t st) {
+                                long long line_hi, int occupancy, cudaStream_t st) {
     if (njobs <= 0 || total <= 0) return cudaSuccess;
     if (line_lo < 0) line_lo = 0;
     if (line_hi < 0 || line_hi > total) line_hi = total;
@@ -100,8 +107,13 @@ static cudaError_t launch_batch(const TraceJob<F>* jobs, const long long* begin,
     long long g = (line_hi - line_lo + kTraceBlock - 1) / kTraceBlock;
     if (max_blocks > 0 && g > max_blocks) g = max_blocks;  // the grid-stride loop covers the rest
     const int grid = (int)(g > (1 << 30) ? (1 << 30) : g);
-    if (twist) k_trace_batch<true, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
-    else k_trace_batch<false, F><<<grid, kTraceBlock, 0, st>>>(jobs, begin, njobs, samples, line_lo, line_hi);
+    switch (occupancy) {
+        case 6: launch_batch_minb<F, 6>(grid, jobs, begin, njobs, twist, samples, line_lo, line_hi, st); break;
+        case 7: launch_batch_minb<F, 7>(grid, jobs, begin, njobs, twist, samples, line_lo, line_hi, st); break;
+        case 9: launch_batch_minb<F, 9>(grid, jobs, begin, njobs, twist, samples, line_lo, line_hi, st); break;
+        case 10: launch_batch_minb<F, 10>(grid, jobs, begin, njobs, twist, samples, line_lo, line_hi, st); break;
+        default: launch_batch_minb<F, 8>(grid, jobs, begin, njobs, twist, samples, line_lo, line_hi, st); break;
+    }
     return cudaGetLastError();
 }
 

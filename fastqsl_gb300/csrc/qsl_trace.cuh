@@ -261,6 +261,9 @@ __device__ __forceinline__ double len_scale(const FieldStretchT<M>& f) {
 }
 template <int M>
 __device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
+    // the packed stores' constants are formed on the host (qsl_trace_stretch)
+    // in this same arithmetic and stay kernel parameters
+    if constexpr (M == 1 || M == 2) return;
     f.lo = v3(__ldg(f.ax), __ldg(f.ay), __ldg(f.az));
     f.hi = v3(__ldg(f.ax + f.d.nx - 1), __ldg(f.ay + f.d.ny - 1), __ldg(f.az + f.d.nz - 1));
     // per-sample constants of the cell search, formed once (the FP64 pipe
@@ -558,8 +561,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     F f = J.f;
     // only the drop-in stores (the caller's arrays) take their shape from the
     // device; the packed stores' dims stay kernel parameters
-    if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value ||
-                  std::is_same<F, FieldStretchP>::value || std::is_same<F, FieldStretchPU>::value) {
+    if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value) {
         if (J.shape_dev) {
             f.d.nx = __ldg(J.shape_dev);
             f.d.ny = __ldg(J.shape_dev + 1);
@@ -582,12 +584,14 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     if (J.s.n_cap >= 0 && n > J.s.n_cap) n = J.s.n_cap;
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
     store_prepare(f);
-    // the packed stores' dims are known on the host: their length limit is a
-    // kernel parameter (a register would be re-formed from the double
+    // the packed stores' dims (and the stretched stores' coordinate
+    // extents) are known on the host: their length limit is a kernel
+    // parameter (a register would be re-formed from the double
     // product at every step once the loop runs short of registers)
     typename Lane<EXACT>::len_t len_lim;
-    if constexpr (!EXACT && (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldH4BW>::value || std::is_same<F, FieldF4>::value ||
-                             std::is_same<F, FieldH8C>::value))
+    if constexpr (!EXACT && (std::is_same<F, FieldH4B>::value || std::is_same<F, FieldH4BW>::value ||
+                             std::is_same<F, FieldF4>::value || std::is_same<F, FieldH8C>::value ||
+                             std::is_same<F, FieldStretchP>::value || std::is_same<F, FieldStretchPU>::value))
         len_lim = J.lim.len_lim;
     else
         len_lim = (typename Lane<EXACT>::len_t)(J.prm.len_ratio * len_scale(f));

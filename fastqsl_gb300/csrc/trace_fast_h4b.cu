@@ -15,8 +15,8 @@ cudaError_t launch_scott_fast_h4b(const ScottJob<FieldH4B>& J, int grad, bool tw
 
 cudaError_t launch_trace_batch_h4b(const TraceJob<FieldH4B>* jobs, const long long* begin, int njobs,
                                    long long total, bool twist, unsigned long long* samples, int max_blocks,
-                                   long long line_lo, long long line_hi, cudaStream_t st) {
-    return launch_batch(jobs, begin, njobs, total, twist, samples, max_blocks, line_lo, line_hi, st);
+                                   long long line_lo, long long line_hi, int occupancy, cudaStream_t st) {
+    return launch_batch(jobs, begin, njobs, total, twist, samples, max_blocks, line_lo, line_hi, occupancy, st);
 }
 
 }  // namespace qsl

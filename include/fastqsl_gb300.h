@@ -284,9 +284,11 @@ int qsl_batch_pack(const qsl_batch_job *jobs_h, int njobs, void *table_h, int64_
  * launch (0 = no limit; the blocks then loop over the lines).  A serving loop
  * runs a large batch as a sequence of such windows, so that small requests
  * never share the GPU with more than a window of it, and caps its resident
- * blocks below the GPU's capacity. */
+ * blocks below the GPU's capacity.  occupancy: the register budget of the
+ * batched kernels, for this many resident 128-thread blocks per SM (6-10;
+ * 0 = 8). */
 int qsl_batch_run_window(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
-                         int64_t line_lo, int64_t line_hi, int max_blocks, qsl_stream_t stream);
+                         int64_t line_lo, int64_t line_hi, int max_blocks, int occupancy, qsl_stream_t stream);
 int qsl_batch_run(const void *table_dev, const qsl_batch_info *info_h, unsigned long long *samples_dev,
                   qsl_stream_t stream);
 
@@ -349,16 +351,22 @@ int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, con
                                 const float *tol_coef, int64_t capacity, qsl_stream_t stream);
 
 /* Native form: host scalars and settings; Bx/By/Bz of shape nx x ny x nz (x
- * fastest) and the coordinates (increasing) on the device; uni as above.
- * sched may be NULL (static one-line-per-thread grid) or give the schedule,
- * order map, sample counter and occupancy (6: the 6-blocks-per-SM variant of
- * the fast kernels; 0: the default).  In fast arithmetic the call allocates,
- * stream-ordered on `stream` (cudaMallocAsync, freed after the launch), an
- * interleaved float4 copy of the nodes (16 B per node) and, for the search,
- * per-axis search tables (48 B per cell of each axis); the outputs equal the
- * drop-in's (fast arithmetic) bit for bit. */
+ * fastest) on the device, the node coordinates (strictly increasing) on the
+ * HOST (nx + ny + nz floats); uni as above.  The per-axis constants of the
+ * cell location (first and last coordinate, their 1e-6 offsets, the
+ * uniform spacing, the search-table bin width) and the length limit are
+ * formed on the host, in the same arithmetic as the drop-in forms them on
+ * the device, and reach the kernels as parameters.  sched may be NULL
+ * (static one-line-per-thread grid) or give the schedule, order map, sample
+ * counter and occupancy (6: the 6-blocks-per-SM variant of the fast kernels;
+ * 0: the default).  The call allocates, stream-ordered on `stream`
+ * (cudaMallocAsync, freed after the launch), a device copy of the
+ * coordinates (copied from the host arrays before the call returns) and, in
+ * fast arithmetic, an interleaved float4 copy of the nodes (16 B per node)
+ * and, for the search, per-axis search tables (48 B per cell of each axis);
+ * the outputs equal the drop-in's (fast arithmetic) bit for bit. */
 int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz,
-                      const float *x_arr, const float *y_arr, const float *z_arr, int uni,
+                      const float *x_arr_h, const float *y_arr_h, const float *z_arr_h, int uni,
                       const qsl_trace_params *prm, const qsl_trace_io *io, int64_t n, float s_len, float tol_coef,
                       const float *cross_dir_h, const float *curBx, const float *curBy, const float *curBz,
                       const qsl_sched *sched_h, qsl_stream_t stream);

@@ -1,5 +1,7 @@
-"""The launch-configuration tuner measures every candidate and applies the
-fastest; the tuned plan's Q equals an untuned plan's to rounding."""
+"""The launch-configuration tuner measures every candidate (seed tile,
+register budget, static lockstep or work queue with its refill size) and
+applies the fastest; the tuned plan's Q equals an untuned plan's to
+rounding."""
 import numpy as np
 import pytest
 import torch
@@ -18,8 +20,13 @@ def test_tune_plan(cuda):
     plan = api.QMapPlan(n0, n1, 3)
     q0 = plan.run(fs, xs, ys, zs, prm, s_len=0.25).cpu().numpy()
     res = autotune.tune_plan(plan, fs, xs, ys, zs, prm, s_len=0.25, sample_planes=2, use_cache=False)
-    assert len(res["table"]) == len(autotune.TILES) * len(autotune.OCCUPANCIES)
+    # every tile x budget in static lockstep, then the work queue at each
+    # refill size on the best of those
+    assert len(res["table"]) == len(autotune.TILES) * len(autotune.OCCUPANCIES) + len(autotune.QUEUE_CHUNKS)
     assert res["ms"] == min(res["table"].values())
+    assert res["schedule"] in ("static", "queue") and plan.schedule == res["schedule"]
+    if res["schedule"] == "queue":
+        assert plan.chunk == res["chunk"] in autotune.QUEUE_CHUNKS
     q1 = plan.run(fs, xs, ys, zs, prm, s_len=0.25).cpu().numpy()
     assert (np.isnan(q0) == np.isnan(q1)).mean() >= 0.99
     ok = ~np.isnan(q0) & ~np.isnan(q1)

@@ -71,3 +71,27 @@ def test_batch_matches_single_job_pipeline(cuda):
         ok = ~np.isnan(q1) & ~np.isnan(qb)
         d = np.abs(np.log10(q1[ok]) - np.log10(qb[ok]))
         assert np.median(d) <= 1e-5, np.median(d)
+
+
+def test_batch_register_budgets_agree_and_tuner_applies(cuda):
+    """The batched kernels compiled for 6-10 resident blocks per SM give the
+    same Q maps bit for bit (only the register allocation differs); the
+    autotuner's choice is one of them and is what the batch then runs with,
+    captured graph included."""
+    from fastqsl_gb300 import api, autotune
+    specs, stores = _specs()
+    qb = api.QBatch(specs)
+    ref = [q.cpu().numpy() for q in qb.run()]
+    for occ in (6, 7, 9, 10):
+        qb.occupancy = occ
+        got = [q.cpu().numpy() for q in qb.run()]
+        for a, b in zip(got, ref):
+            np.testing.assert_array_equal(a, b)
+    res = autotune.tune_batch(qb, windows=4, window_lines=1024)
+    assert res["occupancy"] in autotune.BATCH_OCCUPANCIES and qb.occupancy == res["occupancy"]
+    assert set(res["table"]) == {f"occ{o}" for o in autotune.BATCH_OCCUPANCIES}
+    qb.capture()
+    got = [q.cpu().numpy() for q in qb.replay()]
+    torch.cuda.synchronize()
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)

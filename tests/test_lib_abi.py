@@ -99,4 +99,6 @@ def test_new_entries_validate_without_gpu(lib):
     assert b"null" in lib.qsl_last_error()
     # qsl_batch_run_window: null table
     info = _lib.BatchInfo()
-    assert lib.qsl_batch_run_window(None, ctypes.byref(info), None, 0, -1, 0, None) != 0
+    assert lib.qsl_batch_run_window(None, ctypes.byref(info), None, 0, -1, 0, 0, None) != 0
+    assert lib.qsl_batch_run_window(ctypes.c_void_p(256), ctypes.byref(info), None, 0, -1, 0, 5, None) == -1
+    assert b"occupancy" in lib.qsl_last_error()
