@@ -37,7 +37,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-FIELD_SHAPE = (512, 512, 256)
+FIELD_SHAPE = [512, 512, 256]
 SUB = dict(x0=128, y0=128, z0=64, nx=256, ny=256, nz=128)
 S_LEN = 0.25
 METRIC = "Q-pixels/s (3-D Q-cube, 512x512x256 field, RKF45 tol 1e-4)"
@@ -98,6 +98,10 @@ class ClockSampler:
                           if r[5 + i].strip().lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload_name():
+    return "qcube-{}-charges32-sub256x256x128-rkf45-tol1e-4".format("x".join(map(str, FIELD_SHAPE)))
 
 
 def spread_planes(n):
@@ -711,7 +715,15 @@ def main():
     ap.add_argument("--batched-only", action="store_true", help="only the batched-graph section (profiling)")
     ap.add_argument("--planes", type=int, default=SUB["nz"], help="z-planes of the cube (profiling: fewer)")
     ap.add_argument("--plane-offset", type=int, default=0, help="first z-plane with --planes")
+    ap.add_argument("--field-nz", type=int, default=FIELD_SHAPE[2],
+                    help="z nodes of the field (512: a 512^3 field around the same central Q-cube)")
     args = ap.parse_args()
+    if args.field_nz != FIELD_SHAPE[2]:
+        # a taller field: the Q sub-box stays central (z offset by half the
+        # extra height), the charges keep their depths below z = 0
+        nz = max(SUB["nz"] + 2, int(args.field_nz))
+        SUB["z0"] += (nz - FIELD_SHAPE[2]) // 2
+        FIELD_SHAPE[2] = nz
     NPLANES[0] = max(1, min(SUB["nz"], args.planes))
     PLANE0[0] = max(0, min(SUB["nz"] - NPLANES[0], args.plane_offset))
 
@@ -751,7 +763,7 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(wall)) * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic",
-                "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
+                "config": {"workload": workload_name(),
                            "step": f"{npl} of the {SUB['nz']} z-planes ({qpix_step} Q-pixels), spread evenly "
                                    f"over the stack and shifted each step"},
                 "cpu_baseline": {**per[-1], "value": v,
@@ -789,7 +801,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (fp16 field storage)" if fp16 else "f32",
         "data": "synthetic",
-        "config": {"workload": "qcube-512x512x256-charges32-sub256x256x128-rkf45-tol1e-4",
+        "config": {"workload": workload_name(),
                    "field": "x".join(map(str, FIELD_SHAPE)), "qcube": "256x256x128", "layout": args.layout,
                    "interpolation": "FP32 weights and lerps of fp16 node values" if args.arith == "fast"
                    else "fp16 x weights (opt-in sampler)",

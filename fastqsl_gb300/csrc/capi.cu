@@ -336,6 +336,9 @@ static int run_trace(TraceJob<F>& J, int arith, bool twist, int schedule, long l
     } else if constexpr (std::is_same<F, FieldStretch>::value) {
         e = arith == QSL_ARITH_EXACT ? launch_trace_exact_stretch(J, twist, sched, n_host, st)
                                      : launch_trace_fast_stretch(J, twist, sched, n_host, st);
+    } else if constexpr (std::is_same<F, FieldStretchU>::value) {
+        e = arith == QSL_ARITH_EXACT ? launch_trace_exact_stretch_uni(J, twist, sched, n_host, st)
+                                     : launch_trace_fast_stretch_uni(J, twist, sched, n_host, st);
     } else {
         e = launch_trace_fast_h8c(J, twist, sched, n_host, st);
     }
@@ -550,7 +553,7 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     const int64_t ncoord = (int64_t)nx + ny + nz;
     const size_t coord_bytes = ((size_t)ncoord * sizeof(float) + 255) / 256 * 256;
     const size_t bytes = coord_bytes + (packed_path ? (size_t)(nodes + tcells) * sizeof(float4) +
-                                                          (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int2)
+                                                          (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int4)
                                                     : 0);
     char* buf = nullptr;
     QSL_CHECK_CUDA(cudaMallocAsync((void**)&buf, bytes, st), "launch buffer allocation");
@@ -578,25 +581,36 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
         J.s.cross[1] = cross_dir_h ? cross_dir_h[1] : 0.f;
         J.s.cross[2] = cross_dir_h ? cross_dir_h[2] : 1.f;
         J.s.twist_on = twist ? 1 : 0;
-        if constexpr (!std::is_same<decltype(store), FieldStretch>::value)
+        if constexpr (std::is_same<decltype(store), FieldStretchP>::value ||
+                      std::is_same<decltype(store), FieldStretchPU>::value)
             J.lim.len_lim = (float)(prm->len_ratio * stretch_len_scale_host(J.f));
         return run_trace(J, prm->arith, twist, sc.schedule, n, sc.queue, st);
     };
     int rc;
     if (!packed_path) {
-        const FieldStretch f{Bx, By, Bz, Dims{nx, ny, nz}, x_arr, y_arr, z_arr, nullptr, uni ? 1 : 0,
-                             make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-        rc = go(f);
+        // the caller's arrays with the one search the host knows applies
+        auto arrays = [&](auto fa) {
+            fa.bx = Bx;
+            fa.by = By;
+            fa.bz = Bz;
+            fa.d = Dims{nx, ny, nz};
+            fa.ax = x_arr;
+            fa.ay = y_arr;
+            fa.az = z_arr;
+            fa.uni_dev = nullptr;
+            return go(fa);
+        };
+        rc = uni ? arrays(FieldStretchU{}) : arrays(FieldStretch{});
         cudaFreeAsync(buf, st);
         return rc;
     }
     // fast arithmetic: the nodes interleaved into a float4 copy for the
     // launch (one 16-byte load per corner; the same values), followed, for
-    // the search, by its tables (a 16-byte record per cell, an int2 range per
-    // bin); the uniform formula needs none
+    // the search, by its tables (a 16-byte record per cell and per bin); the
+    // uniform formula needs none
     float4* b4 = reinterpret_cast<float4*>(buf + coord_bytes);
     float4* srec = uni ? nullptr : b4 + nodes;
-    int2* sbin = uni ? nullptr : reinterpret_cast<int2*>(srec + cells);
+    int4* sbin = uni ? nullptr : reinterpret_cast<int4*>(srec + cells);
     e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
     if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {
@@ -612,7 +626,6 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
         fp.ay = y_arr;
         fp.az = z_arr;
         fp.uni_dev = nullptr;
-        fp.uni = uni ? 1 : 0;
         stretch_constants_host(fp, x_arr_h, y_arr_h, z_arr_h);
         fp.b4 = b4;
         fp.srec = srec;
@@ -650,21 +663,35 @@ int qsl_trace_all_bline_stretch(int arith, const float* Bx, const float* By, con
                     B_end_z, LineLen, twist};
     if (!io_ok(&io)) return fail(QSL_ERR_INVALID, "null pointer in outputs");
     const bool twist_possible = curB_flag && curB_x && curB_y && curB_z && twist;
-    TraceJob<FieldStretch> J;
-    J.f = FieldStretch{Bx, By, Bz, Dims{2, 2, 2}, x_arr, y_arr, z_arr, flag_uni, 0, make_float3(0.f, 0.f, 0.f),
-                       make_float3(0.f, 0.f, 0.f)};
-    fill_common(J, &io, &prm, nullptr);
-    J.shape_dev = BshapeN;
-    J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
-    J.s.s_len_dev = s_len;
-    J.s.tol_coef_dev = tol_coef;
-    J.s.tol_coef = 1.f;
-    J.s.n_dev = N;
-    J.s.cross_dev = inp_cross_dir;
-    J.s.twist_flag_dev = twist_possible ? curB_flag : nullptr;
-    J.s.twist_on = 0;
-    J.s.n_cap = capacity < 0 ? -1 : capacity;
-    return run_trace(J, arith, twist_possible, QSL_SCHED_QUEUE, 0, nullptr, (cudaStream_t)stream);
+    // the search and the uniform formula compiled apart: both kernels are
+    // launched, and each returns at once unless *flag_uni is its own form
+    // (the flag lives on the device; reading it here would synchronise)
+    auto form = [&](auto f) {
+        TraceJob<decltype(f)> J;
+        f.bx = Bx;
+        f.by = By;
+        f.bz = Bz;
+        f.d = Dims{2, 2, 2};
+        f.ax = x_arr;
+        f.ay = y_arr;
+        f.az = z_arr;
+        f.uni_dev = flag_uni;
+        J.f = f;
+        fill_common(J, &io, &prm, nullptr);
+        J.shape_dev = BshapeN;
+        J.cur = FieldSoA{curB_x, curB_y, curB_z, Dims{2, 2, 2}};
+        J.s.s_len_dev = s_len;
+        J.s.tol_coef_dev = tol_coef;
+        J.s.tol_coef = 1.f;
+        J.s.n_dev = N;
+        J.s.cross_dev = inp_cross_dir;
+        J.s.twist_flag_dev = twist_possible ? curB_flag : nullptr;
+        J.s.twist_on = 0;
+        J.s.n_cap = capacity < 0 ? -1 : capacity;
+        return run_trace(J, arith, twist_possible, QSL_SCHED_QUEUE, 0, nullptr, (cudaStream_t)stream);
+    };
+    const int rc = form(FieldStretch{});
+    return rc != QSL_OK ? rc : form(FieldStretchU{});
 }
 
 int qsl_trace_all_bline_rkf45(const float* Bx, const float* By, const float* Bz, const int* BshapeN,

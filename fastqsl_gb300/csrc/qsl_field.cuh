@@ -198,17 +198,19 @@ struct FieldH8C {
 // ay[ny], az[nz].  uni selects the reference's uniform-spacing index formula
 // instead of its search; lo/hi are the first and last coordinates (set at
 // kernel start from the coordinate arrays).
-// M (mode): 0 = the caller's arrays, the search or the formula as uni says
-// at run time (the drop-in); 1 and 2 = packed: the node values come from an
-// interleaved float4 copy (b4: one 16-byte load per corner instead of three
-// 4-byte gathers; the same float values, so the same results), and the cell
-// search is fixed at compile time, so each inlined sample carries one search
-// only (the loop body is instruction-fetch bound): 1 = per-axis tables
-// (srec, sbin; built by launch_stretch_tables) that give the reference
-// search's own cell for every coordinate in two dependent loads instead of
-// ~log2(n); 2 = the uniform-spacing formula.  3 and 4 read the caller's
-// arrays with the search of 1 and 2 (the twist current density of a packed
-// launch, which stays in the caller's arrays).
+// M (mode) fixes the cell search at compile time, so each inlined sample
+// carries one search only (the loop body is instruction-fetch bound):
+// 1 and 2 = packed: the node values come from an interleaved float4 copy
+// (b4: one 16-byte load per corner instead of three 4-byte gathers; the same
+// float values, so the same results); 1 = per-axis tables (srec, sbin; built
+// by launch_stretch_tables) that give the reference search's own cell for
+// every coordinate in one or two dependent loads instead of ~log2(n); 2 = the
+// uniform-spacing formula.  3, 4 and 5 read the caller's arrays: 3 with the
+// tables (the twist current density of a packed search launch), 4 with the
+// formula (the drop-in's uniform form and the current density of a packed
+// uniform launch), 5 with the reference's bisection (the drop-in's search
+// form).  The drop-in, whose choice (flag_uni) lives on the device, launches
+// the 4 and 5 kernels and each returns at once unless the flag is its own.
 template <int M>
 struct FieldStretchT {
     const float* bx;
@@ -218,8 +220,7 @@ struct FieldStretchT {
     const float* ax;
     const float* ay;
     const float* az;
-    const bool* uni_dev;  // when set, uni is read from here (drop-in)
-    int uni;
+    const bool* uni_dev;  // drop-in: the kernel runs only if *uni_dev matches its mode
     float3 lo, hi;        // first and last node coordinates (read at kernel start)
     float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
     float3 us;            // uniform-formula spacing (hi - lo) / n
@@ -230,11 +231,13 @@ struct FieldStretchT {
     //            (a[j], a[j+1]] and its first coordinate and width:
     //            {a[i], a[i+1] - a[i], i as int bits, 0}
     //   sbin[b]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins over [a[0],
-    //            a[n-1]] per axis: the lowest and highest cell a coordinate
-    //            of the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
-    //            float rounding of the bin index) can lie in
+    //            a[n-1]] per axis, each covering the cells a coordinate of
+    //            the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
+    //            float rounding of the bin index) can lie in: one cell ->
+    //            that cell's record {i, j, a[i] bits, width bits}; more ->
+    //            {-1, lo, hi, 0}
     const float4* srec;
-    const int2* sbin;
+    const int4* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (M == 1 || M == 2) {
@@ -257,12 +260,13 @@ struct FieldStretchT {
         }
     }
 };
-using FieldStretch = FieldStretchT<0>;
+using FieldStretch = FieldStretchT<5>;    // caller's arrays, the reference's search
+using FieldStretchU = FieldStretchT<4>;   // caller's arrays, the uniform-spacing formula
 using FieldStretchP = FieldStretchT<1>;
 using FieldStretchPU = FieldStretchT<2>;
-// the search a mode runs: 1 tables, 2 formula, 0 chosen at run time
+// the search a mode runs: 1 tables, 2 formula, 3 the reference's bisection
 template <int M>
-constexpr int stretch_search_mode() { return M == 3 ? 1 : (M == 4 ? 2 : M); }
+constexpr int stretch_search_mode() { return M == 3 ? 1 : (M == 4 ? 2 : (M == 5 ? 3 : M)); }
 
 constexpr int STRETCH_BINS_PER_CELL = 4;
 // first table cell of axis k (0, 1, 2) for node counts d
@@ -710,8 +714,13 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, f
     const int nb = STRETCH_BINS_PER_CELL * (n - 1);
     int b = __float2int_rz((c - a0) * binv);
     b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-    const int2 range = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
-    int lo = range.x, hi = range.y;
+    const int4 bin = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
+    if (bin.x >= 0) {  // the bin covers one interval: its cell record is in the bin
+        ai = __int_as_float(bin.z);
+        di = __int_as_float(bin.w);
+        return bin.x;
+    }
+    int lo = bin.y, hi = bin.z;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (c > __ldg(a + mid)) lo = mid;
@@ -739,7 +748,7 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
         i = stretch_table(f, k, c, a0, binv, ai, di);
     } else {
         if constexpr (stretch_search_mode<M>() == 2) i = stretch_uni(c, n, a0, du);
-        else i = f.uni ? stretch_uni(c, n, a0, du) : stretch_bisect(c, n, a);
+        else i = stretch_bisect(c, n, a);
         ai = __ldg(a + i);
         di = __ldg(a + i + 1) - ai;
     }
@@ -796,6 +805,10 @@ __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, floa
 
 template <>
 __device__ __forceinline__ float3 sample<true, FieldStretch>(const FieldStretch& f, float3 p, bool unit) {
+    return sample_stretch<true>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample<true, FieldStretchU>(const FieldStretchU& f, float3 p, bool unit) {
     return sample_stretch<true>(f, p, unit);
 }
 template <>
@@ -879,6 +892,14 @@ __device__ __forceinline__ float3 sample_endpoint<true, FieldStretch>(const Fiel
 }
 template <>
 __device__ __forceinline__ float3 sample_endpoint<false, FieldStretch>(const FieldStretch& f, float3 p) {
+    return sample_stretch<false>(f, p, false);
+}
+template <>
+__device__ __forceinline__ float3 sample_endpoint<true, FieldStretchU>(const FieldStretchU& f, float3 p) {
+    return sample_stretch<true>(f, p, false);
+}
+template <>
+__device__ __forceinline__ float3 sample_endpoint<false, FieldStretchU>(const FieldStretchU& f, float3 p) {
     return sample_stretch<false>(f, p, false);
 }
 template <>

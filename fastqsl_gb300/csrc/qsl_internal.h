@@ -24,9 +24,13 @@ cudaError_t launch_trace_exact(const TraceJob<FieldSoA>& J, bool twist, Schedule
                                cudaStream_t st);
 cudaError_t launch_trace_exact_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
                                        cudaStream_t st);
+cudaError_t launch_trace_exact_stretch_uni(const TraceJob<FieldStretchU>& J, bool twist, Schedule sched,
+                                           long long n_host, cudaStream_t st);
 // trace_fast_stretch.cu
 cudaError_t launch_trace_fast_stretch(const TraceJob<FieldStretch>& J, bool twist, Schedule sched, long long n_host,
                                       cudaStream_t st);
+cudaError_t launch_trace_fast_stretch_uni(const TraceJob<FieldStretchU>& J, bool twist, Schedule sched,
+                                          long long n_host, cudaStream_t st);
 cudaError_t launch_trace_fast_stretch_packed(const TraceJob<FieldStretchP>& J, bool twist, Schedule sched,
                                              long long n_host, cudaStream_t st);
 // trace_fast_stretch_packed_uni.cu
@@ -90,7 +94,7 @@ cudaError_t launch_hybrid_merge(const int* bflag, const float* qperp, long long 
 // field_store.cu
 cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);
 cudaError_t launch_stretch_tables(const float* ax, const float* ay, const float* az, Dims d, float4* srec,
-                                  int2* sbin, cudaStream_t st);
+                                  int4* sbin, cudaStream_t st);
 cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
                             uint4* bricks, float* scale, cudaStream_t st);
 cudaError_t launch_pack_h8c(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,

@@ -226,6 +226,18 @@ __device__ __forceinline__ double len_scale(const F& f) {
 }
 template <class F>
 __device__ __forceinline__ void store_prepare(F&) {}
+// Whether this launch's kernel does the work: always, except for the
+// drop-in's two stretched kernels (search / uniform formula), of which only
+// the one matching the caller's device flag runs.
+template <class F>
+__device__ __forceinline__ bool store_active(const F&) { return true; }
+template <int M>
+__device__ __forceinline__ bool store_active(const FieldStretchT<M>& f) {
+    if constexpr (M == 4 || M == 5) {
+        if (f.uni_dev) return (*f.uni_dev) == (M == 4);
+    }
+    return true;
+}
 // The current density shares the traced field's grid; J.cur carries only its
 // three arrays, the geometry comes from the traced store (whose dims may have
 // been read from the device at kernel start).
@@ -272,7 +284,6 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
     f.chi = v3((float)((double)f.hi.x - 1e-6), (float)((double)f.hi.y - 1e-6), (float)((double)f.hi.z - 1e-6));
     f.us = v3((f.hi.x - f.lo.x) / __int2float_rd(f.d.nx), (f.hi.y - f.lo.y) / __int2float_rd(f.d.ny),
               (f.hi.z - f.lo.z) / __int2float_rd(f.d.nz));
-    if (f.uni_dev) f.uni = *f.uni_dev ? 1 : 0;
     if constexpr (M == 1) {
         // the bin width of the search tables (only picks the bin; the
         // tables' ranges absorb its rounding)
@@ -286,7 +297,7 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
 // tables or formula, else the drop-in's run-time choice).
 template <int M>
 __device__ __forceinline__ auto current_view(const FieldStretchT<M>& f, const FieldSoA& c) {
-    FieldStretchT<M == 1 ? 3 : (M == 2 ? 4 : 0)> r;
+    FieldStretchT<M == 1 ? 3 : (M == 2 ? 4 : M)> r;
     r.bx = c.bx;
     r.by = c.by;
     r.bz = c.bz;
@@ -295,7 +306,6 @@ __device__ __forceinline__ auto current_view(const FieldStretchT<M>& f, const Fi
     r.ay = f.ay;
     r.az = f.az;
     r.uni_dev = nullptr;
-    r.uni = f.uni;
     r.lo = f.lo;
     r.hi = f.hi;
     r.clo = f.clo;
@@ -561,7 +571,8 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     F f = J.f;
     // only the drop-in stores (the caller's arrays) take their shape from the
     // device; the packed stores' dims stay kernel parameters
-    if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value) {
+    if constexpr (std::is_same<F, FieldSoA>::value || std::is_same<F, FieldStretch>::value ||
+                  std::is_same<F, FieldStretchU>::value) {
         if (J.shape_dev) {
             f.d.nx = __ldg(J.shape_dev);
             f.d.ny = __ldg(J.shape_dev + 1);
@@ -583,6 +594,7 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
     long long n = J.s.n_dev ? (long long)__ldg(J.s.n_dev) : J.s.n;
     if (J.s.n_cap >= 0 && n > J.s.n_cap) n = J.s.n_cap;
     const bool tw_on = TWIST && (J.s.twist_flag_dev ? *J.s.twist_flag_dev : (J.s.twist_on != 0));
+    if (!store_active(f)) return;
     store_prepare(f);
     // the packed stores' dims (and the stretched stores' coordinate
     // extents) are known on the host: their length limit is a kernel

@@ -48,6 +48,11 @@ cudaError_t launch_trace_exact_stretch(const TraceJob<FieldStretch>& J, bool twi
     return launch_exact(J, twist, sched, n_host, st);
 }
 
+cudaError_t launch_trace_exact_stretch_uni(const TraceJob<FieldStretchU>& J, bool twist, Schedule sched,
+                                           long long n_host, cudaStream_t st) {
+    return launch_exact(J, twist, sched, n_host, st);
+}
+
 template <bool TWIST>
 __global__ void __launch_bounds__(kTraceBlock) k_scott_exact(const ScottJob<FieldSoA> J) {
     scott_kernel_body<true, GRAD_FD, TWIST>(J);
