@@ -29,10 +29,10 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
 //    value up to nb: 4e-7 nb bins covers it), in double, each the largest
 //    j <= n-2 with a[j] below the edge (0 if none).  A coordinate the
 //    kernel puts in bin b lies within those edges, so its interval is in the
-//    range, on axes of any length.  A bin whose range is one interval holds
-//    that interval's cell record itself, {i, j, a[i], a[i+1] - a[i]} (one
-//    load finds the cell); a wider one {-1, lo, hi, 0} (the kernel bisects
-//    over the range and reads the interval's record).
+//    range, on axes of any length.  (Bins holding the cell record of a
+//    one-interval range themselves, to save the dependent record load,
+//    measured slower: 10.0 against 8.7 ms on the search workload, the
+//    lanes of a warp diverging between the two cases.)
 __device__ __forceinline__ int stretch_cell_below(double c, int n, const float* __restrict__ a) {
     int lo = 0, hi = n - 2;  // largest j in [0, n-2] with a[j] < c, else 0
     while (lo < hi) {
@@ -45,7 +45,7 @@ __device__ __forceinline__ int stretch_cell_below(double c, int n, const float* 
 
 __global__ void k_stretch_tables(const float* __restrict__ ax, const float* __restrict__ ay,
                                  const float* __restrict__ az, Dims d, float4* __restrict__ srec,
-                                 int4* __restrict__ sbin) {
+                                 int2* __restrict__ sbin) {
     const int cells = (d.nx - 1) + (d.ny - 1) + (d.nz - 1);
     const int bins = STRETCH_BINS_PER_CELL * cells;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells + bins; t += gridDim.x * blockDim.x) {
@@ -67,19 +67,13 @@ __global__ void k_stretch_tables(const float* __restrict__ ax, const float* __re
             const double wid = 0.01 + 4e-7 * (double)nb;
             const int lo = stretch_cell_below(a0 + (b - wid) * w, n, a);
             const int hi = stretch_cell_below(a0 + (b + 1 + wid) * w, n, a);
-            if (hi <= lo) {
-                const int i = stretch_bisect(__ldg(a + lo + 1), n, a);
-                const float ai = __ldg(a + i);
-                sbin[t - cells] = make_int4(i, lo, __float_as_int(ai), __float_as_int(__ldg(a + i + 1) - ai));
-            } else {
-                sbin[t - cells] = make_int4(-1, lo, hi, 0);
-            }
+            sbin[t - cells] = make_int2(lo, hi < lo ? lo : hi);
         }
     }
 }
 
 cudaError_t launch_stretch_tables(const float* ax, const float* ay, const float* az, Dims d, float4* srec,
-                                  int4* sbin, cudaStream_t st) {
+                                  int2* sbin, cudaStream_t st) {
     const long long total = (long long)(1 + STRETCH_BINS_PER_CELL) * ((d.nx - 1) + (d.ny - 1) + (d.nz - 1));
     long long g = (total + 255) / 256;
     if (g > 4096) g = 4096;

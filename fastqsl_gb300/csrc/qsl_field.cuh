@@ -231,13 +231,11 @@ struct FieldStretchT {
     //            (a[j], a[j+1]] and its first coordinate and width:
     //            {a[i], a[i+1] - a[i], i as int bits, 0}
     //   sbin[b]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins over [a[0],
-    //            a[n-1]] per axis, each covering the cells a coordinate of
-    //            the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
-    //            float rounding of the bin index) can lie in: one cell ->
-    //            that cell's record {i, j, a[i] bits, width bits}; more ->
-    //            {-1, lo, hi, 0}
+    //            a[n-1]] per axis: the lowest and highest cell a coordinate
+    //            of the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
+    //            float rounding of the bin index) can lie in
     const float4* srec;
-    const int4* sbin;
+    const int2* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (M == 1 || M == 2) {
@@ -714,13 +712,8 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, f
     const int nb = STRETCH_BINS_PER_CELL * (n - 1);
     int b = __float2int_rz((c - a0) * binv);
     b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-    const int4 bin = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
-    if (bin.x >= 0) {  // the bin covers one interval: its cell record is in the bin
-        ai = __int_as_float(bin.z);
-        di = __int_as_float(bin.w);
-        return bin.x;
-    }
-    int lo = bin.y, hi = bin.z;
+    const int2 range = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
+    int lo = range.x, hi = range.y;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (c > __ldg(a + mid)) lo = mid;
