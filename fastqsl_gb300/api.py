@@ -521,6 +521,81 @@ def _hybrid_impl(self, field, xs, ys, zs, params, s_len, tol_coef, scott_params,
 QMapPlan._hybrid = _hybrid_impl
 
 
+class QSeries:
+    """Q maps of a series of fields given on the host (the snapshots of a
+    simulation, a run of magnetograms' extrapolations) on one seed geometry,
+    pipelined over two field stores and two plans:
+
+    * upload: field k's H2D copy on the uploader's copy stream (pinned host
+      arrays, FieldUploader) while earlier fields are on the GPU;
+    * pack: field k into store k % 2 on a pack stream, once that store's
+      previous trace (field k - 2) is done: it overlaps field k - 1's trace;
+    * trace + Q: plan k % 2 on `stream` (default: the current stream), once
+      field k is packed and that plan's previous Q (field k - 2) has been
+      copied out;
+    * D2H: field k's Q into the caller's pinned host tensor on a copy stream,
+      overlapping field k + 1's trace.
+
+    Nothing here synchronises the host; wait() makes `stream` wait for every
+    queued copy.  Each field's Q equals QMapPlan.run's on that field alone
+    (the same kernels on the same inputs)."""
+
+    def __init__(self, shape, n0, n1, nplanes, layout="h4b", device="cuda", tile=(8, 8), occupancy=None):
+        self.device = torch.device(device)
+        self.up = FieldUploader(shape, device=self.device)
+        zero = torch.zeros(tuple(shape)[::-1], dtype=torch.float32, device=self.device).permute(2, 1, 0)
+        self.stores = [FieldStore(zero, zero, zero, layout=layout) for _ in range(2)]
+        self.plans = [QMapPlan(n0, n1, nplanes, device=self.device, tile=tile, occupancy=occupancy)
+                      for _ in range(2)]
+        self.pack_stream = torch.cuda.Stream(device=self.device)
+        self.d2h_stream = torch.cuda.Stream(device=self.device)
+        self.traced = [None, None]   # per store / plan: the event after its last trace and Q
+        self.copied = [None, None]   # per plan: the event after its last Q copy to the host
+        self.k = 0
+
+    def push(self, Bx, By, Bz, xs, ys, zs, params, q_out, stream=None, **run_kw):
+        """Queues one field (pinned host arrays as FieldUploader.upload takes
+        them) through the pipeline; its Q lands in `q_out`, a pinned CPU
+        float64 tensor of the plan's Q shape, once wait() (or an event after
+        it) has completed.  run_kw: QMapPlan.run's settings (s_len, stride,
+        cross_dir, tol_coef, ...)."""
+        st = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.current_stream(self.device)
+        s = self.k % 2
+        self.k += 1
+        slot = self.up.upload(Bx, By, Bz)
+        if self.traced[s] is not None:
+            self.pack_stream.wait_event(self.traced[s])
+        self.up.pack(self.stores[s], slot, self.pack_stream)
+        packed = torch.cuda.Event()
+        packed.record(self.pack_stream)
+        st.wait_event(packed)
+        if self.copied[s] is not None:
+            st.wait_event(self.copied[s])
+        q = self.plans[s].run(self.stores[s], xs, ys, zs, params, stream=st, **run_kw)
+        ev = torch.cuda.Event()
+        ev.record(st)
+        self.traced[s] = ev
+        self.d2h_stream.wait_event(ev)
+        with torch.cuda.stream(self.d2h_stream):
+            q_out.copy_(q, non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(self.d2h_stream)
+        self.copied[s] = done
+        return q_out
+
+    def wait(self, stream=None):
+        """Makes `stream` (default: the current stream) wait for every field
+        queued so far, its Q copied to the host included."""
+        st = stream if isinstance(stream, torch.cuda.Stream) else torch.cuda.current_stream(self.device)
+        for ev in self.copied:
+            if ev is not None:
+                st.wait_event(ev)
+
+    def close(self):
+        for fs in self.stores:
+            fs.close()
+
+
 def plane_seed_grid(x0, x1, nx, y0, y1, ny, zs, device="cuda"):
     """Stacked seed planes: for each z in `zs`, an (ny, nx) grid over
     [x0, x1] x [y0, y1] (linspace per axis, rows along y).  Returns flattened

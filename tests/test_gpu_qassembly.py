@@ -202,3 +202,36 @@ def test_field_uploader_pipeline(cuda, layout):
         np.testing.assert_array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
     with pytest.raises(ValueError):
         up.upload(*[h[:-1] for h in hosts[0]])
+
+
+@pytest.mark.parametrize("layout", ["h4b", "f4"])
+def test_qseries_pipeline(cuda, layout):
+    """A series of host fields through api.QSeries (two stores, two plans:
+    uploads, packs and Q copies to the host overlapping the neighbouring
+    fields' traces): every field's Q equals the Q of a plan run on a store
+    built directly from that field, bit for bit, with four fields
+    alternating over the two stores."""
+    from fastqsl_gb300 import api, synthetic as S
+    shape = (56, 48, 40)
+    fields = [S.make_field(S.charges_random(40 + k, shape, 4 + k)) for k in range(4)]
+    n0, n1 = 24, 28
+    xs, ys, zz = api.plane_seed_grid(3.0, 3.0 + 1.5 * (n1 - 1), n1, 3.0, 3.0 + 1.5 * (n0 - 1), n0, [0.0, 5.0])
+    prm = P.absolute_rkf45()
+    plan = api.QMapPlan(n0, n1, 2)
+    ref = []
+    for B in fields:
+        fs = api.FieldStore(*[torch.from_numpy(b) for b in B], layout=layout)
+        ref.append(plan.run(fs, xs, ys, zz, prm, s_len=0.25, stride=1.5).cpu().numpy())
+        fs.close()
+    hosts = [[torch.from_numpy(np.ascontiguousarray(b.transpose(2, 1, 0))).pin_memory() for b in B] for B in fields]
+    series = api.QSeries(shape, n0, n1, 2, layout=layout)
+    outs = [torch.empty((2, n0 - 2, n1 - 2), dtype=torch.float64).pin_memory() for _ in fields]
+    for h, q in zip(hosts, outs):
+        series.push(*h, xs, ys, zz, prm, q, s_len=0.25, stride=1.5)
+    series.wait()
+    torch.cuda.synchronize()
+    for a, b in zip(outs, ref):
+        a = a.numpy()
+        np.testing.assert_array_equal(np.isnan(a), np.isnan(b))
+        np.testing.assert_array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
+    series.close()
