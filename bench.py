@@ -626,10 +626,15 @@ def forms(device, planes=16):
         api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01, uni=uni, samples=cnt)
         torch.cuda.synchronize()
         tiles = api.tile_order(1, 1024, 1024, 8, 8, device)
+        # static lockstep over the register budgets (4, 5 = the default, 6
+        # blocks per SM) in seed rows and 8x8 tiles; the work queue at the
+        # default budget in tiles
+        cfgs = [("static", o, name, order) for o in (4, 5, 6) for name, order in (("rows", None), ("tiles", tiles))]
+        cfgs.append(("queue", 5, "tiles", tiles))
         cfg_ms = {f"{sch}/occ{o}/{name}": timed(lambda: api.trace_stretch(*Bs, coords, px, py, pz, sp, s_len=0.01,
                                                                           uni=uni, occupancy=o, schedule=sch,
                                                                           order=order))
-                  for sch in ("static", "queue") for o in (0, 6) for name, order in (("rows", None), ("tiles", tiles))}
+                  for sch, o, name, order in cfgs}
         ms = min(cfg_ms.values())
         res["stretch_" + ("uniform_formula" if uni else "search")] = {
             "grid": "x".join(map(str, shape)), "z_ratio": ratio, "lines": int(px.numel()), "ms": ms,

@@ -250,8 +250,8 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     coords = (x_arr, y_arr, z_arr) increasing node coordinates, seeds in the
     same physical coordinates (float32 CUDA vectors).  uni: index cells by the
     uniform-spacing formula instead of the search.  occupancy: resident-block
-    variant of the fast kernels (6; any other value takes the default: the
-    compiler's register choice, held to 3 blocks per SM in fast arithmetic).
+    variant of the fast kernels (4, 5 or 6 blocks per SM; 0 or 7-10 take the
+    default, 5).
     Fast arithmetic traces an interleaved float4 copy of the nodes and finds
     cells through per-axis search tables, both built for the launch; the
     results equal the drop-in's bit for bit.  Defaults to the reference

@@ -538,8 +538,8 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (sched_h) sc = *sched_h;
     if (sc.schedule != QSL_SCHED_QUEUE && sc.schedule != QSL_SCHED_STATIC)
         return fail(QSL_ERR_INVALID, "bad schedule %d", sc.schedule);
-    if (sc.occupancy != 0 && (sc.occupancy < 6 || sc.occupancy > 10))
-        return fail(QSL_ERR_INVALID, "occupancy must be 0, 6, 7, 8, 9 or 10");
+    if (sc.occupancy != 0 && (sc.occupancy < 4 || sc.occupancy > 10))
+        return fail(QSL_ERR_INVALID, "occupancy must be 0 or 4 to 10");
     if (sc.order && n > 0xffffffffLL) return fail(QSL_ERR_TOO_LARGE, "order map limits n to 2^32-1");
     const bool twist = curBx != nullptr;
     if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");

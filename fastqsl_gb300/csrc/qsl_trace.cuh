@@ -143,9 +143,63 @@ __device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h,
     return f3(scal(h, axpy(C::b6, b6, axpy(C::b5, b5, axpy(C::b4, b4, axpy(C::b3, b3, scal(C::b1, b1)))))));
 }
 
+// The fast Fehlberg step with its six stages in a rolled loop, for the
+// stretched-grid stores: their sample (three axis searches, eight corner
+// loads and the blend) inlined six times makes a loop body that does not fit
+// the instruction cache.  The sums of the stages still to come are held in
+// a shift register of five vectors: entering stage st, slot[i] is the sum
+// of stage st + i (slot[0] complete); after its sample each slot takes the
+// next one's sum plus this stage's term, so the shift costs no moves and
+// every index is static.  Coefficients from constant memory.  The same sums
+// in the same order as step_rkf45_fast except that the step multiplies each
+// stage's sum (h * sum a_ij b_j) instead of being folded into a21.
+struct FehlbergTab {
+    float a[6][5];  // a[st][i] = A(st + 1 + i, st)
+    float b[6], e[6];
+};
+static __constant__ FehlbergTab kFehlbergTab = {
+    {{Fehlberg::a21, Fehlberg::a31, Fehlberg::a41, Fehlberg::a51, Fehlberg::a61},
+     {Fehlberg::a32, Fehlberg::a42, Fehlberg::a52, Fehlberg::a62, 0.f},
+     {Fehlberg::a43, Fehlberg::a53, Fehlberg::a63, 0.f, 0.f},
+     {Fehlberg::a54, Fehlberg::a64, 0.f, 0.f, 0.f},
+     {Fehlberg::a65, 0.f, 0.f, 0.f, 0.f},
+     {0.f, 0.f, 0.f, 0.f, 0.f}},
+    {Fehlberg::b1, 0.f, Fehlberg::b3, Fehlberg::b4, Fehlberg::b5, Fehlberg::b6},
+    {Fehlberg::e1, 0.f, Fehlberg::e3, Fehlberg::e4, Fehlberg::e5, Fehlberg::e6}};
+
+template <class F>
+struct RolledStages : std::false_type {};
+template <int M>
+struct RolledStages<FieldStretchT<M>> : std::true_type {};
+
+template <class F>
+__device__ __forceinline__ float3 step_rkf45_fast_rolled(const F& f, float3 p, float h, float& err, unsigned& ns,
+                                                        float3* b_raw) {
+    const PV P = pv(p);
+    const PV zero = {make_float2(0.f, 0.f), 0.f};
+    PV slot[5] = {zero, zero, zero, zero, zero};
+    PV sol = zero, e = zero;
+    // b_raw (twist kernels): the first stage's B itself, from its own
+    // interpolation before the loop so that the loop holds one sample
+    PV b = pv(b_raw ? sample_unit_raw(f, p, *b_raw) : sample<false>(f, p, true));
+#pragma unroll 1
+    for (int st = 0; st < 6; ++st) {
+        if (st > 0) b = pv(sample<false>(f, f3(axpy(h, slot[0], P)), true));
+#pragma unroll
+        for (int i = 0; i < 4; ++i) slot[i] = axpy(kFehlbergTab.a[st][i], b, slot[i + 1]);
+        slot[4] = scal(kFehlbergTab.a[st][4], b);
+        sol = axpy(kFehlbergTab.b[st], b, sol);
+        e = axpy(kFehlbergTab.e[st], b, e);
+    }
+    err = fabsf(h) * norm_fast(f3(e));
+    ns += 6;
+    return f3(scal(h, sol));
+}
+
 template <bool EXACT, class F>
 __device__ __forceinline__ float3 step_rkf45(const F& f, float3 p, float h, float& err, unsigned& ns,
                                             float3* b_raw = nullptr) {
+    if constexpr (!EXACT && RolledStages<F>::value) return step_rkf45_fast_rolled(f, p, h, err, ns, b_raw);
     if (!EXACT) return step_rkf45_fast(f, p, h, err, ns, b_raw);
     using C = Fehlberg;
     const float3 k1 = h * sample<EXACT>(f, p, true);

@@ -358,8 +358,10 @@ int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, con
  * formed on the host, in the same arithmetic as the drop-in forms them on
  * the device, and reach the kernels as parameters.  sched may be NULL
  * (static one-line-per-thread grid) or give the schedule, order map, sample
- * counter and occupancy (6: the 6-blocks-per-SM variant of the fast kernels;
- * 0: the default).  The call allocates, stream-ordered on `stream`
+ * counter and occupancy (4, 5 or 6: the register budget for that many
+ * resident blocks per SM of the fast packed kernels, 5 by default; 6 or the
+ * default for the fast kernels on the arrays; 0 or any other value: the
+ * default).  The call allocates, stream-ordered on `stream`
  * (cudaMallocAsync, freed after the launch), a device copy of the
  * coordinates (copied from the host arrays before the call returns) and, in
  * fast arithmetic, an interleaved float4 copy of the nodes (16 B per node)
