@@ -111,6 +111,8 @@ _SIGS = {
     "qsl_qcut": (c_int, [_P] * 10 + [c_i64, _P, c_i64, c_double, _P, _P, _P]),
     "qsl_qmerge": (c_int, [_P, _P, _P, c_i64, _P, c_i64, c_int, c_int, _P, _P, _P]),
     "qsl_l1_probe": (c_int, [_P, c_i64, c_int, c_int, c_int, _P, _P]),
+    "qsl_plane_seeds": (c_int, [_P, _P, _P, _P, c_double, c_int, c_int, c_int, _P, _P, _P, _P]),
+    "qsl_tile_order": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, _P, _P]),
 }
 
 

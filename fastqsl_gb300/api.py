@@ -25,9 +25,12 @@ TRACE_I32 = ["flag_start", "flag_end", "B_flag"]
 
 
 def ptr(a):
-    """Device address of a CUDA tensor / __cuda_array_interface__ array."""
+    """Device address of a CUDA tensor / __cuda_array_interface__ array (an
+    int is taken as an address already)."""
     if a is None:
         return None
+    if isinstance(a, int):
+        return a
     if isinstance(a, torch.Tensor):
         if not a.is_cuda:
             raise ValueError("expected a CUDA tensor")
@@ -180,17 +183,50 @@ class FieldUploader:
         self._last = slot
 
 
-def alloc_trace_outputs(n, device="cuda", twist=False, status=False):
-    """The per-seed output arrays of a trace.  status=True adds int32
-    'status_start' / 'status_end' (qsl_line_status of each direction:
-    params.LINE_FACE ... LINE_REJECT_LIMIT)."""
-    out = {k: torch.zeros(n, dtype=torch.float32, device=device) for k in TRACE_F32}
-    out.update({k: torch.zeros(n, dtype=torch.int32, device=device) for k in TRACE_I32})
-    out["LineLen"] = torch.zeros(n, dtype=torch.float64, device=device)
-    out["twist"] = torch.zeros(n, dtype=torch.float64, device=device) if twist else None
+_ESIZE = {torch.float32: 4, torch.float64: 8, torch.int32: 4, torch.int64: 8, torch.uint8: 1}
+
+
+def _layout(parts):
+    """Byte offsets of parts = [(name, numel, dtype)] packed on 256-byte
+    boundaries, and the total."""
+    offs, total = {}, 0
+    for name, n, dt in parts:
+        offs[name] = total
+        total += (int(n) * _ESIZE[dt] + 255) // 256 * 256
+    return offs, max(total, 256)
+
+
+def carve(parts, device="cuda"):
+    """One device allocation split into tensors: parts = [(name, numel,
+    dtype)], each starting on a 256-byte boundary, uninitialised.  Returns
+    ({name: tensor}, backing uint8 tensor)."""
+    offs, total = _layout(parts)
+    buf = torch.empty(total, dtype=torch.uint8, device=device)
+    out = {name: buf[offs[name]:offs[name] + int(n) * _ESIZE[dt]].view(dt) for name, n, dt in parts}
+    return out, buf
+
+
+def trace_output_parts(n, twist=False, status=False, prefix=""):
+    """carve() parts of the per-seed outputs of a trace."""
+    parts = [(prefix + k, n, torch.float32) for k in TRACE_F32] + [(prefix + k, n, torch.int32) for k in TRACE_I32]
+    parts.append((prefix + "LineLen", n, torch.float64))
+    if twist:
+        parts.append((prefix + "twist", n, torch.float64))
     if status:
-        out["status_start"] = torch.zeros(n, dtype=torch.int32, device=device)
-        out["status_end"] = torch.zeros(n, dtype=torch.int32, device=device)
+        parts += [(prefix + "status_start", n, torch.int32), (prefix + "status_end", n, torch.int32)]
+    return parts
+
+
+def alloc_trace_outputs(n, device="cuda", twist=False, status=False, zero=True):
+    """The per-seed output arrays of a trace, views of one allocation
+    (zeroed by one memset unless zero=False: a trace writes every output of
+    each of its n lines).  status=True adds int32 'status_start' /
+    'status_end' (qsl_line_status of each direction: params.LINE_FACE ...
+    LINE_REJECT_LIMIT)."""
+    out, buf = carve(trace_output_parts(n, twist, status), device)
+    if zero:
+        buf.zero_()
+    out.setdefault("twist", None)
     return out
 
 
@@ -294,7 +330,7 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     return out
 
 
-def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda", plane_group=None):
+def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda", plane_group=None, stream=None):
     """A permutation of the seeds of `nplanes` stacked (n0, n1) planes that
     visits them tile by tile (ty x tx seeds, row-major inside a tile), as
     int32 on the device.  Neighbouring seeds start neighbouring field lines,
@@ -304,15 +340,29 @@ def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda", plane_group=None):
     all planes; 1 = plane by plane), so the blocks resident at a time trace
     the lines through a few thin columns of the stack rather than through
     whole planes, and share more of L1 and L2 (the benchmark cube's main
-    trace: 57.9 ms against 62.2 ms plane by plane)."""
+    trace: 57.9 ms against 62.2 ms plane by plane).  One launch
+    (qsl_tile_order) on `stream` (default: the current stream)."""
     g = int(nplanes if plane_group is None else max(1, plane_group))
-    p = torch.arange(nplanes, device=device, dtype=torch.int64).view(-1, 1, 1)
-    y = torch.arange(n0, device=device, dtype=torch.int64).view(1, -1, 1)
-    x = torch.arange(n1, device=device, dtype=torch.int64).view(1, 1, -1)
-    ntx = (n1 + tx - 1) // tx
-    nty = (n0 + ty - 1) // ty
-    key = ((((p // g) * nty + y // ty) * ntx + x // tx) * g + p % g) * (ty * tx) + (y % ty) * tx + (x % tx)
-    return torch.argsort(key.reshape(-1)).to(torch.int32)
+    out = torch.empty(int(nplanes) * int(n0) * int(n1), dtype=torch.int32, device=device)
+    _lib.check(_lib.load().qsl_tile_order(int(nplanes), int(n0), int(n1), int(ty), int(tx), g, out.data_ptr(),
+                                          stream_handle(stream)), "qsl_tile_order")
+    return out
+
+
+def plane_seeds(center, normal, u, v, spacing, n0, n1, nplanes=1, device="cuda", stream=None):
+    """Seeds of `nplanes` stacked (n0, n1) planes centred on `center`, rows
+    along v, columns along u, planes stepping along `normal`, `spacing`
+    apart (qsl_plane_seeds: one launch): seed (k, i, j) at ((center + k s
+    normal) + (i - (n0-1)/2) s v) + (j - (n1-1)/2) s u in double, rounded
+    to float32.  Returns xs, ys, zs (views of one allocation)."""
+    total = int(n0) * int(n1) * int(nplanes)
+    buf = torch.empty((3, total), dtype=torch.float32, device=device)
+    d3 = ctypes.c_double * 3
+    _lib.check(_lib.load().qsl_plane_seeds(d3(*[float(c) for c in center]), d3(*[float(c) for c in normal]),
+                                           d3(*[float(c) for c in u]), d3(*[float(c) for c in v]), float(spacing),
+                                           int(n0), int(n1), int(nplanes), buf[0].data_ptr(), buf[1].data_ptr(),
+                                           buf[2].data_ptr(), stream_handle(stream)), "qsl_plane_seeds")
+    return buf[0], buf[1], buf[2]
 
 
 SCOTT_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "B_this_x", "B_this_y", "B_this_z",
@@ -630,7 +680,7 @@ class BatchPlan:
             b.field = j["field"].handle
             b.params = j["params"]
             b.io = _io(j["xs"], j["ys"], j["zs"], j["out"])
-            b.n = int(j.get("n", j["xs"].shape[0]))
+            b.n = int(j["n"]) if "n" in j else int(j["xs"].shape[0])
             b.s_len = float(j.get("s_len", 0.25))
             b.tol_coef = float(j.get("tol_coef", 1.0))
             for c in range(3):
@@ -699,24 +749,42 @@ class QBatch:
             n = n0 * n1 * npl
             m = npl * (n0 - 2) * (n1 - 2)
             J = dict(sp=sp, n0=n0, n1=n1, npl=npl, n=n, m=m)
-            J["main"] = alloc_trace_outputs(n, device)
-            J["order"] = tile_order(npl, n0, n1, tile[0], tile[1], device) if tile else None
-            J["Q"] = torch.empty((npl, n0 - 2, n1 - 2), dtype=torch.float64, device=device)
-            J["cut"] = [torch.empty(4 * m, dtype=torch.float32, device=device) for _ in range(3)]
-            J["bz0s"] = torch.empty(m, dtype=torch.float32, device=device)
-            J["bz0e"] = torch.empty(m, dtype=torch.float32, device=device)
-            J["pix"] = torch.empty(m, dtype=torch.int64, device=device)
-            J["count"] = torch.zeros(2, dtype=torch.int64, device=device)
+            # every array of the job in one allocation, uninitialised: the
+            # kernels write each element they later read (the pseudo-line
+            # arrays up to the device count the compaction writes)
             wb = int(lib.qsl_cook_workspace_bytes(n))
-            J["work"] = torch.empty((wb + 7) // 8, dtype=torch.int64, device=device)
-            J["work_bytes"] = wb
-            J["sub"] = alloc_trace_outputs(4 * m, device)
-            J["qcut"] = torch.empty(m, dtype=torch.float64, device=device)
+            parts = (trace_output_parts(n, prefix="main.") + trace_output_parts(4 * m, prefix="sub.") +
+                     [("Q", npl * (n0 - 2) * (n1 - 2), torch.float64), ("cut0", 4 * m, torch.float32),
+                      ("cut1", 4 * m, torch.float32), ("cut2", 4 * m, torch.float32), ("bz0s", m, torch.float32),
+                      ("bz0e", m, torch.float32), ("pix", m, torch.int64), ("count", 2, torch.int64),
+                      ("work", (wb + 7) // 8, torch.int64), ("qcut", m, torch.float64)])
+            if tile:
+                parts.append(("order", n, torch.int32))
+            # the arrays only kernels touch are carried as device addresses
+            # (no tensor objects: the host cost of a small request's batch
+            # is mostly per-array bookkeeping); Q is a tensor for the caller
+            offs, total = _layout(parts)
+            J["buf"] = torch.empty(total, dtype=torch.uint8, device=device)
+            a = {name: J["buf"].data_ptr() + o for name, o in offs.items()}
+            J["main"] = {k[5:]: v for k, v in a.items() if k.startswith("main.")}
+            J["sub"] = {k[4:]: v for k, v in a.items() if k.startswith("sub.")}
+            J["main"]["twist"] = J["sub"]["twist"] = None
+            qn = npl * (n0 - 2) * (n1 - 2)
+            J["Q"] = J["buf"][offs["Q"]:offs["Q"] + 8 * qn].view(torch.float64).view(npl, n0 - 2, n1 - 2)
+            J["cut"] = [a["cut0"], a["cut1"], a["cut2"]]
+            J["bz0s"], J["bz0e"], J["pix"], J["qcut"] = a["bz0s"], a["bz0e"], a["pix"], a["qcut"]
+            J["count"] = a["count"]  # written by the compaction before anything reads it
+            J["work"], J["work_bytes"] = a["work"], wb
+            J["order"] = None
+            if tile:
+                J["order"] = a["order"]
+                _lib.check(lib.qsl_tile_order(npl, n0, n1, int(tile[0]), int(tile[1]), npl, J["order"],
+                                              stream_handle(stream)), "qsl_tile_order")
             common = dict(field=sp["field"], params=sp["params"], s_len=sp.get("s_len", 0.25),
                           tol_coef=sp.get("tol_coef", 1.0), cross_dir=sp.get("cross_dir", (0.0, 0.0, 1.0)))
             main_jobs.append(dict(common, xs=sp["xs"], ys=sp["ys"], zs=sp["zs"], out=J["main"], order=J["order"]))
             sub_jobs.append(dict(common, xs=J["cut"][0], ys=J["cut"][1], zs=J["cut"][2], out=J["sub"],
-                                 n=4 * m, n_dev=J["count"][1:2]))
+                                 n=4 * m, n_dev=J["count"] + 8))
             self.jobs.append(J)
         self.main_batch = BatchPlan(main_jobs, stream=stream)
         self.sub_batch = BatchPlan(sub_jobs, stream=stream)
@@ -762,9 +830,9 @@ class QBatch:
             jac = (1.0 / (2.0 * float(sp.get("stride", 1.0)))) ** 4.0
             _lib.check(lib.qsl_qcut(ptr(s["start_x"]), ptr(s["start_y"]), ptr(s["start_z"]), ptr(s["flag_start"]),
                                     ptr(s["end_x"]), ptr(s["end_y"]), ptr(s["end_z"]), ptr(s["flag_end"]),
-                                    ptr(J["bz0s"]), ptr(J["bz0e"]), 0, ptr(J["count"][0:1]), J["m"], jac, None,
+                                    ptr(J["bz0s"]), ptr(J["bz0e"]), 0, J["count"], J["m"], jac, None,
                                     ptr(J["qcut"]), st), "qcut")
-            _lib.check(lib.qsl_qmerge(ptr(J["pix"]), None, ptr(J["qcut"]), 0, ptr(J["count"][0:1]), J["m"],
+            _lib.check(lib.qsl_qmerge(ptr(J["pix"]), None, ptr(J["qcut"]), 0, J["count"], J["m"],
                                       J["n0"], J["n1"], None, ptr(J["Q"]), st), "qmerge")
         return [J["Q"] for J in self.jobs]
 

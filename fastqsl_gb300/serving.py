@@ -98,21 +98,12 @@ def plane_axes(normal):
 
 
 def seeds_on_device(req: QRequest, device):
-    """Seeds of the request's planes, built on the device (no host copy):
-    plane k, row i, column j at center + (j - (n1-1)/2) s u + (i - (n0-1)/2) s v
-    + k s n."""
+    """Seeds of the request's planes, built on the device in one launch (no
+    host copy): plane k, row i, column j at center + (j - (n1-1)/2) s u +
+    (i - (n0-1)/2) s v + k s n (api.plane_seeds)."""
     n, u, v = plane_axes(req.normal)
-    s = float(req.spacing)
-    c = torch.tensor(req.center, dtype=torch.float64, device=device)
-    j = (torch.arange(req.n1, dtype=torch.float64, device=device) - (req.n1 - 1) / 2.0) * s
-    i = (torch.arange(req.n0, dtype=torch.float64, device=device) - (req.n0 - 1) / 2.0) * s
-    k = torch.arange(req.nplanes, dtype=torch.float64, device=device) * s
-    U = torch.tensor(u, dtype=torch.float64, device=device)
-    V = torch.tensor(v, dtype=torch.float64, device=device)
-    N = torch.tensor(n, dtype=torch.float64, device=device)
-    pts = (c.view(1, 1, 1, 3) + k.view(-1, 1, 1, 1) * N + i.view(1, -1, 1, 1) * V + j.view(1, 1, -1, 1) * U)
-    pts = pts.reshape(-1, 3).to(torch.float32)
-    return pts[:, 0].contiguous(), pts[:, 1].contiguous(), pts[:, 2].contiguous(), tuple(float(x) for x in n)
+    xs, ys, zs = api.plane_seeds(req.center, n, u, v, req.spacing, req.n0, req.n1, req.nplanes, device=device)
+    return xs, ys, zs, tuple(float(x) for x in n)
 
 
 class _Flight:
@@ -143,8 +134,11 @@ class QServer:
 
     # size classes: (upper bound on seeds, requests per batch, batches in flight)
     # (larger requests fill the GPU alone: batching them only makes each
-    # wait for its batch mates)
-    CLASSES = ((1.5e5, 32, 2), (1.2e6, 2, 3), (float("inf"), 1, 3))
+    # wait for its batch mates; the smallest class's batches are set up on
+    # the host one request after another, so a request waits for its batch
+    # mates' set-up: 8 per batch with 4 in flight gave the lowest p99 and the
+    # highest saturated rate of the sizes measured, 2-16 per batch)
+    CLASSES = ((1.5e5, 8, 4), (1.2e6, 2, 3), (float("inf"), 1, 3))
 
     def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
                  tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=6,

@@ -523,6 +523,29 @@ int qsl_qmerge(const int64_t *pix, const float *Qcut32, const double *Qcut64, in
                const unsigned long long *count_dev, int64_t max_count, int n0, int n1, float *Qfinal32,
                double *Qfinal64, qsl_stream_t stream);
 
+/* Seed grid of nplanes stacked (n0, n1) planes (no reference counterpart:
+ * the notebooks build their seed planes with cupy.linspace / meshgrid on the
+ * host side of the kernel call, demo/Q_RKF45CuPy.ipynb cell 7).  Seed
+ * q = (k * n0 + i) * n1 + j, written as float32 to xs, ys, zs, is
+ *   ((center + (k s) normal) + ((i - (n0-1)/2) s) v) + ((j - (n1-1)/2) s) u
+ * with s = spacing, each product and sum rounded in double on its own, then
+ * rounded to float (the same values as that expression evaluated one
+ * array operation at a time in double).  center, normal, u, v: 3 doubles on
+ * the HOST.  One launch on `stream`. */
+int qsl_plane_seeds(const double *center_h, const double *normal_h, const double *u_h, const double *v_h,
+                    double spacing, int n0, int n1, int nplanes, float *xs, float *ys, float *zs,
+                    qsl_stream_t stream);
+
+/* Tile visiting order of nplanes stacked (n0, n1) seed planes (seed index
+ * (p * n0 + y) * n1 + x), the `order` map of qsl_sched / qsl_batch_job:
+ * order[k] = the seed visited k-th when the seeds are sorted by (plane
+ * group, y / ty, x / tx, plane within the group, y % ty, x % tx); groups of
+ * plane_group consecutive planes (<= 0 or >= nplanes: one group of all
+ * planes).  Tiles at the far edges are smaller.  nplanes * n0 * n1 <= 2^32.
+ * One launch on `stream`. */
+int qsl_tile_order(int nplanes, int n0, int n1, int ty, int tx, int plane_group, uint32_t *order,
+                   qsl_stream_t stream);
+
 /* Measurement helper with no reference counterpart: the L1 ceiling of the
  * tracers' 16-byte field gathers.  Launches `blocks` blocks of 128 threads;
  * each thread issues 8 * iters 16-byte read-only loads from `buf`
