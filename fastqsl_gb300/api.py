@@ -22,14 +22,13 @@ TRACE_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z",
              "B_this_x", "B_this_y", "B_this_z", "B_start_x", "B_start_y", "B_start_z",
              "B_end_x", "B_end_y", "B_end_z"]
 TRACE_I32 = ["flag_start", "flag_end", "B_flag"]
+_TRACE_OUT = TRACE_F32 + TRACE_I32 + ["LineLen"]
 
 
 def ptr(a):
     """Device address of a CUDA tensor / __cuda_array_interface__ array (an
     int is taken as an address already)."""
-    if a is None:
-        return None
-    if isinstance(a, int):
+    if a is None or type(a) is int:
         return a
     if isinstance(a, torch.Tensor):
         if not a.is_cuda:
@@ -349,6 +348,9 @@ def tile_order(nplanes, n0, n1, ty=16, tx=16, device="cuda", plane_group=None, s
     return out
 
 
+_D3 = ctypes.c_double * 3
+
+
 def plane_seeds(center, normal, u, v, spacing, n0, n1, nplanes=1, device="cuda", stream=None):
     """Seeds of `nplanes` stacked (n0, n1) planes centred on `center`, rows
     along v, columns along u, planes stepping along `normal`, `spacing`
@@ -357,12 +359,11 @@ def plane_seeds(center, normal, u, v, spacing, n0, n1, nplanes=1, device="cuda",
     to float32.  Returns xs, ys, zs (views of one allocation)."""
     total = int(n0) * int(n1) * int(nplanes)
     buf = torch.empty((3, total), dtype=torch.float32, device=device)
-    d3 = ctypes.c_double * 3
-    _lib.check(_lib.load().qsl_plane_seeds(d3(*[float(c) for c in center]), d3(*[float(c) for c in normal]),
-                                           d3(*[float(c) for c in u]), d3(*[float(c) for c in v]), float(spacing),
-                                           int(n0), int(n1), int(nplanes), buf[0].data_ptr(), buf[1].data_ptr(),
-                                           buf[2].data_ptr(), stream_handle(stream)), "qsl_plane_seeds")
-    return buf[0], buf[1], buf[2]
+    base = buf.data_ptr()
+    _lib.check(_lib.load().qsl_plane_seeds(_D3(*center), _D3(*normal), _D3(*u), _D3(*v), float(spacing), int(n0),
+                                           int(n1), int(nplanes), base, base + 4 * total, base + 8 * total,
+                                           stream_handle(stream)), "qsl_plane_seeds")
+    return buf.unbind(0)
 
 
 SCOTT_F32 = ["start_x", "start_y", "start_z", "end_x", "end_y", "end_z", "B_this_x", "B_this_y", "B_this_z",
@@ -765,9 +766,10 @@ class QBatch:
             # is mostly per-array bookkeeping); Q is a tensor for the caller
             offs, total = _layout(parts)
             J["buf"] = torch.empty(total, dtype=torch.uint8, device=device)
-            a = {name: J["buf"].data_ptr() + o for name, o in offs.items()}
-            J["main"] = {k[5:]: v for k, v in a.items() if k.startswith("main.")}
-            J["sub"] = {k[4:]: v for k, v in a.items() if k.startswith("sub.")}
+            base = J["buf"].data_ptr()
+            a = {name: base + o for name, o in offs.items()}
+            J["main"] = {k: a["main." + k] for k in _TRACE_OUT}
+            J["sub"] = {k: a["sub." + k] for k in _TRACE_OUT}
             J["main"]["twist"] = J["sub"]["twist"] = None
             qn = npl * (n0 - 2) * (n1 - 2)
             J["Q"] = J["buf"][offs["Q"]:offs["Q"] + 8 * qn].view(torch.float64).view(npl, n0 - 2, n1 - 2)

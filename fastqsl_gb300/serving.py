@@ -35,6 +35,7 @@ from __future__ import annotations
 
 import collections
 import gc
+import math
 import time
 from dataclasses import dataclass, field as dc_field
 
@@ -87,23 +88,35 @@ def request_bytes(req: QRequest) -> int:
     return int(n * (72 + 8 + 4 + 12 + 4) + m * (4 * (72 + 8 + 12) + 8 + 8 + 8 + 8) + (n // 1024 + 1) * 12 + 4096)
 
 
+def _cross(a, b):
+    return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+
+def _unit(a):
+    r = math.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2])
+    return (a[0] / r, a[1] / r, a[2] / r)
+
+
 def plane_axes(normal):
-    n = np.asarray(normal, np.float64)
-    n = n / np.linalg.norm(n)
-    e = np.eye(3)[int(np.argmin(np.abs(n)))]
-    u = np.cross(n, e)
-    u /= np.linalg.norm(u)
-    v = np.cross(n, u)
-    return n, u, v
+    """An orthonormal frame (n, u, v) of a plane with normal `normal`: u
+    across the coordinate axis least aligned with n, v = n x u (plain
+    floats: called once per request on the serving path)."""
+    n = _unit(tuple(float(c) for c in normal))
+    k = min(range(3), key=lambda i: abs(n[i]))
+    e = tuple(1.0 if i == k else 0.0 for i in range(3))
+    u = _unit(_cross(n, e))
+    return n, u, _cross(n, u)
 
 
-def seeds_on_device(req: QRequest, device):
+def seeds_on_device(req: QRequest, device, stream=None):
     """Seeds of the request's planes, built on the device in one launch (no
     host copy): plane k, row i, column j at center + (j - (n1-1)/2) s u +
-    (i - (n0-1)/2) s v + k s n (api.plane_seeds)."""
+    (i - (n0-1)/2) s v + k s n (api.plane_seeds), on `stream` (default:
+    the current stream)."""
     n, u, v = plane_axes(req.normal)
-    xs, ys, zs = api.plane_seeds(req.center, n, u, v, req.spacing, req.n0, req.n1, req.nplanes, device=device)
-    return xs, ys, zs, tuple(float(x) for x in n)
+    xs, ys, zs = api.plane_seeds(req.center, n, u, v, req.spacing, req.n0, req.n1, req.nplanes, device=device,
+                                 stream=stream)
+    return xs, ys, zs, n
 
 
 class _Flight:
@@ -266,10 +279,14 @@ class QServer:
             fl.stream.wait_event(ev)
         with torch.cuda.stream(fl.stream):
             qs = fl.qb.run_post(stream=fl.stream)
+            # one pinned buffer for the batch's Q maps (each result a view)
+            h = torch.empty(sum(q.numel() for q in qs), dtype=torch.float64, pin_memory=True)
+            o = 0
             for q in qs:
-                h = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
-                h.copy_(q, non_blocking=True)
-                fl.hosts.append(h)
+                hv = h[o:o + q.numel()].view(q.shape)
+                hv.copy_(q, non_blocking=True)
+                fl.hosts.append(hv)
+                o += q.numel()
             fl.event = torch.cuda.Event()
             fl.event.record(fl.stream)
 
@@ -298,7 +315,7 @@ class QServer:
             specs = []
             for r in group:
                 r.t_admit = t
-                xs, ys, zs, nrm = seeds_on_device(r, self.device)
+                xs, ys, zs, nrm = seeds_on_device(r, self.device, st)
                 prm = absolute_rkf45(tol=r.tol, h_min=self.h_min, h_max=self.h_max)
                 specs.append(dict(field=self.fields[r.field], xs=xs, ys=ys, zs=zs, n0=r.n0, n1=r.n1,
                                   nplanes=r.nplanes, params=prm, s_len=self.s_len, stride=r.spacing, cross_dir=nrm))

@@ -102,3 +102,22 @@ def test_new_entries_validate_without_gpu(lib):
     assert lib.qsl_batch_run_window(None, ctypes.byref(info), None, 0, -1, 0, 0, None) != 0
     assert lib.qsl_batch_run_window(ctypes.c_void_p(256), ctypes.byref(info), None, 0, -1, 0, 5, None) == -1
     assert b"occupancy" in lib.qsl_last_error()
+
+
+def test_seed_geometry_entries_validate_without_gpu(lib):
+    """qsl_plane_seeds and qsl_tile_order reject nulls, non-positive sizes
+    and order maps beyond 2^32 seeds before any CUDA call."""
+    import ctypes
+    d3 = ctypes.c_double * 3
+    dummy = ctypes.c_void_p(256)
+    v = d3(0.0, 0.0, 1.0)
+    assert lib.qsl_plane_seeds(None, v, v, v, 1.0, 4, 4, 1, dummy, dummy, dummy, None) == -1
+    assert b"null" in lib.qsl_last_error()
+    assert lib.qsl_plane_seeds(v, v, v, v, 1.0, 0, 4, 1, dummy, dummy, dummy, None) == -1
+    assert b"positive" in lib.qsl_last_error()
+    assert lib.qsl_plane_seeds(v, v, v, v, 1.0, 4, 4, 1, dummy, None, dummy, None) == -1
+    assert lib.qsl_tile_order(1, 4, 4, 8, 8, 0, None, None) == -1
+    assert b"null" in lib.qsl_last_error()
+    assert lib.qsl_tile_order(1, 4, 4, 0, 8, 0, dummy, None) == -1
+    assert lib.qsl_tile_order(2, 65536, 65536, 8, 8, 0, dummy, None) != 0
+    assert b"2^32" in lib.qsl_last_error()
