@@ -553,7 +553,7 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     const int64_t ncoord = (int64_t)nx + ny + nz;
     const size_t coord_bytes = ((size_t)ncoord * sizeof(float) + 255) / 256 * 256;
     const size_t bytes = coord_bytes + (packed_path ? (size_t)(nodes + tcells) * sizeof(float4) +
-                                                          (size_t)tcells * STRETCH_BINS_PER_CELL * sizeof(int2)
+                                                          (size_t)tcells * STRETCH_BINS_PER_CELL * 2 * sizeof(float4)
                                                     : 0);
     char* buf = nullptr;
     QSL_CHECK_CUDA(cudaMallocAsync((void**)&buf, bytes, st), "launch buffer allocation");
@@ -606,11 +606,11 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     }
     // fast arithmetic: the nodes interleaved into a float4 copy for the
     // launch (one 16-byte load per corner; the same values), followed, for
-    // the search, by its tables (a 16-byte record per cell, an int2 range per
-    // bin); the uniform formula needs none
+    // the search, by its tables (a 16-byte record per cell, two 16-byte
+    // records per bin); the uniform formula needs none
     float4* b4 = reinterpret_cast<float4*>(buf + coord_bytes);
     float4* srec = uni ? nullptr : b4 + nodes;
-    int2* sbin = uni ? nullptr : reinterpret_cast<int2*>(srec + cells);
+    float4* sbin = uni ? nullptr : srec + cells;
     e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
     if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {

@@ -29,10 +29,18 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
 //    value up to nb: 4e-7 nb bins covers it), in double, each the largest
 //    j <= n-2 with a[j] below the edge (0 if none).  A coordinate the
 //    kernel puts in bin b lies within those edges, so its interval is in the
-//    range, on axes of any length.  (Bins holding the cell record of a
-//    one-interval range themselves, to save the dependent record load,
-//    measured slower: 10.0 against 8.7 ms on the search workload, the
-//    lanes of a warp diverging between the two cases.)
+//    range [lo, hi], on axes of any length.  A range of one or two intervals
+//    (every bin unless cells are under ~1/4 of the mean width) is stored as
+//    both intervals' records and the node between them, 32 bytes:
+//      {a[lo+1] (+inf for one interval), rec(lo).x, .y, .z}
+//      {rec(hi).x, .y, .z, 0}
+//    so the lookup is two independent loads and a select; a wider range as
+//      {0, lo, hi (int bits), 0} {0, 0, 0, 1 (int bits)}
+//    for a bisection over [lo, hi] and the cell record.  (The earlier form,
+//    an int2 range per bin and always the dependent record load: 8.05-8.11
+//    against 7.63-7.66 ms on the search workload; bins holding one record
+//    only, with a branch for the others: 10.0 ms, the lanes of a warp
+//    diverging between the two cases.)
 __device__ __forceinline__ int stretch_cell_below(double c, int n, const float* __restrict__ a) {
     int lo = 0, hi = n - 2;  // largest j in [0, n-2] with a[j] < c, else 0
     while (lo < hi) {
@@ -45,7 +53,7 @@ __device__ __forceinline__ int stretch_cell_below(double c, int n, const float* 
 
 __global__ void k_stretch_tables(const float* __restrict__ ax, const float* __restrict__ ay,
                                  const float* __restrict__ az, Dims d, float4* __restrict__ srec,
-                                 int2* __restrict__ sbin) {
+                                 float4* __restrict__ sbin) {
     const int cells = (d.nx - 1) + (d.ny - 1) + (d.nz - 1);
     const int bins = STRETCH_BINS_PER_CELL * cells;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cells + bins; t += gridDim.x * blockDim.x) {
@@ -67,13 +75,28 @@ __global__ void k_stretch_tables(const float* __restrict__ ax, const float* __re
             const double wid = 0.01 + 4e-7 * (double)nb;
             const int lo = stretch_cell_below(a0 + (b - wid) * w, n, a);
             const int hi = stretch_cell_below(a0 + (b + 1 + wid) * w, n, a);
-            sbin[t - cells] = make_int2(lo, hi < lo ? lo : hi);
+            const int h = hi < lo ? lo : hi;
+            float4* out = sbin + 2 * (t - cells);
+            if (h <= lo + 1) {
+                auto rec_of = [&](int j) {
+                    const int i = stretch_bisect(__ldg(a + j + 1), n, a);
+                    const float ai = __ldg(a + i);
+                    return make_float4(ai, __ldg(a + i + 1) - ai, __int_as_float(i), 0.f);
+                };
+                const float4 r0 = rec_of(lo), r1 = rec_of(h);
+                const float s = h > lo ? __ldg(a + lo + 1) : __int_as_float(0x7f800000);
+                out[0] = make_float4(s, r0.x, r0.y, r0.z);
+                out[1] = make_float4(r1.x, r1.y, r1.z, 0.f);
+            } else {
+                out[0] = make_float4(0.f, __int_as_float(lo), __int_as_float(h), 0.f);
+                out[1] = make_float4(0.f, 0.f, 0.f, __int_as_float(1));
+            }
         }
     }
 }
 
 cudaError_t launch_stretch_tables(const float* ax, const float* ay, const float* az, Dims d, float4* srec,
-                                  int2* sbin, cudaStream_t st) {
+                                  float4* sbin, cudaStream_t st) {
     const long long total = (long long)(1 + STRETCH_BINS_PER_CELL) * ((d.nx - 1) + (d.ny - 1) + (d.nz - 1));
     long long g = (total + 255) / 256;
     if (g > 4096) g = 4096;

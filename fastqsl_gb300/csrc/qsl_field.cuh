@@ -230,12 +230,14 @@ struct FieldStretchT {
     //   srec[j]  the cell the reference's search gives for any coordinate in
     //            (a[j], a[j+1]] and its first coordinate and width:
     //            {a[i], a[i+1] - a[i], i as int bits, 0}
-    //   sbin[b]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins over [a[0],
-    //            a[n-1]] per axis: the lowest and highest cell a coordinate
-    //            of the bin (widened by 1 % of a bin plus 4e-7 nb bins, the
-    //            float rounding of the bin index) can lie in
+    //   sbin[2b], sbin[2b+1]  STRETCH_BINS_PER_CELL * (n - 1) uniform bins
+    //            over [a[0], a[n-1]] per axis, each covering the cells a
+    //            coordinate of the bin (widened by 1 % of a bin plus 4e-7 nb
+    //            bins, the float rounding of the bin index) can lie in: for
+    //            one or two cells their srec records and the node between
+    //            them, else the range (k_stretch_tables)
     const float4* srec;
-    const int2* sbin;
+    const float4* sbin;
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (M == 1 || M == 2) {
@@ -695,14 +697,15 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
 }
 
 // The reference search's cell for c through the tables of a packed store
-// (FieldStretchP): the bin of c gives the range of cells c can lie in
-// (usually one, else a few), a bisection over that range the cell j with
-// a[j] < c <= a[j+1] (or the range's low end), and srec[j] the cell the
-// reference's search returns for every coordinate of that interval (its
-// comparisons are all of the form c > a[m]), with that cell's first
-// coordinate and width.  The same cell, coordinate and width as
-// stretch_bisect followed by the two coordinate loads, for c clamped as
-// stretch_locate clamps it.
+// (FieldStretchP): srec[j] is the cell the reference's search returns for
+// every coordinate of the interval (a[j], a[j+1]] (its comparisons are all
+// of the form c > a[m]), with that cell's first coordinate and width.  The
+// bin of c covers the intervals c can lie in: when they are one or two the
+// bin holds both records and the node between them (two independent loads,
+// c > node picks the upper one), else their range, bisected to the interval
+// j with a[j] < c <= a[j+1] (or the range's low end) before srec[j] is
+// read.  The same cell, coordinate and width as stretch_bisect followed by
+// the two coordinate loads, for c clamped as stretch_locate clamps it.
 template <int M>
 __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, float c, float a0, float binv,
                                              float& ai, float& di) {
@@ -712,8 +715,16 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, f
     const int nb = STRETCH_BINS_PER_CELL * (n - 1);
     int b = __float2int_rz((c - a0) * binv);
     b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-    const int2 range = __ldg(f.sbin + STRETCH_BINS_PER_CELL * c0 + b);
-    int lo = range.x, hi = range.y;
+    const float4* sb = f.sbin + 2 * (STRETCH_BINS_PER_CELL * c0 + b);
+    const float4 A = __ldg(sb), B = __ldg(sb + 1);
+    if (__float_as_int(B.w) == 0) {
+        // one or two intervals: the records of both and the node between
+        const bool up = c > A.x;
+        ai = up ? B.x : A.y;
+        di = up ? B.y : A.z;
+        return up ? __float_as_int(B.z) : __float_as_int(A.w);
+    }
+    int lo = __float_as_int(A.y), hi = __float_as_int(A.z);
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (c > __ldg(a + mid)) lo = mid;

@@ -365,7 +365,7 @@ int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, con
  * (cudaMallocAsync, freed after the launch), a device copy of the
  * coordinates (copied from the host arrays before the call returns) and, in
  * fast arithmetic, an interleaved float4 copy of the nodes (16 B per node)
- * and, for the search, per-axis search tables (48 B per cell of each axis);
+ * and, for the search, per-axis search tables (144 B per cell of each axis);
  * the outputs equal the drop-in's (fast arithmetic) bit for bit. */
 int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz,
                       const float *x_arr_h, const float *y_arr_h, const float *z_arr_h, int uni,

@@ -1,6 +1,8 @@
 """The stretched tracer's search tables (field_store.cu: k_stretch_tables;
-qsl_field.cuh: stretch_table) restated in float32 on the CPU against the
-reference's bisection (GetIndexBiSearch, TraceBlineAdaptiveStretch.cu:42-64):
+qsl_field.cuh: stretch_table; bins of one or two intervals as two records
+and the node between them, wider bins as ranges) restated in float32 on the
+CPU against the reference's bisection (GetIndexBiSearch,
+TraceBlineAdaptiveStretch.cu:42-64):
 for every coordinate the tables give the cell the bisection gives, including
 its answers that are not the containing cell (the cell below near the top of
 its last interval, the cell above for the first interval of a 4-node axis).
@@ -56,15 +58,27 @@ def build_tables(a):
     bins = []
     for b in range(nb):
         lo, hi = cell_below(a0 + (b - wid) * w, a), cell_below(a0 + (b + 1 + wid) * w, a)
-        bins.append((lo, max(lo, hi)))
+        hi = max(lo, hi)
+        # the device's encoding: one or two intervals as their two records
+        # and the node between them (+inf for one), wider ranges as a range
+        if hi <= lo + 1:
+            bins.append(("pair", f32(a[lo + 1]) if hi > lo else f32(np.inf), rec[lo], rec[hi]))
+        else:
+            bins.append(("range", lo, hi))
     binv = f32(f32(nb) / f32(a[-1] - a[0]))
     return rec, bins, binv
 
 
-def table_lookup(c, a, rec, bins, binv):
+def table_lookup(c, a, rec, bins, binv, seen=None):
     nb = len(bins)
     b = int(np.trunc(f32(f32(c - a[0]) * binv)))
-    lo, hi = bins[min(max(b, 0), nb - 1)]
+    entry = bins[min(max(b, 0), nb - 1)]
+    if seen is not None:
+        seen.add(entry[0])
+    if entry[0] == "pair":
+        _, node, r_lo, r_hi = entry
+        return r_hi if c > node else r_lo
+    _, lo, hi = entry
     while lo < hi:
         mid = (lo + hi + 1) >> 1
         if c > a[mid]:
@@ -85,6 +99,7 @@ def axes(rng):
 def test_tables_give_the_reference_search_cell(seed):
     rng = np.random.default_rng(seed)
     checked = 0
+    seen = set()
     for a in axes(rng):
         a = np.unique(a)
         if len(a) < 2:
@@ -97,9 +112,10 @@ def test_tables_give_the_reference_search_cell(seed):
             c = f32(c)
             c = c if c > a[0] else clo          # the kernel's clamp (stretch_locate)
             c = c if c < a[-1] else chi
-            assert table_lookup(c, a, rec, bins, binv) == reference_bisect(c, a), (len(a), float(c))
+            assert table_lookup(c, a, rec, bins, binv, seen) == reference_bisect(c, a), (len(a), float(c))
             checked += 1
     assert checked > 10000
+    assert seen == {"pair", "range"}  # both encodings are exercised (the geometric axes have wide bins)
 
 
 def test_four_node_axis_takes_the_cell_above():
