@@ -37,7 +37,7 @@ __device__ __forceinline__ void batch_line(const TraceJob<F>& J, long long line,
     const TraceOut& o = J.o;
     while (true) {
         if (!lane_step<false, TWIST>(f, J, L, len_lim, tw_on, ns)) continue;
-        if (L.dir > 0) {
+        if (L.dsign == 0) {
             const float3 be = sample_endpoint<false>(f, L.out);
             ns += 1;
             o.end_x[i] = L.out.x; o.end_y[i] = L.out.y; o.end_z[i] = L.out.z;

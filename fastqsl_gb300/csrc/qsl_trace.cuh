@@ -103,7 +103,9 @@ struct Fehlberg {
 
 // One Fehlberg step (RKF45, TraceBlineAdaptive.cu:215-254): returns the
 // 5th-order increment (the reference adds it to P0 in one rounding) and the
-// error-estimate norm.
+// error estimate: its norm in exact arithmetic; in fast arithmetic its
+// square, h^2 |e|^2 (the fast controller works with log2 of it, so no square
+// root is taken).
 // Vector as an (x, y) pair for the packed f32x2 pipe plus a scalar z.
 struct PV {
     float2 xy;
@@ -120,9 +122,9 @@ __device__ __forceinline__ PV scal(float a, PV x) { return {__fmul2_rn(make_floa
 // Fast-arithmetic Fehlberg step: the same stages on the unit field b with
 // the step folded in once per stage (p + h * sum a_ij b_j), combinations on
 // packed (x, y) pairs.  Differs from the reference's rounding sequence only
-// in rounding.
+// in rounding.  err2: the squared error estimate h^2 |e|^2.
 template <class F>
-__device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h, float& err, unsigned& ns,
+__device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h, float& err2, unsigned& ns,
                                                  float3* b_raw = nullptr) {
     using C = Fehlberg;
     const PV P = pv(p);
@@ -138,7 +140,7 @@ __device__ __forceinline__ float3 step_rkf45_fast(const F& f, float3 p, float h,
     c = axpy(C::a65, b5, axpy(C::a64, b4, axpy(C::a63, b3, axpy(C::a62, b2, scal(C::a61, b1)))));
     const PV b6 = pv(sample<false>(f, f3(axpy(h, c, P)), true));
     const PV e = axpy(C::e6, b6, axpy(C::e5, b5, axpy(C::e4, b4, axpy(C::e3, b3, scal(C::e1, b1)))));
-    err = fabsf(h) * norm_fast(f3(e));
+    err2 = (h * h) * fmaf(e.xy.x, e.xy.x, fmaf(e.xy.y, e.xy.y, e.z * e.z));
     ns += 6;
     return f3(scal(h, axpy(C::b6, b6, axpy(C::b5, b5, axpy(C::b4, b4, axpy(C::b3, b3, scal(C::b1, b1)))))));
 }
@@ -173,7 +175,7 @@ template <int M>
 struct RolledStages<FieldStretchT<M>> : std::true_type {};
 
 template <class F>
-__device__ __forceinline__ float3 step_rkf45_fast_rolled(const F& f, float3 p, float h, float& err, unsigned& ns,
+__device__ __forceinline__ float3 step_rkf45_fast_rolled(const F& f, float3 p, float h, float& err2, unsigned& ns,
                                                         float3* b_raw) {
     const PV P = pv(p);
     const PV zero = {make_float2(0.f, 0.f), 0.f};
@@ -191,7 +193,7 @@ __device__ __forceinline__ float3 step_rkf45_fast_rolled(const F& f, float3 p, f
         sol = axpy(kFehlbergTab.b[st], b, sol);
         e = axpy(kFehlbergTab.e[st], b, e);
     }
-    err = fabsf(h) * norm_fast(f3(e));
+    err2 = (h * h) * fmaf(e.xy.x, e.xy.x, fmaf(e.xy.y, e.xy.y, e.z * e.z));
     ns += 6;
     return f3(scal(h, sol));
 }
@@ -400,13 +402,13 @@ struct Lane {
     float3 p;      // current point
     float3 pc;     // Kahan compensation of p (fast arithmetic)
     float h;       // current step
-    float tol;     // local error tolerance
+    float tol;     // local error tolerance (fast arithmetic: 0.2 log2(tol / 11.09), the controller's form)
     len_t len;     // accumulated length
     float lc;      // Kahan compensation of len (fast arithmetic)
     double tw;     // accumulated twist
     int steps;     // accepted steps
     int rej;       // trial steps rejected in a row
-    int dir;       // +1 forward, -1 backward
+    unsigned dsign;  // sign bit of the step: 0 forward, 0x80000000 backward
     long long line;
     float3 out;    // footpoint of this direction when finished
     int flag;      // reference flag; bits 8.. hold the qsl_line_status when finished
@@ -434,7 +436,7 @@ template <bool EXACT, class F>
 __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, long long line, int dir,
                                            float s_len, float tol_coef, const float3 nrm, unsigned& ns) {
     L.line = line;
-    L.dir = dir;
+    L.dsign = dir > 0 ? 0u : 0x80000000u;
     L.p = v3(__ldg(J.inp_x + line), __ldg(J.inp_y + line), __ldg(J.inp_z + line));
     L.pc = v3(0.f, 0.f, 0.f);
     L.h = s_len;
@@ -459,16 +461,111 @@ __device__ __forceinline__ void lane_begin(const F& f, const TraceJob<F>& J, Lan
             tol = (float)J.prm.tol;
         }
         L.tol = tol * tol_coef;
+        // the fast controller's power (tol / (11.09 err))^0.2 as
+        // 2^(0.2 log2(tol / 11.09) - 0.1 log2(err^2)): the first term once
+        if (!EXACT) L.tol = 0.2f * log2f(L.tol * (float)(1.0 / 11.09));
     }
 }
 
-// 2^x by the hardware approximation (ex2.approx.ftz.f32): the fast step
-// controller only needs the next step size to a few digits.
+// 2^x and log2 x by the hardware approximations (ex2/lg2.approx.ftz.f32):
+// the fast step controller only needs the next step size to a few digits.
 __device__ __forceinline__ float ex2_approx(float x) {
     float r;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// a - b on the packed f32x2 pipe
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t"
+        ".reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t"
+        "}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+// The limits checked before a trial step: true (direction finished, L.out
+// and L.flag set) when the length or step limit stops it.
+template <bool EXACT, class F>
+__device__ __forceinline__ bool lane_limits(const TraceJob<F>& J, Lane<EXACT>& L,
+                                            typename Lane<EXACT>::len_t len_lim) {
+    const bool more_steps = EXACT ? ((long long)L.steps < J.prm.max_steps) : (L.steps < J.lim.max_steps);
+    const bool more_len = L.len < len_lim;
+    if (!(more_len & more_steps)) {
+        L.out = L.p;
+        L.flag = pack_flag(0, more_len ? QSL_LINE_MAX_STEPS : QSL_LINE_MAX_LENGTH);
+        return true;
+    }
+    return false;
+}
+
+// the signed step: h with the direction's sign bit (h x +-1 exactly)
+template <bool EXACT>
+__device__ __forceinline__ float lane_hd(const Lane<EXACT>& L) {
+    return __int_as_float(__float_as_int(L.h) ^ (int)L.dsign);
+}
+
+// The RKF45 step controller after a trial step with error estimate err (its
+// norm in exact arithmetic, h^2 |e|^2 in fast): 0 = accepted (L.h is the
+// next step), 1 = rejected (L.h shrunk; try again), 2 = rejected and the
+// direction finished by the reject limit.
+template <bool EXACT, class F>
+__device__ __forceinline__ int lane_control(const TraceJob<F>& J, Lane<EXACT>& L, float err) {
+    const qsl_trace_params& pr = J.prm;
+    float scale;
+    if (EXACT) {
+        scale = pow_cr((float)((double)(L.tol / err) / 11.09), 0.2f);
+        if ((double)scale < 0.618) {
+            L.h = (float)((double)L.h * pr.reject_factor);
+            if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
+                L.out = L.p;
+                L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
+                return 2;
+            }
+            return 1;
+        }
+    } else {
+        // only the next step size depends on this power: hardware
+        // log2 / exp2 are accurate enough (err is h^2 |e|^2 here, L.tol
+        // 0.2 log2(tol / 11.09))
+        scale = ex2_approx(fmaf(-0.1f, lg2_approx(err), L.tol));
+        if (scale < 0.618f) {
+            L.h = L.h * J.lim.reject;
+            if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
+                L.out = L.p;
+                L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
+                return 2;
+            }
+            return 1;
+        }
+    }
+    L.rej = 0;
+    float h = L.h * scale;
+    if (EXACT) {
+        if ((double)h > pr.h_max) h = (float)pr.h_max;
+        if ((double)h < pr.h_min) h = (float)pr.h_min;
+    } else {
+        if (h > J.lim.h_max) h = J.lim.h_max;  // a NaN step stays NaN, as above
+        if (h < J.lim.h_min) h = J.lim.h_min;
+    }
+    L.h = h;
+    return 0;
+}
+
+template <bool EXACT, bool TWIST, class F>
+__device__ __forceinline__ bool lane_move(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, float3 inc,
+                                          float3 b_at_p, bool tw_on, unsigned& ns);
 
 // One trial step of the current direction.  Returns true when the direction
 // is finished (left the box, or stopped by the length / step limit) with
@@ -478,73 +575,52 @@ template <bool EXACT, bool TWIST, class F>
 __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane<EXACT>& L,
                                           typename Lane<EXACT>::len_t len_lim, bool tw_on,
                                           unsigned& ns) {
-    const qsl_trace_params& pr = J.prm;
-    const bool more_steps = EXACT ? ((long long)L.steps < pr.max_steps) : (L.steps < J.lim.max_steps);
-    const bool more_len = L.len < len_lim;
-    if (!(more_len & more_steps)) {
-        L.out = L.p;
-        L.flag = pack_flag(0, more_len ? QSL_LINE_MAX_STEPS : QSL_LINE_MAX_LENGTH);
-        return true;
-    }
-    const float hd = L.h * (float)L.dir;
+    if (lane_limits(J, L, len_lim)) return true;
+    const float hd = lane_hd(L);
     float3 inc;
     // fast twist kernels: B at L.p comes out of the step's first sample
     float3 b_at_p = v3(0.f, 0.f, 0.f);
     float3* const want_b = (!EXACT && TWIST && tw_on) ? &b_at_p : nullptr;
-    if (pr.integrator == QSL_RKF45) {
+    if (J.prm.integrator == QSL_RKF45) {
         float err;
         inc = step_rkf45<EXACT>(f, L.p, hd, err, ns, want_b);
-        float scale;
-        if (EXACT) {
-            scale = pow_cr((float)((double)(L.tol / err) / 11.09), 0.2f);
-            if ((double)scale < 0.618) {
-                L.h = (float)((double)L.h * pr.reject_factor);
-                if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
-                    L.out = L.p;
-                    L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
-                    return true;
-                }
-                return false;
-            }
-        } else {
-            // only the next step size depends on this power: hardware
-            // log2 / exp2 are accurate enough
-            scale = ex2_approx(0.2f * __log2f(__fdividef(L.tol, err) * (float)(1.0 / 11.09)));
-            if (scale < 0.618f) {
-                L.h = L.h * J.lim.reject;
-                if (pr.max_rejects > 0 && ++L.rej >= pr.max_rejects) {
-                    L.out = L.p;
-                    L.flag = pack_flag(0, QSL_LINE_REJECT_LIMIT);
-                    return true;
-                }
-                return false;
-            }
-        }
-        L.rej = 0;
-        float h = L.h * scale;
-        if (EXACT) {
-            if ((double)h > pr.h_max) h = (float)pr.h_max;
-            if ((double)h < pr.h_min) h = (float)pr.h_min;
-        } else {
-            if (h > J.lim.h_max) h = J.lim.h_max;  // a NaN step stays NaN, as above
-            if (h < J.lim.h_min) h = J.lim.h_min;
-        }
-        L.h = h;
+        const int c = lane_control(J, L, err);
+        if (c != 0) return c == 2;
     } else {
         inc = step_rk4<EXACT>(f, L.p, hd, ns, want_b);
     }
+    return lane_move<EXACT, TWIST>(f, J, L, inc, b_at_p, tw_on, ns);
+}
+
+// The accepted step's move: the position update (Kahan-compensated in fast
+// arithmetic), the length, the twist increment and the exit test with the
+// footpoint on the face.  True when the direction is finished.
+template <bool EXACT, bool TWIST, class F>
+__device__ __forceinline__ bool lane_move(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, float3 inc,
+                                          float3 b_at_p, bool tw_on, unsigned& ns) {
+    const qsl_trace_params& pr = J.prm;
     float3 p2;
+    float dl;
     if (EXACT) {
         p2 = L.p + inc;
+        dl = norm(L.p - p2);
     } else {
         // Kahan-compensated position update: the rounding lost in p + inc is
         // carried into the next step, so long lines of short steps do not
-        // drift by accumulated float rounding.
-        const float3 y = inc - L.pc;
-        p2 = L.p + y;
-        L.pc = (p2 - L.p) - y;
+        // drift by accumulated float rounding.  (x, y) on the packed pipe;
+        // t = p2 - p, the increment as applied, also gives the step length.
+        const float2 pxy = make_float2(L.p.x, L.p.y);
+        const float2 yxy = fsub2(make_float2(inc.x, inc.y), make_float2(L.pc.x, L.pc.y));
+        const float yz = inc.z - L.pc.z;
+        const float2 qxy = __fadd2_rn(pxy, yxy);
+        const float qz = L.p.z + yz;
+        const float2 txy = fsub2(qxy, pxy);
+        const float tz = qz - L.p.z;
+        const float2 cxy = fsub2(txy, yxy);
+        L.pc = v3(cxy.x, cxy.y, tz - yz);
+        p2 = v3(qxy.x, qxy.y, qz);
+        dl = norm_fast(v3(txy.x, txy.y, tz));
     }
-    const float dl = EXACT ? norm(L.p - p2) : norm_fast(L.p - p2);
     len_add(L, (double)dl, dl);
     float td = 0.f;
     float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
@@ -604,6 +680,51 @@ __device__ __forceinline__ bool lane_step(const F& f, const TraceJob<F>& J, Lane
     }
     L.p = p2;
     L.steps++;
+    return false;
+}
+
+// A finished direction's outputs, as the reference writes them
+// (TraceBlineAdaptive.cu:466-501): after the forward direction its end
+// footpoint, flag, B and length, then the backward direction begins (returns
+// true); after the backward one the start footpoint, B at the seed and
+// B_flag (returns false: the line is done).  The per-line scalars come from
+// functors so that they are re-read rather than held in registers.
+template <bool EXACT, bool TWIST, class F, class SL, class TC, class NR>
+__device__ __forceinline__ bool lane_finish(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, bool tw_on,
+                                            unsigned& ns, const SL& s_len_of, const TC& tol_coef_of,
+                                            const NR& nrm_of) {
+    const long long i = L.line;
+    const TraceOut& o = J.o;
+    if (L.dsign == 0) {
+        const float3 pe = L.out;
+        const float3 be = sample_endpoint<EXACT>(f, pe);
+        ns += 1;
+        o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
+        o.flag_end[i] = lane_flag(L.flag);
+        if (o.status_end) o.status_end[i] = lane_status(L.flag);
+        o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
+        o.line_len[i] = (double)L.len;
+        if (TWIST && tw_on) o.twist[i] = L.tw;
+        lane_begin<EXACT>(f, J, L, i, -1, s_len_of(), tol_coef_of(), nrm_of(), ns);
+        return true;
+    }
+    const float3 ps = L.out;
+    const float3 bs = sample_endpoint<EXACT>(f, ps);
+    const float3 p0 = v3(__ldg(J.inp_x + i), __ldg(J.inp_y + i), __ldg(J.inp_z + i));
+    const float3 b0 = sample_endpoint<EXACT>(f, p0);
+    ns += 2;
+    o.start_x[i] = ps.x; o.start_y[i] = ps.y; o.start_z[i] = ps.z;
+    o.flag_start[i] = lane_flag(L.flag);
+    if (o.status_start) o.status_start[i] = lane_status(L.flag);
+    o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
+    o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
+    o.line_len[i] = o.line_len[i] + (double)L.len;
+    if (TWIST && tw_on) o.twist[i] = o.twist[i] + L.tw;
+    // B nearly in the seed plane (TraceBlineAdaptive.cu:498-501)
+    const float3 nrm = nrm_of();
+    const float bn = b0.x * nrm.x + b0.y * nrm.y + b0.z * nrm.z;
+    const float bm = sqrtf(b0.x * b0.x + b0.y * b0.y + b0.z * b0.z);
+    o.b_flag[i] = ((double)fabsf(bn) * 100. < (double)bm) ? 1 : 0;
     return false;
 }
 
@@ -722,45 +843,14 @@ __device__ __forceinline__ void trace_kernel_body(const TraceJob<F>& J) {
 
         // ---- advance this lane's line by one trial step ----
         if (lane_step<EXACT, TWIST>(f, J, L, len_lim, tw_on, ns)) {
-            const long long i = L.line;
-            const TraceOut& o = J.o;
-            if (L.dir > 0) {
-                // forward direction done: its outputs go out now, as the
-                // reference writes them (TraceBlineAdaptive.cu:466-474)
-                const float3 pe = L.out;
-                const float3 be = sample_endpoint<EXACT>(f, pe);
-                ns += 1;
-                o.end_x[i] = pe.x; o.end_y[i] = pe.y; o.end_z[i] = pe.z;
-                o.flag_end[i] = lane_flag(L.flag);
-                if (o.status_end) o.status_end[i] = lane_status(L.flag);
-                o.bend_x[i] = be.x; o.bend_y[i] = be.y; o.bend_z[i] = be.z;
-                o.line_len[i] = (double)L.len;
-                if (TWIST && tw_on) o.twist[i] = L.tw;
-                lane_begin<EXACT>(f, J, L, i, -1, s_len_of(), tol_coef_of(), nrm_of(), ns);
-            } else {
-                const float3 ps = L.out;
-                const float3 bs = sample_endpoint<EXACT>(f, ps);
-                const float3 p0 = v3(__ldg(J.inp_x + i), __ldg(J.inp_y + i), __ldg(J.inp_z + i));
-                const float3 b0 = sample_endpoint<EXACT>(f, p0);
-                ns += 2;
-                o.start_x[i] = ps.x; o.start_y[i] = ps.y; o.start_z[i] = ps.z;
-                o.flag_start[i] = lane_flag(L.flag);
-                if (o.status_start) o.status_start[i] = lane_status(L.flag);
-                o.bstart_x[i] = bs.x; o.bstart_y[i] = bs.y; o.bstart_z[i] = bs.z;
-                o.bthis_x[i] = b0.x; o.bthis_y[i] = b0.y; o.bthis_z[i] = b0.z;
-                o.line_len[i] = o.line_len[i] + (double)L.len;
-                if (TWIST && tw_on) o.twist[i] = o.twist[i] + L.tw;
-                // B nearly in the seed plane (TraceBlineAdaptive.cu:498-501)
-                const float3 nrm = nrm_of();
-                const float bn = b0.x * nrm.x + b0.y * nrm.y + b0.z * nrm.z;
-                const float bm = sqrtf(b0.x * b0.x + b0.y * b0.y + b0.z * b0.z);
-                o.b_flag[i] = ((double)fabsf(bn) * 100. < (double)bm) ? 1 : 0;
-                active = false;
+            // a lane's sample count nears 32 bits: hand it over (checked at
+            // direction ends only; exact while one direction takes fewer than
+            // 5e8 trial steps)
+            if (ns > (1u << 30)) {
+                if (J.samples) atomicAdd(J.samples, (unsigned long long)ns);
+                ns = 0;
             }
-        }
-        if (ns > (1u << 30)) {  // a lane's count nears 32 bits: hand it over (rare)
-            if (J.samples) atomicAdd(J.samples, (unsigned long long)ns);
-            ns = 0;
+            active = lane_finish<EXACT, TWIST>(f, J, L, tw_on, ns, s_len_of, tol_coef_of, nrm_of);
         }
     }
     if (J.samples) {
