@@ -43,12 +43,20 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) { return v3(s * a
 __device__ __forceinline__ float3 operator/(float3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float norm(float3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
-// |a| with the hardware square-root approximation (sqrt.approx.f32, relative
-// error ~2^-22): the fast stepper's error norm and step length, where the
+// |a| with the hardware square-root approximation (sqrt.approx.ftz.f32,
+// relative error ~2^-22): the fast stepper's error norm and step length, where the
 // IEEE square root's range checks and fix-up cost more than they are worth
 __device__ __forceinline__ float norm_fast(float3 a) {
     float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(fmaf(a.x, a.x, fmaf(a.y, a.y, a.z * a.z))));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(fmaf(a.x, a.x, fmaf(a.y, a.y, a.z * a.z))));
+    return r;
+}
+// 1/sqrt(x) by the hardware approximation with subnormal inputs flushed to
+// zero (rsqrt.approx.ftz.f32): the fast samplers' normalisation, where |B|^2
+// is far above the subnormal range whenever B/|B| is defined
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
 // x / y as x times the hardware reciprocal approximation (rcp.approx.f32,
@@ -366,7 +374,7 @@ __device__ __forceinline__ float3 sample(const F& f, float3 p, bool unit) {
             const float nb = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
             r = v3(r.x / nb, r.y / nb, r.z / nb);
         } else {
-            const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+            const float inv = rsqrt_fast(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
             r = v3(r.x * inv, r.y * inv, r.z * inv);
         }
     } else if (s != 1.0f) {
@@ -398,7 +406,7 @@ __device__ __forceinline__ float3 sample_unit_raw_generic(const F& f, float3 p, 
     const float s = f.corners(ix, iy, iz, c);
     const float3 r = blend<false>(c, w);
     raw = s != 1.0f ? v3(r.x * s, r.y * s, r.z * s) : r;
-    const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+    const float inv = rsqrt_fast(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
     return v3(r.x * inv, r.y * inv, r.z * inv);
 }
 template <>
@@ -562,7 +570,7 @@ __device__ __forceinline__ float3 h4b_sample(const FieldH4B& f, float3 p, bool u
     unsigned brick;
     float3 r = h4b_interp<W16>(f, p, brick);
     if (unit) {
-        const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+        const float inv = rsqrt_fast(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
         const float2 xy = __fmul2_rn(make_float2(r.x, r.y), make_float2(inv, inv));
         r = v3(xy.x, xy.y, r.z * inv);
     } else {
@@ -577,7 +585,7 @@ __device__ __forceinline__ float3 h4b_sample_unit_raw(const FieldH4B& f, float3 
     const float3 r = h4b_interp<W16>(f, p, brick);
     const float s = __ldg(f.scale + brick);
     raw = v3(r.x * s, r.y * s, r.z * s);
-    const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+    const float inv = rsqrt_fast(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
     return v3(r.x * inv, r.y * inv, r.z * inv);
 }
 
@@ -643,7 +651,7 @@ __device__ __forceinline__ float3 sample_h8c(const FieldH8C& f, float3 p, bool u
     const float2 rxy = lerp2(g0, g1, oz, rz);
     float3 v = v3(rxy.x, rxy.y, fmaf(gz1, rz, gz0 * oz));
     if (unit) {
-        const float inv = rsqrtf(fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z)));
+        const float inv = rsqrt_fast(fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z)));
         v = v3(v.x * inv, v.y * inv, v.z * inv);
     } else {
         const float s = __ldg(reinterpret_cast<const float*>(r + 3));
@@ -800,7 +808,7 @@ __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, floa
             const float nb = sqrtf(r.x * r.x + r.y * r.y + r.z * r.z);
             r = v3(r.x / nb, r.y / nb, r.z / nb);
         } else {
-            const float inv = rsqrtf(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
+            const float inv = rsqrt_fast(fmaf(r.x, r.x, fmaf(r.y, r.y, r.z * r.z)));
             r = v3(r.x * inv, r.y * inv, r.z * inv);
         }
     }

@@ -99,7 +99,7 @@ __device__ __forceinline__ float3 unit_and_grad_analytic(const F& f, float3 p, f
         Dy = Dy + (sy * wx * wz) * c[q];
         Dz = Dz + (sz * wx * wy) * c[q];
     }
-    const float inv = rsqrtf(dot(B, B));
+    const float inv = rsqrt_fast(dot(B, B));
     const float3 b = inv * B;
     const float3 D[3] = {Dx, Dy, Dz};
 #pragma unroll
@@ -197,7 +197,7 @@ __device__ __forceinline__ Vec9 scott_step_rolled(const F& f, const Vec9& s, flo
 // exact arithmetic, the hardware rsqrt otherwise.
 template <bool EXACT>
 __device__ __forceinline__ float3 unit_rsq(float3 a) {
-    const float inv = EXACT ? 1.0f / sqrtf(dot(a, a)) : rsqrtf(dot(a, a));
+    const float inv = EXACT ? 1.0f / sqrtf(dot(a, a)) : rsqrt_fast(dot(a, a));
     return v3(a.x * inv, a.y * inv, a.z * inv);
 }
 
