@@ -189,7 +189,9 @@ def run_ours(args, rank, world):
         tuned = {"tile": (8, 8), "occupancy": plan.occupancy_for(store), "schedule": plan.schedule, "chunk": 0,
                  "table": {}}
     else:
-        tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=8)
+        # a quarter of the stack, spread over it: on 8 planes the register
+        # budgets of 7 and 8 blocks/SM ranked the other way round from the full cube
+        tuned = autotune.tune_plan(plan, store, xs, ys, zz, prm, s_len=S_LEN, sample_planes=max(8, npl // 4))
     stream = torch.cuda.current_stream()
 
     def step(count=False, ev=None):
