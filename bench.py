@@ -583,18 +583,25 @@ def forms(device, planes=16):
     ax = [torch.arange(n, dtype=torch.float32, device=device) for n in bx.shape]
     cur = [api.as_xfast(c.float()) for c in FastQSL.curl_of_B_grid(bx, by, bz, *ax)]
     cnt = torch.zeros(1, dtype=torch.int64, device=device)
-    kw = dict(s_len=S_LEN, schedule="static", out=out, order=order, occupancy=8)
+    kw = dict(s_len=S_LEN, schedule="static", out=out, order=order)
     f4 = api.FieldStore(bx, by, bz, layout="f4")
+
+    def best(fn):
+        # each form at its best register budget of 6, 7 or 8 blocks/SM (the
+        # twist kernels hold more live values than the plain trace)
+        return min((timed(lambda: fn(o)), o) for o in (6, 7, 8))
+
     for name, st in (("h4b", store), ("f4", f4)):
         cs = api.FieldStore(*cur, layout=name)
-        ms0 = timed(lambda: api.trace(st, xs, ys, zz, prm, **kw))
-        ms1 = timed(lambda: api.trace(st, xs, ys, zz, prm, curB=cur, **kw))
-        ms2 = timed(lambda: api.trace(st, xs, ys, zz, prm, curB=cs, **kw))
+        ms0, o0 = best(lambda o: api.trace(st, xs, ys, zz, prm, occupancy=o, **kw))
+        ms1, o1 = best(lambda o: api.trace(st, xs, ys, zz, prm, curB=cur, occupancy=o, **kw))
+        ms2, o2 = best(lambda o: api.trace(st, xs, ys, zz, prm, curB=cs, occupancy=o, **kw))
         cnt.zero_()
-        api.trace(st, xs, ys, zz, prm, curB=cs, samples=cnt, **kw)
+        api.trace(st, xs, ys, zz, prm, curB=cs, samples=cnt, occupancy=o2, **kw)
         torch.cuda.synchronize()
         res[f"trace_twist_{name}"] = {"lines": int(xs.numel()), "ms_without": ms0, "ms_with_current_arrays": ms1,
-                                      "ms_with_current_store": ms2, "samples_with": int(cnt.item())}
+                                      "ms_with_current_store": ms2, "samples_with": int(cnt.item()),
+                                      "blocks_per_sm": {"without": o0, "current_arrays": o1, "current_store": o2}}
         cs.close()
     f4.close()
     del cur, out

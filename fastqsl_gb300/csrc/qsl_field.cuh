@@ -59,13 +59,13 @@ __device__ __forceinline__ float rsqrt_fast(float x) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-// x / y as x times the hardware reciprocal approximation (rcp.approx.f32,
-// relative error ~2^-23), the product rounded on its own (__fmul_rn is never
-// merged into a fused multiply-add), so that every kernel that inlines it
-// gets the same bits
+// x / y as x times the hardware reciprocal approximation (rcp.approx.ftz.f32,
+// relative error ~2^-23; y is a cell width, far from the subnormal range),
+// the product rounded on its own (__fmul_rn is never merged into a fused
+// multiply-add), so that every kernel that inlines it gets the same bits
 __device__ __forceinline__ float div_fast(float x, float y) {
     float r;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(y));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(y));
     return __fmul_rn(x, r);
 }
 __device__ __forceinline__ float comp(float3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }

@@ -599,6 +599,21 @@ template <bool EXACT, bool TWIST, class F>
 __device__ __forceinline__ bool lane_move(const F& f, const TraceJob<F>& J, Lane<EXACT>& L, float3 inc,
                                           float3 b_at_p, bool tw_on, unsigned& ns) {
     const qsl_trace_params& pr = J.prm;
+    // the twist integrand at the step's start point, before the position
+    // update (fewer values live during the current density's sample)
+    float td = 0.f;
+    float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
+    if (TWIST && tw_on) {
+        j1 = J.cur_packed ? sample<EXACT>(J.cur_store, L.p, false) : sample<EXACT>(current_view(f, J.cur), L.p, false);
+        if (EXACT) {
+            b1 = sample<EXACT>(f, L.p, false);
+            ns += 2;
+        } else {
+            b1 = b_at_p;
+            ns += 1;
+        }
+        td = twist_density<EXACT>(j1, b1);
+    }
     float3 p2;
     float dl;
     if (EXACT) {
@@ -622,20 +637,8 @@ __device__ __forceinline__ bool lane_move(const F& f, const TraceJob<F>& J, Lane
         dl = norm_fast(v3(txy.x, txy.y, tz));
     }
     len_add(L, (double)dl, dl);
-    float td = 0.f;
-    float3 b1 = v3(0.f, 0.f, 0.f), j1 = v3(0.f, 0.f, 0.f);
-    if (TWIST && tw_on) {
-        j1 = J.cur_packed ? sample<EXACT>(J.cur_store, L.p, false) : sample<EXACT>(current_view(f, J.cur), L.p, false);
-        if (EXACT) {
-            b1 = sample<EXACT>(f, L.p, false);
-            ns += 2;
-        } else {
-            b1 = b_at_p;
-            ns += 1;
-        }
-        td = twist_density<EXACT>(j1, b1);
+    if (TWIST && tw_on)
         L.tw = L.tw + (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
-    }
     // inside test first: the full face classification only runs on exit
     const int flag = box_inside(f, p2) ? 0 : box_exit(f, p2);
     if (flag > 0) {
