@@ -866,8 +866,9 @@ def main():
     line["roofline"]["flops"] = {"achieved": flops / k_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                                  "frac": flops / k_s / 1e12 / fp32_peak, "peak_kind": "nominal",
                                  "sm_count": res["sm_count"]}
-    line["roofline"]["limiter"] = ("SM issue and the L1 data pipe together (ncu on 32 mid-cube planes: "
-                                   "issue active ~81 %, L1 LSU wavefronts ~81 % of peak)")
+    line["roofline"]["limiter"] = ("SM issue, the FMA pipe and the L1 data pipe together (ncu on 32 mid-cube "
+                                   "planes: issue active ~74 %, FMA pipe ~64 % of its cycles, L1 LSU wavefronts "
+                                   "~76 % of peak)")
     # launches per step: main trace, qcalc, flag_count, tile_scan, cook_write,
     # pseudo trace, qcut, qmerge (+ 2 memsets of the queue counters)
     line["gpu_launches"] = 8 * args.steps
