@@ -23,7 +23,8 @@ NO_FMA = {"trace_exact.cu", "qassembly.cu", "curl.cu", "path.cu"}
 SOURCES = ["capi.cu", "trace_exact.cu", "trace_fast_soa.cu", "trace_fast_f4.cu", "trace_fast_h4b.cu",
            "trace_fast_h4bw.cu", "trace_fast_h8c.cu", "trace_fast_stretch.cu", "trace_fast_stretch_packed.cu",
            "trace_fast_stretch_packed_uni.cu", "field_store.cu",
-           "qassembly.cu", "hybrid.cu", "curl.cu", "path.cu", "noalloc.cu", "probe.cu", "seeds.cu"]
+           "qassembly.cu", "hybrid.cu", "curl.cu", "path.cu", "noalloc.cu", "probe.cu", "seeds.cu",
+           "qmap_batch.cu"]
 
 
 def _deps():

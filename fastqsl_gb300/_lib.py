@@ -65,6 +65,22 @@ def _finish_batch_job():
 
 _finish_batch_job()
 
+
+class QmapJob(ctypes.Structure):
+    pass  # fields set below (needs TraceParams)
+
+
+def _finish_qmap_job():
+    from .params import TraceParams
+    d3 = ctypes.c_double * 3
+    QmapJob._fields_ = [("field", ctypes.c_void_p), ("params", TraceParams), ("center", d3), ("normal", d3),
+                        ("u", d3), ("v", d3), ("spacing", ctypes.c_double), ("n0", ctypes.c_int32),
+                        ("n1", ctypes.c_int32), ("nplanes", ctypes.c_int32), ("tile_y", ctypes.c_int32),
+                        ("tile_x", ctypes.c_int32), ("s_len", ctypes.c_float), ("tol_coef", ctypes.c_float)]
+
+
+_finish_qmap_job()
+
 # name -> (restype, argtypes); every pointer is c_void_p
 _P = c_vp
 _SIGS = {
@@ -113,6 +129,13 @@ _SIGS = {
     "qsl_l1_probe": (c_int, [_P, c_i64, c_int, c_int, c_int, _P, _P]),
     "qsl_plane_seeds": (c_int, [_P, _P, _P, _P, c_double, c_int, c_int, c_int, _P, _P, _P, _P]),
     "qsl_tile_order": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, _P, _P]),
+    "qsl_qmap_batch_size": (c_int, [_P, c_int, _P, _P]),
+    "qsl_qmap_batch_create": (c_int, [_P, c_int, _P, c_i64, _P, c_i64, _P, _P]),
+    "qsl_qmap_batch_lines": (c_i64, [_P]),
+    "qsl_qmap_batch_run_main": (c_int, [_P, c_i64, c_i64, c_int, c_int, _P]),
+    "qsl_qmap_batch_run_post": (c_int, [_P, c_int, c_int, _P]),
+    "qsl_qmap_batch_q": (_P, [_P, c_int]),
+    "qsl_qmap_batch_destroy": (c_int, [_P]),
 }
 
 

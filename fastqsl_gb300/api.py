@@ -572,6 +572,95 @@ def _hybrid_impl(self, field, xs, ys, zs, params, s_len, tol_coef, scott_params,
 QMapPlan._hybrid = _hybrid_impl
 
 
+class PlaneQBatch:
+    """Q maps of many plane jobs as one native batch (qsl_qmap_batch_*): the
+    seed grids, tile orders, job tables, batched traces and per-job Q
+    assembly are laid out in one workspace allocation and queued by the C++
+    library, a few launches per job and no per-array host bookkeeping.  The
+    Q maps equal QBatch's on the same jobs bit for bit (the same kernels in
+    the same order).  Reference workflow per job: demo/Q_RKF45CuPy.ipynb
+    cells 7-11.
+
+    jobs: list of dicts with keys field (FieldStore), params, center, normal,
+    u, v (unit plane axes: columns along u, rows along v), spacing, n0, n1,
+    nplanes and optionally s_len (0.25), tol_coef (1.0).  tile: the seed tile
+    of the trace order (None: seed order).  blocks_per_sm > 0: the batched
+    traces keep at most that many resident blocks per SM."""
+
+    def __init__(self, jobs, device="cuda", tile=(8, 8), stream=None, blocks_per_sm=0):
+        lib = _lib.load()
+        self.max_blocks = 0
+        if blocks_per_sm:
+            sms = ctypes.c_int(0)
+            _lib.check(lib.qsl_device_sm_count(ctypes.byref(sms)), "qsl_device_sm_count")
+            self.max_blocks = int(blocks_per_sm) * sms.value
+        self.njobs = len(jobs)
+        arr = (_lib.QmapJob * max(1, self.njobs))()
+        ty, tx = (int(tile[0]), int(tile[1])) if tile else (0, 0)
+        for k, j in enumerate(jobs):
+            a = arr[k]
+            a.field = j["field"].handle
+            a.params = j["params"]
+            a.center[:] = [float(c) for c in j["center"]]
+            a.normal[:] = [float(c) for c in j["normal"]]
+            a.u[:] = [float(c) for c in j["u"]]
+            a.v[:] = [float(c) for c in j["v"]]
+            a.spacing = float(j["spacing"])
+            a.n0, a.n1, a.nplanes = int(j["n0"]), int(j["n1"]), int(j.get("nplanes", 1))
+            a.tile_y, a.tile_x = ty, tx
+            a.s_len = float(j.get("s_len", 0.25))
+            a.tol_coef = float(j.get("tol_coef", 1.0))
+        db, hb = ctypes.c_int64(0), ctypes.c_int64(0)
+        _lib.check(lib.qsl_qmap_batch_size(arr, self.njobs, ctypes.byref(db), ctypes.byref(hb)), "qsl_qmap_batch_size")
+        self.workspace = torch.empty(max(256, db.value), dtype=torch.uint8, device=device)
+        self._host = torch.empty(max(256, hb.value), dtype=torch.uint8, pin_memory=True)
+        h = ctypes.c_void_p()
+        _lib.check(lib.qsl_qmap_batch_create(arr, self.njobs, self.workspace.data_ptr(), db.value,
+                                             self._host.data_ptr(), hb.value, stream_handle(stream), ctypes.byref(h)),
+                   "qsl_qmap_batch_create")
+        self.handle = h
+        base = self.workspace.data_ptr()
+        self.Q = []
+        for k, j in enumerate(jobs):
+            off = int(lib.qsl_qmap_batch_q(h, k)) - base
+            n0, n1, npl = int(j["n0"]), int(j["n1"]), int(j.get("nplanes", 1))
+            qn = npl * (n0 - 2) * (n1 - 2)
+            self.Q.append(self.workspace[off:off + 8 * qn].view(torch.float64).view(npl, n0 - 2, n1 - 2))
+        # register budget of the batched kernels (resident blocks per SM; 0 = 8)
+        self.occupancy = 0
+
+    @property
+    def main_lines(self):
+        return int(_lib.load().qsl_qmap_batch_lines(self.handle))
+
+    def run_main(self, stream=None, lo=0, hi=-1):
+        """The batched main trace, or the window [lo, hi) of its lines."""
+        _lib.check(_lib.load().qsl_qmap_batch_run_main(self.handle, int(lo), int(hi), self.max_blocks, self.occupancy,
+                                                       stream_handle(stream)), "qsl_qmap_batch_run_main")
+
+    def run_post(self, stream=None):
+        """Everything after the main trace: Q, pseudo-lines, merge; returns
+        the jobs' Q maps (views of the workspace)."""
+        _lib.check(_lib.load().qsl_qmap_batch_run_post(self.handle, self.max_blocks, self.occupancy,
+                                                       stream_handle(stream)), "qsl_qmap_batch_run_post")
+        return self.Q
+
+    def run(self, stream=None):
+        self.run_main(stream)
+        return self.run_post(stream)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().qsl_qmap_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class QSeries:
     """Q maps of a series of fields given on the host (the snapshots of a
     simulation, a run of magnetograms' extrapolations) on one seed geometry,

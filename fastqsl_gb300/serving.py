@@ -10,8 +10,10 @@ sub-box) and an RKF45 tolerance.  The scheduler loop:
 * sorts requests into size classes; per class, admits waiting requests in
   arrival order while their device memory fits in what the budget has left,
   up to the class's batch size and in-flight limit;
-* launches every newly admitted group as one batch (QBatch: one main-trace
-  launch and one pseudo-line launch for all of them) on one of the class's
+* launches every newly admitted group as one batch (PlaneQBatch, the native
+  qsl_qmap_batch: seed grids, tile orders and job tables built by the C++
+  library in one workspace allocation; one main-trace launch and one
+  pseudo-line launch for all of them) on one of the class's
   CUDA streams, so a batch starts while earlier ones are still on the GPU and
   their work overlaps on the device.  Smaller classes run on higher-priority
   streams: their blocks are dispatched ahead of a large batch's remaining
@@ -81,11 +83,13 @@ class QRequest:
 
 
 def request_bytes(req: QRequest) -> int:
-    """Device bytes a request holds while in flight (QBatch buffers: main
+    """Device bytes a request holds while in flight (batch buffers: main
     trace outputs, order, seeds, the pseudo-line buffers sized for every
     interior pixel, Q and the compaction workspace)."""
     n, m = req.seeds, req.qpixels
-    return int(n * (72 + 8 + 4 + 12 + 4) + m * (4 * (72 + 8 + 12) + 8 + 8 + 8 + 8) + (n // 1024 + 1) * 12 + 4096)
+    # (+ the 256-byte alignment of each of the job's ~60 arrays and its
+    # share of the job tables)
+    return int(n * (72 + 8 + 4 + 12 + 4) + m * (4 * (72 + 8 + 12) + 8 + 8 + 8 + 8) + (n // 1024 + 1) * 12 + 20480)
 
 
 def _cross(a, b):
@@ -312,16 +316,18 @@ class QServer:
         self._next_stream[cls] = (self._next_stream[cls] + 1) % len(self.streams[cls])
         t = time.perf_counter()
         with torch.cuda.stream(st):
-            specs = []
+            jobs = []
             for r in group:
                 r.t_admit = t
-                xs, ys, zs, nrm = seeds_on_device(r, self.device, st)
+                n, u, v = plane_axes(r.normal)
                 prm = absolute_rkf45(tol=r.tol, h_min=self.h_min, h_max=self.h_max)
-                specs.append(dict(field=self.fields[r.field], xs=xs, ys=ys, zs=zs, n0=r.n0, n1=r.n1,
-                                  nplanes=r.nplanes, params=prm, s_len=self.s_len, stride=r.spacing, cross_dir=nrm))
+                jobs.append(dict(field=self.fields[r.field], params=prm, center=r.center, normal=n, u=u, v=v,
+                                 spacing=r.spacing, n0=r.n0, n1=r.n1, nplanes=r.nplanes, s_len=self.s_len))
             windowed = cls > 0 and self.chunk_lines > 0
             cap = self.window_blocks_per_sm if windowed else self.big_blocks_per_sm if cls > 0 else 0
-            qb = api.QBatch(specs, device=self.device, tile=self.tile, stream=st, blocks_per_sm=cap)
+            # the native batch: seeds, tile orders, job tables and every
+            # launch of the pipeline queued by the C++ library
+            qb = api.PlaneQBatch(jobs, device=self.device, tile=self.tile, stream=st, blocks_per_sm=cap)
         self.used += nbytes
         self.batches += 1
         fl = _Flight(group, qb, cls, st, nbytes)

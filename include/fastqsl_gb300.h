@@ -536,6 +536,57 @@ int qsl_plane_seeds(const double *center_h, const double *normal_h, const double
                     double spacing, int n0, int n1, int nplanes, float *xs, float *ys, float *zs,
                     qsl_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Native Q-map batches (no reference counterpart: the reference's notebooks
+ * run one Q map at a time, demo/Q_RKF45CuPy.ipynb cells 7-11, with the
+ * RKF45 kernel TraceBlineAdaptive.cu:429-510 and FastQSL.py:4-117).  The
+ * whole plane Q pipeline of many jobs laid out in one caller-provided
+ * workspace and queued from the host library: per job its seed grid
+ * (qsl_plane_seeds) and tile order (qsl_tile_order), one batched main trace
+ * (or windows of it), then per job Q (qsl_qcalc_plane, FP64) and the
+ * pseudo-line compaction (qsl_cook_pseudo_line), one batched pseudo-line
+ * trace, per job pseudo Q and merge (qsl_qcut, qsl_qmerge).  The Q maps
+ * equal a batch of the same jobs built from those entries one by one, bit
+ * for bit.  No device allocation, no synchronisation; a serving loop builds
+ * a batch of small requests in a few launches per request.
+ * ------------------------------------------------------------------------ */
+typedef struct qsl_qmap_job {
+    const qsl_field_t *field;
+    qsl_trace_params params;   /* arith must be QSL_ARITH_FAST */
+    double center[3];          /* plane k at center + k spacing normal */
+    double normal[3];          /* unit normal: the plane step and the Q cross direction */
+    double u[3], v[3];         /* in-plane unit axes: columns along u, rows along v */
+    double spacing;            /* seed spacing within and between planes (the Q stride) */
+    int32_t n0, n1, nplanes;   /* rows, columns (>= 3 each), planes (>= 1); at most 2^32 seeds */
+    int32_t tile_y, tile_x;    /* seed tile of the trace order (0: seed order) */
+    float s_len, tol_coef;
+} qsl_qmap_job;
+typedef struct qsl_qmap_batch qsl_qmap_batch_t;
+
+/* Bytes a batch of these jobs needs: device workspace (its arrays and job
+ * tables) and pinned host staging (the job tables on their way to the
+ * device). */
+int qsl_qmap_batch_size(const qsl_qmap_job *jobs, int njobs, int64_t *device_bytes, int64_t *host_bytes);
+/* Lays the batch out in `workspace` (device, 256-byte aligned, at least
+ * device_bytes) and queues on `stream` the seed grids, the tile orders and
+ * the host-to-device copy of the job tables from `host_staging` (host, at
+ * least host_bytes, pinned for an asynchronous copy; it must stay untouched
+ * until the stream has passed the copy).  *out: a host handle. */
+int qsl_qmap_batch_create(const qsl_qmap_job *jobs, int njobs, void *workspace, int64_t workspace_bytes,
+                          void *host_staging, int64_t host_bytes, qsl_stream_t stream, qsl_qmap_batch_t **out);
+/* End of the batched main trace's line space (for windows). */
+int64_t qsl_qmap_batch_lines(const qsl_qmap_batch_t *batch);
+/* The batched main trace over lines [line_lo, line_hi) (line_hi < 0: to the
+ * end), max_blocks / occupancy as in qsl_batch_run_window. */
+int qsl_qmap_batch_run_main(const qsl_qmap_batch_t *batch, int64_t line_lo, int64_t line_hi, int max_blocks,
+                            int occupancy, qsl_stream_t stream);
+/* Everything after the main trace: Q, pseudo-lines and merge of every job. */
+int qsl_qmap_batch_run_post(const qsl_qmap_batch_t *batch, int max_blocks, int occupancy, qsl_stream_t stream);
+/* Device address of job k's Q, float64 (nplanes, n0 - 2, n1 - 2) inside the workspace. */
+double *qsl_qmap_batch_q(const qsl_qmap_batch_t *batch, int job);
+/* Frees the host handle (the workspace belongs to the caller). */
+int qsl_qmap_batch_destroy(qsl_qmap_batch_t *batch);
+
 /* Tile visiting order of nplanes stacked (n0, n1) seed planes (seed index
  * (p * n0 + y) * n1 + x), the `order` map of qsl_sched / qsl_batch_job:
  * order[k] = the seed visited k-th when the seeds are sorted by (plane

@@ -121,3 +121,24 @@ def test_seed_geometry_entries_validate_without_gpu(lib):
     assert lib.qsl_tile_order(1, 4, 4, 0, 8, 0, dummy, None) == -1
     assert lib.qsl_tile_order(2, 65536, 65536, 8, 8, 0, dummy, None) != 0
     assert b"2^32" in lib.qsl_last_error()
+
+
+def test_qmap_batch_validates_without_gpu(lib):
+    """qsl_qmap_batch_size / _create reject empty job lists, null fields and
+    degenerate planes before any CUDA call."""
+    import ctypes
+    from fastqsl_gb300 import _lib, params as P
+    d, h = ctypes.c_int64(0), ctypes.c_int64(0)
+    jobs = (_lib.QmapJob * 1)()
+    assert lib.qsl_qmap_batch_size(jobs, 0, ctypes.byref(d), ctypes.byref(h)) == -1
+    assert b"at least one job" in lib.qsl_last_error()
+    jobs[0].params = P.absolute_rkf45()
+    jobs[0].n0, jobs[0].n1, jobs[0].nplanes, jobs[0].spacing = 5, 5, 1, 1.0
+    assert lib.qsl_qmap_batch_size(jobs, 1, ctypes.byref(d), ctypes.byref(h)) == -1  # null field
+    jobs[0].field = 256
+    jobs[0].n0 = 2
+    assert lib.qsl_qmap_batch_size(jobs, 1, ctypes.byref(d), ctypes.byref(h)) == -1
+    out = ctypes.c_void_p()
+    assert lib.qsl_qmap_batch_create(jobs, 1, None, 0, None, 0, None, ctypes.byref(out)) == -1
+    assert lib.qsl_qmap_batch_run_main(None, 0, -1, 0, 0, None) == -1
+    assert lib.qsl_qmap_batch_q(None, 0) is None
