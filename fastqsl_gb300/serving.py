@@ -158,8 +158,8 @@ class QServer:
     CLASSES = ((1.5e5, 8, 4), (1.2e6, 2, 3), (float("inf"), 1, 3))
 
     def __init__(self, fields, hbm_budget=16 << 30, streams=2, max_batch=None, s_len=0.25, h_min=1e-3, h_max=1.0,
-                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=6,
-                 chunks_when_interactive=2, window_streams=2, window_blocks_per_sm=0, window_order="srpt"):
+                 tile=(8, 8), device="cuda", classes=None, big_blocks_per_sm=6, chunk_lines=1 << 17, max_chunks=4,
+                 chunks_when_interactive=1, window_streams=2, window_blocks_per_sm=0, window_order="srpt"):
         self.fields = dict(fields)
         self.budget = int(hbm_budget)
         self.used = 0
