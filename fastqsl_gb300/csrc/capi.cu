@@ -545,14 +545,16 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     if (twist && (!curBy || !curBz || !io->twist)) return fail(QSL_ERR_INVALID, "twist needs curB_x/y/z and twist");
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t cells = (int64_t)(nx - 1) + (ny - 1) + (nz - 1);
-    const bool packed_path = prm->arith == QSL_ARITH_FAST && cells * (1 + STRETCH_BINS_PER_CELL) < (1LL << 31);
-    // one stream-ordered buffer for the launch: the coordinates, then (fast
-    // arithmetic) the float4 node copy and the search tables
     const int64_t nodes = (int64_t)nx * ny * nz;
+    // (the packed sampler indexes records in 32 bits)
+    const bool packed_path = prm->arith == QSL_ARITH_FAST && cells * (1 + STRETCH_BINS_PER_CELL) < (1LL << 31) &&
+                             nodes < (1LL << 31);
+    // one stream-ordered buffer for the launch: the coordinates, then (fast
+    // arithmetic) the x-pair node records and the search tables
     const int64_t tcells = (packed_path && !uni) ? cells : 0;
     const int64_t ncoord = (int64_t)nx + ny + nz;
     const size_t coord_bytes = ((size_t)ncoord * sizeof(float) + 255) / 256 * 256;
-    const size_t bytes = coord_bytes + (packed_path ? (size_t)(nodes + tcells) * sizeof(float4) +
+    const size_t bytes = coord_bytes + (packed_path ? (size_t)(2 * nodes + tcells) * sizeof(float4) +
                                                           (size_t)tcells * STRETCH_BINS_PER_CELL * 2 * sizeof(float4)
                                                     : 0);
     char* buf = nullptr;
@@ -604,14 +606,15 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
         cudaFreeAsync(buf, st);
         return rc;
     }
-    // fast arithmetic: the nodes interleaved into a float4 copy for the
-    // launch (one 16-byte load per corner; the same values), followed, for
-    // the search, by its tables (a 16-byte record per cell, two 16-byte
-    // records per bin); the uniform formula needs none
+    // fast arithmetic: the nodes interleaved into x-pair records for the
+    // launch (node o and o + 1 as two float4: one 32-byte load per corner
+    // pair; the same values), followed, for the search, by its tables (a
+    // 16-byte record per cell, two 16-byte records per bin); the uniform
+    // formula needs none
     float4* b4 = reinterpret_cast<float4*>(buf + coord_bytes);
-    float4* srec = uni ? nullptr : b4 + nodes;
+    float4* srec = uni ? nullptr : b4 + 2 * nodes;
     float4* sbin = uni ? nullptr : srec + cells;
-    e = launch_pack_f4(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
+    e = launch_pack_f4x2(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
     if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {
         cudaFreeAsync(buf, st);

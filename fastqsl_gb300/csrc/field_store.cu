@@ -19,6 +19,28 @@ cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Di
     return cudaGetLastError();
 }
 
+// x-pair records of the packed stretched stores: record o = {node o, node
+// o + 1} as two float4 (Bx, By, Bz, 0), o = ix + nx (iy + ny iz); the last node
+// of a row pairs with itself (no cell reads that half).  One 32-byte record
+// per x corner pair of a trilinear stencil.
+__global__ void k_pack_f4x2(const float* __restrict__ bx, const float* __restrict__ by,
+                            const float* __restrict__ bz, int nx, long long n, float4* __restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long j = (i % nx == nx - 1) ? i : i + 1;
+        out[2 * i] = make_float4(__ldg(bx + i), __ldg(by + i), __ldg(bz + i), 0.f);
+        out[2 * i + 1] = make_float4(__ldg(bx + j), __ldg(by + j), __ldg(bz + j), 0.f);
+    }
+}
+
+cudaError_t launch_pack_f4x2(const float* bx, const float* by, const float* bz, Dims d, float4* out,
+                             cudaStream_t st) {
+    const long long n = (long long)d.nx * d.ny * d.nz;
+    long long g = (n + 255) / 256;
+    if (g > 65535LL * 64) g = 65535LL * 64;
+    k_pack_f4x2<<<(unsigned)g, 256, 0, st>>>(bx, by, bz, d.nx, n, out);
+    return cudaGetLastError();
+}
+
 // Search tables of a stretched grid (FieldStretchP::srec / sbin), all three
 // axes in one launch: one thread per cell and per bin.
 //  * cell j: the reference's search at c = a[j+1] (its comparisons c > a[m]

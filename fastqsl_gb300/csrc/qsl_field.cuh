@@ -232,7 +232,8 @@ struct FieldStretchT {
     float3 lo, hi;        // first and last node coordinates (read at kernel start)
     float3 clo, chi;      // lo + 1e-6 and hi - 1e-6, formed in double and narrowed
     float3 us;            // uniform-formula spacing (hi - lo) / n
-    const float4* b4;     // packed: Bx, By, Bz, 0 per node, x fastest
+    const float4* b4;     // packed: x-pair records {node o, node o + 1}, two float4 (Bx, By, Bz, 0) each,
+                          // o = ix + nx (iy + ny iz) (one 32-byte load per x corner pair)
     // search tables (M = 1), axes x, y, z one after another (axis k starts at
     // cell offset stretch_cell_offset(k)):
     //   srec[j]  the cell the reference's search gives for any coordinate in
@@ -249,21 +250,32 @@ struct FieldStretchT {
     float3 sbinv;         // bins per unit coordinate (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (M == 1 || M == 2) {
-            const FieldF4 s{b4, d};
-            return s.corners(ix, iy, iz, c);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {  // q = (dy << 1) | dz
+                const float4* r = b4 + 2 * record(ix, iy + (q >> 1), iz + (q & 1));
+                const float4 a = __ldg(r), b = __ldg(r + 1);
+                c[q] = v3(a.x, a.y, a.z);
+                c[4 | q] = v3(b.x, b.y, b.z);
+            }
+            return 1.0f;
         } else {
             const FieldSoA s{bx, by, bz, d};
             return s.corners(ix, iy, iz, c);
         }
     }
     __device__ __forceinline__ const float* axis(int k) const { return k == 0 ? ax : (k == 1 ? ay : az); }
+    // record index of node (ix, iy, iz) in the packed copy (the copy holds
+    // fewer than 2^31 nodes)
+    __device__ __forceinline__ unsigned record(int ix, int iy, int iz) const {
+        return (unsigned)ix + (unsigned)d.nx * ((unsigned)iy + (unsigned)d.ny * (unsigned)iz);
+    }
     // one node's (Bx, By, Bz)
     __device__ __forceinline__ float3 node(int ix, int iy, int iz) const {
-        const int64_t o = ix + (int64_t)d.nx * (iy + (int64_t)d.ny * iz);
         if constexpr (M == 1 || M == 2) {
-            const float4 v = __ldg(b4 + o);
+            const float4 v = __ldg(b4 + 2 * (size_t)record(ix, iy, iz));
             return v3(v.x, v.y, v.z);
         } else {
+            const int64_t o = ix + (int64_t)d.nx * (iy + (int64_t)d.ny * iz);
             return v3(__ldg(bx + o), __ldg(by + o), __ldg(bz + o));
         }
     }
@@ -767,7 +779,9 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
     r = EXACT ? (c - ai) / di : div_fast(__fsub_rn(c, ai), di);
 }
 
-template <bool EXACT, int M>
+// WIDE: the packed stores' 32-byte x-pair records as one 32-byte load (code
+// inlined into kernels only; see sample_h8c) or two 16-byte loads.
+template <bool EXACT, int M, bool WIDE = true>
 __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
@@ -789,10 +803,29 @@ __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, floa
         const float ox = 1.f - rx, oy = 1.f - ry, oz = 1.f - rz;
         float2 exy[4];
         float ez[4];
+        // packed stores: the four x-pair records of the stencil, at record
+        // indices o, o + nx ny (dz), o + nx (dy), o + nx + nx ny
+        const unsigned o0 = (M == 1 || M == 2) ? f.record(ix, iy, iz) : 0u;
+        const unsigned sy = (unsigned)f.d.nx, sz = (unsigned)f.d.nx * (unsigned)f.d.ny;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const float3 a = f.node(ix, iy + (q >> 1), iz + (q & 1));
-            const float3 b = f.node(ix + 1, iy + (q >> 1), iz + (q & 1));
+            float3 a, b;
+            if constexpr (M == 1 || M == 2) {
+                const float4* r = f.b4 + 2 * (size_t)(o0 + ((q >> 1) & 1) * sy + (q & 1) * sz);
+                if constexpr (WIDE) {
+                    unsigned w[8];
+                    ldg_v8(r, w);
+                    a = v3(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]));
+                    b = v3(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]));
+                } else {
+                    const float4 ra = __ldg(r), rb = __ldg(r + 1);
+                    a = v3(ra.x, ra.y, ra.z);
+                    b = v3(rb.x, rb.y, rb.z);
+                }
+            } else {
+                a = f.node(ix, iy + (q >> 1), iz + (q & 1));
+                b = f.node(ix + 1, iy + (q >> 1), iz + (q & 1));
+            }
             exy[q] = __ffma2_rn(make_float2(b.x, b.y), make_float2(rx, rx),
                                 __fmul2_rn(make_float2(a.x, a.y), make_float2(ox, ox)));
             ez[q] = fmaf(b.z, rx, a.z * ox);
@@ -834,6 +867,17 @@ __device__ __forceinline__ float3 sample<false, FieldStretchP>(const FieldStretc
 template <>
 __device__ __forceinline__ float3 sample<false, FieldStretchPU>(const FieldStretchPU& f, float3 p, bool unit) {
     return sample_stretch<false>(f, p, unit);
+}
+// out-of-line callers (the boundary RK4 leg) load the records as two
+// 16-byte halves
+template <>
+__device__ __forceinline__ float3 sample_outlined<false, FieldStretchP>(const FieldStretchP& f, float3 p, bool unit) {
+    return sample_stretch<false, 1, false>(f, p, unit);
+}
+template <>
+__device__ __forceinline__ float3 sample_outlined<false, FieldStretchPU>(const FieldStretchPU& f, float3 p,
+                                                                         bool unit) {
+    return sample_stretch<false, 2, false>(f, p, unit);
 }
 template <>
 __device__ __forceinline__ float3 sample<false, FieldStretchT<3>>(const FieldStretchT<3>& f, float3 p, bool unit) {

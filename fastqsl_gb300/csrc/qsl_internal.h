@@ -93,6 +93,8 @@ cudaError_t launch_hybrid_merge(const int* bflag, const float* qperp, long long 
 
 // field_store.cu
 cudaError_t launch_pack_f4(const float* bx, const float* by, const float* bz, Dims d, float4* out, cudaStream_t st);
+cudaError_t launch_pack_f4x2(const float* bx, const float* by, const float* bz, Dims d, float4* out,
+                             cudaStream_t st);
 cudaError_t launch_stretch_tables(const float* ax, const float* ay, const float* az, Dims d, float4* srec,
                                   float4* sbin, cudaStream_t st);
 cudaError_t launch_pack_h4b(const float* bx, const float* by, const float* bz, Dims d, int nbx, int nby, int nbz,
