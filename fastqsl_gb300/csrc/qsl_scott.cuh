@@ -118,7 +118,8 @@ __device__ __forceinline__ Vec9 scott_rhs(const F& f, const Vec9& s, unsigned& n
 }
 
 // Fehlberg step on the 9-vector; the error uses the position part only
-// (RKF45_Scott, TraceBlineScott.cu:256-290).
+// (RKF45_Scott, TraceBlineScott.cu:256-290): its norm in exact arithmetic,
+// its square in fast arithmetic (the fast controller works with log2 of it).
 template <bool EXACT, int GRAD, class F>
 __device__ __forceinline__ Vec9 scott_step(const F& f, const Vec9& s, float h, float& err, unsigned& ns) {
     using C = Fehlberg;
@@ -138,7 +139,7 @@ __device__ __forceinline__ Vec9 scott_step(const F& f, const Vec9& s, float h, f
                             mul9(C::a65, k5))),
                ns));
     const float3 e = (((C::e1 * k1.p + C::e3 * k3.p) + C::e4 * k4.p) + C::e5 * k5.p) + C::e6 * k6.p;
-    err = norm(e);
+    err = EXACT ? norm(e) : fmaf(e.x, e.x, fmaf(e.y, e.y, e.z * e.z));
     return add9(s, add9(add9(add9(add9(mul9(C::b1, k1), mul9(C::b3, k3)), mul9(C::b4, k4)), mul9(C::b5, k5)),
                         mul9(C::b6, k6)));
 }
@@ -189,7 +190,7 @@ __device__ __forceinline__ Vec9 scott_step_rolled(const F& f, const Vec9& s, flo
         for (int i = 0; i < 4; ++i) slot[i] = slot[i + 1];
         slot[4] = zero;
     }
-    err = norm(e);
+    err = fmaf(e.x, e.x, fmaf(e.y, e.y, e.z * e.z));  // squared (fast arithmetic)
     return add9(s, sol);
 }
 
@@ -218,16 +219,36 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
         return;
     }
     const double len_lim = pr.len_ratio * (double)(f.d.nx + f.d.ny + f.d.nz);
+    // fast arithmetic: the controller in the log domain (no divide, exact
+    // power or square root per step), the step limits narrowed to float
+    // (the same clamps, as StepLimits argues), the length in Kahan-
+    // compensated float (FP64 adds are slow on this GPU)
+    typedef typename std::conditional<EXACT, double, float>::type len_t;
+    const float h_max_f = (float)pr.h_max, h_min_f = (float)pr.h_min, reject_f = (float)pr.reject_factor;
+    const len_t len_lim_t = (len_t)len_lim;
     const float3 b0 = sample<EXACT>(f, p0, true);
     const float nb0 = norm(sample<EXACT>(f, p0, false));
     ns += 2;
     const float tol = (float)(pr.tol * (double)tol_coef);
+    const float ltol = EXACT ? 0.f : 0.2f * log2f(tol * (float)(1.0 / 11.09));
     float3 v0 = v3(b0.y, -b0.x, 0.f);
     v0 = unit_rsq<EXACT>(v0 - dot(v0, b0) * b0);
     float3 u0 = v3(b0.y * v0.z - b0.z * v0.y, b0.z * v0.x - b0.x * v0.z, b0.x * v0.y - b0.y * v0.x);
     u0 = unit_rsq<EXACT>(u0);
     const bool z0 = (double)p0.z < 1e-6;
-    double len = 0.0, tw = 0.0;
+    len_t len = 0;
+    float lc = 0.f;  // Kahan compensation of len (fast arithmetic)
+    double tw = 0.0;
+    auto len_add = [&](double x_exact, float x_fast) {
+        if (EXACT) {
+            len = len + (len_t)x_exact;
+        } else {
+            const float y = x_fast - lc;
+            const float t = (float)len + y;
+            lc = (t - (float)len) - y;
+            len = (len_t)t;
+        }
+    };
     long long steps = 0;
     Vec9 es = {p0, u0, v0}, ee = es;
     int fs = 0, fe = 0;
@@ -241,7 +262,7 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
         }
         h = fabsf(h);
         int flag = 0;
-        while ((flag == 0) & (len < len_lim) & (steps < pr.max_steps)) {
+        while ((flag == 0) & (len < len_lim_t) & (steps < pr.max_steps)) {
             float err;
             Vec9 b;
             // the rolled stages pay for the central differences' seven
@@ -250,18 +271,28 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
             // against 3.8 rolled)
             if constexpr (EXACT || GRAD == GRAD_ANALYTIC) b = scott_step<EXACT, GRAD>(f, a, h * (float)sgn, err, ns);
             else b = scott_step_rolled<GRAD>(f, a, h * (float)sgn, err, ns);
-            float scale;
-            if (EXACT) scale = pow_cr((float)((double)(tol / err) / 11.09), 0.2f);
-            else scale = exp2f(0.2f * __log2f(tol / err * (float)(1.0 / 11.09)));
-            if ((double)scale < 0.618) {
-                h = (float)((double)h * pr.reject_factor);
-                continue;
+            if (EXACT) {
+                const float scale = pow_cr((float)((double)(tol / err) / 11.09), 0.2f);
+                if ((double)scale < 0.618) {
+                    h = (float)((double)h * pr.reject_factor);
+                    continue;
+                }
+                h = h * scale;
+                if ((double)h > pr.h_max) h = (float)pr.h_max;
+                if ((double)h < pr.h_min) h = (float)pr.h_min;
+            } else {
+                // (tol / (11.09 err))^0.2 = 2^(0.2 log2(tol / 11.09) - 0.1 log2(err^2))
+                const float scale = ex2_approx(fmaf(-0.1f, lg2_approx(err), ltol));
+                if (scale < 0.618f) {
+                    h = h * reject_f;
+                    continue;
+                }
+                h = h * scale;
+                if (h > h_max_f) h = h_max_f;
+                if (h < h_min_f) h = h_min_f;
             }
-            h = h * scale;
-            if ((double)h > pr.h_max) h = (float)pr.h_max;
-            if ((double)h < pr.h_min) h = (float)pr.h_min;
-            const float dl = norm(b.p - a.p);
-            len = len + (double)dl;
+            const float dl = EXACT ? norm(b.p - a.p) : norm_fast(b.p - a.p);
+            len_add((double)dl, dl);
             float td = 0.f;
             float3 bp1 = v3(0.f, 0.f, 0.f);
             if (TWIST && tw_on) {
@@ -273,7 +304,7 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
             }
             flag = box_flag(f.d, b.p);
             if (flag > 0) {
-                len = len - (double)dl;
+                len_add(-(double)dl, -dl);
                 if (TWIST && tw_on) tw = tw - (double)td / 4.0 / kRefPi * (double)dl;
                 if (flag <= 6) {
                     const int d = (flag - 1) / 2;
@@ -298,7 +329,8 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
                             ua = sample<EXACT>(f, a.p, true);
                             ns += 1;
                         }
-                        len = len + (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(ua, d)));
+                        len_add((double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(ua, d))),
+                                fabsf(qmid - q1) / (1e-4f + fabsf(comp(ua, d))));
                     } else {
                         e = a;
                     }
