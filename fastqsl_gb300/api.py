@@ -585,7 +585,9 @@ class PlaneQBatch:
     u, v (unit plane axes: columns along u, rows along v), spacing, n0, n1,
     nplanes and optionally s_len (0.25), tol_coef (1.0).  tile: the seed tile
     of the trace order (None: seed order).  blocks_per_sm > 0: the batched
-    traces keep at most that many resident blocks per SM."""
+    traces keep at most that many resident blocks per SM.  The object owns
+    the workspace and the pinned staging buffer its queued work reads: keep
+    it alive until that work has completed (an event after run_post)."""
 
     def __init__(self, jobs, device="cuda", tile=(8, 8), stream=None, blocks_per_sm=0):
         lib = _lib.load()
