@@ -287,7 +287,7 @@ def trace_stretch(Bx, By, Bz, coords, xs, ys, zs, params: TraceParams | None = N
     uniform-spacing formula instead of the search.  occupancy: resident-block
     variant of the fast kernels (4, 5 or 6 blocks per SM; 0 or 7-10 take the
     default, 5).
-    Fast arithmetic traces an interleaved float4 copy of the nodes and finds
+    Fast arithmetic traces a copy of the nodes as x-pair records and finds
     cells through per-axis search tables, both built for the launch; the
     results equal the drop-in's bit for bit.  Defaults to the reference
     stretched kernel's settings (TraceBlineAdaptiveStretch.cu)."""

@@ -364,7 +364,8 @@ int qsl_trace_all_bline_stretch(int arith, const float *Bx, const float *By, con
  * default).  The call allocates, stream-ordered on `stream`
  * (cudaMallocAsync, freed after the launch), a device copy of the
  * coordinates (copied from the host arrays before the call returns) and, in
- * fast arithmetic, an interleaved float4 copy of the nodes (16 B per node)
+ * fast arithmetic, a copy of the nodes as x-pair records (node o and o + 1
+ * as two float4, 32 B per node; fewer than 2^31 nodes, else the arrays)
  * and, for the search, per-axis search tables (144 B per cell of each axis);
  * the outputs equal the drop-in's (fast arithmetic) bit for bit. */
 int qsl_trace_stretch(const float *Bx, const float *By, const float *Bz, int nx, int ny, int nz,
