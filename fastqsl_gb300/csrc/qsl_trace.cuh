@@ -248,6 +248,35 @@ __device__ __noinline__ float3 step_rk4_normal(const F f, float3 p, float h, int
     return p + c * (((k1 + 2.f * k2) + 2.f * k3) + k4);
 }
 
+// The same boundary RK4 inlined, its four stages in a rolled loop, for the
+// stretched-grid stores: the out-of-line form takes the store view by value,
+// and for their large views (coordinate arrays, per-axis constants, search
+// tables) the caller then keeps a copy of the view in local memory, which
+// the hot loop reads too.  The same operations in the same order.
+template <bool EXACT, class F>
+__device__ __forceinline__ float3 step_rk4_normal_rolled(const F& f, float3 p, float h, int d) {
+    float3 k1 = v3(0.f, 0.f, 0.f), k2 = k1, k3 = k1, k4 = k1, q = p;
+#pragma unroll 1
+    for (int st = 0; st < 4; ++st) {
+        const float3 b = sample<EXACT>(f, q, true);
+        const float3 k = b / comp(b, d);
+        if (st == 0) {
+            k1 = k;
+            q = p + (h * k1) / 2.f;
+        } else if (st == 1) {
+            k2 = k;
+            q = p + (h * k2) / 2.f;
+        } else if (st == 2) {
+            k3 = k;
+            q = p + h * k3;
+        } else {
+            k4 = k;
+        }
+    }
+    const float c = EXACT ? (float)(1.0 / 6.0 * (double)h) : h * (1.f / 6.f);
+    return p + c * (((k1 + 2.f * k2) + 2.f * k3) + k4);
+}
+
 // Boundary classification (checkFlag, TraceBlineAdaptive.cu:309-331).
 __device__ __forceinline__ int box_flag(const Dims& n, float3 p) {
     const float X = (float)(n.nx - 1), Y = (float)(n.ny - 1), Z = (float)(n.nz - 1);
@@ -659,7 +688,8 @@ __device__ __forceinline__ bool lane_move(const F& f, const TraceJob<F>& J, Lane
                     L.out.y = (L.p.y * (q2 - qmid) + p2.y * (qmid - q1)) / (q2 - q1);
                     L.out.z = (L.p.z * (q2 - qmid) + p2.z * (qmid - q1)) / (q2 - q1);
                 } else {
-                    L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d);
+                    if constexpr (RolledStages<F>::value) L.out = step_rk4_normal_rolled<EXACT>(f, L.p, qmid - q1, d);
+                    else L.out = step_rk4_normal<EXACT>(f, L.p, qmid - q1, d);
                     ns += 4;
                 }
                 len_add(L, (double)fabsf(qmid - q1) / (1e-4 + (double)fabsf(comp(u1, d))),
