@@ -449,6 +449,7 @@ class QMapPlan:
         self.order = tile_order(self.nplanes, self.n0, self.n1, tile[0], tile[1], device) if tile else None
         self.main = alloc_trace_outputs(self.n, device)
         self.Q = torch.empty((self.nplanes, self.n0 - 2, self.n1 - 2), dtype=torch.float64, device=device)
+        self._side = None  # side stream of the Q assembly (created at the first run)
         self.queue = torch.zeros(2, dtype=torch.int64, device=device)
         self.samples_buf = torch.zeros(2, dtype=torch.int64, device=device)  # main, pseudo-line trace
         if pseudo:
@@ -520,11 +521,21 @@ class QMapPlan:
             kernel_events[1].record(ev_stream)
         jac = (1.0 / (2.0 * float(stride))) ** 4.0
         cd = (ctypes.c_float * 3)(*[float(c) for c in cross_dir])
-        _lib.check(lib.qsl_qcalc_plane(ptr(m["end_x"]), ptr(m["end_y"]), ptr(m["end_z"]), ptr(m["flag_end"]),
-                                       ptr(m["start_x"]), ptr(m["start_y"]), ptr(m["start_z"]), ptr(m["flag_start"]),
-                                       ptr(m["B_start_z"]), ptr(m["B_end_z"]), ptr(m["B_this_x"]),
-                                       ptr(m["B_this_y"]), ptr(m["B_this_z"]), self.n0, self.n1, self.nplanes, jac,
-                                       cd, None, ptr(self.Q), st), "qsl_qcalc_plane")
+        def qcalc(qst):
+            _lib.check(lib.qsl_qcalc_plane(ptr(m["end_x"]), ptr(m["end_y"]), ptr(m["end_z"]), ptr(m["flag_end"]),
+                                           ptr(m["start_x"]), ptr(m["start_y"]), ptr(m["start_z"]),
+                                           ptr(m["flag_start"]), ptr(m["B_start_z"]), ptr(m["B_end_z"]),
+                                           ptr(m["B_this_x"]), ptr(m["B_this_y"]), ptr(m["B_this_z"]), self.n0,
+                                           self.n1, self.nplanes, jac, cd, None, ptr(self.Q), qst), "qsl_qcalc_plane")
+
+        # with pseudo-lines the Q assembly of all pixels runs on a side stream
+        # beside the pseudo-line trace (both depend only on the main trace and
+        # the compaction), launched after it so that the trace's blocks are
+        # dispatched first and the assembly fills the SMs its few long lines
+        # leave idle; the merge waits for it
+        overlap = self.pseudo and not self.hybrid and (stream is None or isinstance(stream, torch.cuda.Stream))
+        if not overlap:
+            qcalc(st)
         if self.hybrid:
             return self._hybrid(field, xs, ys, zs, params, s_len, tol_coef, scott_params, scott_grad, stream, st)
         if not self.pseudo:
@@ -536,16 +547,28 @@ class QMapPlan:
                                             ptr(self.bz0e), ptr(self.pix), ptr(self.count), ptr(self.work),
                                             self.work_bytes, st), "qsl_cook_pseudo_line")
         cnt_seeds = self.count[1:2]
+        if overlap:
+            fork = torch.cuda.Event()
+            fork.record(ev_stream)
         trace(field, self.cut[0], self.cut[1], self.cut[2], params, s_len, tol_coef * pseudo_tol_factor, cross_dir,
               out=self.sub, n=4 * self.max_pix, n_dev=cnt_seeds, schedule="static",
               occupancy=self.occupancy_for(field),
               samples=self.samples_buf[1:2] if count_samples else None, queue=self.queue[1:2],
               stream=stream)
+        if overlap:
+            if self._side is None:
+                self._side = torch.cuda.Stream(device=self.Q.device)
+            self._side.wait_event(fork)
+            qcalc(self._side.cuda_stream)
+            qdone = torch.cuda.Event()
+            qdone.record(self._side)
         s = self.sub
         _lib.check(lib.qsl_qcut(ptr(s["start_x"]), ptr(s["start_y"]), ptr(s["start_z"]), ptr(s["flag_start"]),
                                 ptr(s["end_x"]), ptr(s["end_y"]), ptr(s["end_z"]), ptr(s["flag_end"]),
                                 ptr(self.bz0s), ptr(self.bz0e), 0, ptr(self.count[0:1]), self.max_pix, jac, None,
                                 ptr(self.qcut), st), "qsl_qcut")
+        if overlap:
+            ev_stream.wait_event(qdone)
         _lib.check(lib.qsl_qmerge(ptr(self.pix), None, ptr(self.qcut), 0, ptr(self.count[0:1]), self.max_pix,
                                   self.n0, self.n1, None, ptr(self.Q), st), "qsl_qmerge")
         return self.Q
