@@ -552,9 +552,10 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     // one stream-ordered buffer for the launch: the coordinates, then (fast
     // arithmetic) the x-pair node records and the search tables
     const int64_t tcells = (packed_path && !uni) ? cells : 0;
+    const int64_t srec_len = (tcells + 1) & ~(int64_t)1;  // even: sbin starts on a 32-byte boundary
     const int64_t ncoord = (int64_t)nx + ny + nz;
     const size_t coord_bytes = ((size_t)ncoord * sizeof(float) + 255) / 256 * 256;
-    const size_t bytes = coord_bytes + (packed_path ? (size_t)(2 * nodes + tcells) * sizeof(float4) +
+    const size_t bytes = coord_bytes + (packed_path ? (size_t)(2 * nodes + srec_len) * sizeof(float4) +
                                                           (size_t)tcells * STRETCH_BINS_PER_CELL * 2 * sizeof(float4)
                                                     : 0);
     char* buf = nullptr;
@@ -609,11 +610,12 @@ int qsl_trace_stretch(const float* Bx, const float* By, const float* Bz, int nx,
     // fast arithmetic: the nodes interleaved into x-pair records for the
     // launch (node o and o + 1 as two float4: one 32-byte load per corner
     // pair; the same values), followed, for the search, by its tables (a
-    // 16-byte record per cell, two 16-byte records per bin); the uniform
-    // formula needs none
+    // 16-byte record per cell, padded to an even count, then two 16-byte
+    // records per bin, read as one 32-byte load); the uniform formula needs
+    // none
     float4* b4 = reinterpret_cast<float4*>(buf + coord_bytes);
     float4* srec = uni ? nullptr : b4 + 2 * nodes;
-    float4* sbin = uni ? nullptr : srec + cells;
+    float4* sbin = uni ? nullptr : srec + srec_len;
     e = launch_pack_f4x2(Bx, By, Bz, Dims{nx, ny, nz}, b4, st);
     if (e == cudaSuccess && !uni) e = launch_stretch_tables(x_arr, y_arr, z_arr, Dims{nx, ny, nz}, srec, sbin, st);
     if (e != cudaSuccess) {

@@ -726,7 +726,8 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
 // j with a[j] < c <= a[j+1] (or the range's low end) before srec[j] is
 // read.  The same cell, coordinate and width as stretch_bisect followed by
 // the two coordinate loads, for c clamped as stretch_locate clamps it.
-template <int M>
+// WIDE: the bin's two records as one 32-byte load (sbin is 32-byte aligned).
+template <int M, bool WIDE>
 __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, float c, float a0, float binv,
                                              float& ai, float& di) {
     const float* a = f.axis(k);
@@ -736,7 +737,16 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, f
     int b = __float2int_rz((c - a0) * binv);
     b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
     const float4* sb = f.sbin + 2 * (STRETCH_BINS_PER_CELL * c0 + b);
-    const float4 A = __ldg(sb), B = __ldg(sb + 1);
+    float4 A, B;
+    if constexpr (WIDE) {
+        unsigned w[8];
+        ldg_v8(sb, w);
+        A = make_float4(__uint_as_float(w[0]), __uint_as_float(w[1]), __uint_as_float(w[2]), __uint_as_float(w[3]));
+        B = make_float4(__uint_as_float(w[4]), __uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7]));
+    } else {
+        A = __ldg(sb);
+        B = __ldg(sb + 1);
+    }
     if (__float_as_int(B.w) == 0) {
         // one or two intervals: the records of both and the node between
         const bool up = c > A.x;
@@ -760,7 +770,7 @@ __device__ __forceinline__ int stretch_table(const FieldStretchT<M>& f, int k, f
 // (offsets applied in double and narrowed, once per kernel: clo, chi), then
 // the index and r = (c - a[i]) / (a[i+1] - a[i])  (Interp3dxyzn, :100-122);
 // the fast arithmetic divides with the hardware reciprocal (div_fast).
-template <bool EXACT, int M>
+template <bool EXACT, bool WIDE, int M>
 __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k, float c, float a0, float an,
                                                float clo, float chi, float du, float binv, int& i, float& r) {
     const float* a = f.axis(k);
@@ -769,7 +779,7 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
     c = (c < an) ? c : chi;
     float ai, di;
     if constexpr (stretch_search_mode<M>() == 1) {
-        i = stretch_table(f, k, c, a0, binv, ai, di);
+        i = stretch_table<M, WIDE>(f, k, c, a0, binv, ai, di);
     } else {
         if constexpr (stretch_search_mode<M>() == 2) i = stretch_uni(c, n, a0, du);
         else i = stretch_bisect(c, n, a);
@@ -779,15 +789,16 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
     r = EXACT ? (c - ai) / di : div_fast(__fsub_rn(c, ai), di);
 }
 
-// WIDE: the packed stores' 32-byte x-pair records as one 32-byte load (code
-// inlined into kernels only; see sample_h8c) or two 16-byte loads.
+// WIDE: the packed stores' 32-byte x-pair records and search bins as one
+// 32-byte load each (code inlined into kernels only; see sample_h8c) or two
+// 16-byte loads.
 template <bool EXACT, int M, bool WIDE = true>
 __device__ __forceinline__ float3 sample_stretch(const FieldStretchT<M>& f, float3 p, bool unit) {
     int ix, iy, iz;
     float rx, ry, rz;
-    stretch_locate<EXACT>(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, f.sbinv.x, ix, rx);
-    stretch_locate<EXACT>(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, f.sbinv.y, iy, ry);
-    stretch_locate<EXACT>(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, f.sbinv.z, iz, rz);
+    stretch_locate<EXACT, WIDE>(f, 0, p.x, f.lo.x, f.hi.x, f.clo.x, f.chi.x, f.us.x, f.sbinv.x, ix, rx);
+    stretch_locate<EXACT, WIDE>(f, 1, p.y, f.lo.y, f.hi.y, f.clo.y, f.chi.y, f.us.y, f.sbinv.y, iy, ry);
+    stretch_locate<EXACT, WIDE>(f, 2, p.z, f.lo.z, f.hi.z, f.clo.z, f.chi.z, f.us.z, f.sbinv.z, iz, rz);
     float3 r;
     if constexpr (EXACT) {
         float w[8];
