@@ -597,11 +597,12 @@ QMapPlan._hybrid = _hybrid_impl
 
 class PlaneQBatch:
     """Q maps of many plane jobs as one native batch (qsl_qmap_batch_*): the
-    seed grids, tile orders, job tables, batched traces and per-job Q
+    seed grids, tile orders, job tables, batched traces and the batched Q
     assembly are laid out in one workspace allocation and queued by the C++
-    library, a few launches per job and no per-array host bookkeeping.  The
-    Q maps equal QBatch's on the same jobs bit for bit (the same kernels in
-    the same order).  Reference workflow per job: demo/Q_RKF45CuPy.ipynb
+    library: two launches per job (seed grid, tile order), then the batch's
+    traces and six Q-assembly launches for all jobs, and no per-array host
+    bookkeeping.  The Q maps equal QBatch's on the same jobs bit for bit (the
+    same trace kernels; the Q-assembly kernels' arithmetic per pixel).  Reference workflow per job: demo/Q_RKF45CuPy.ipynb
     cells 7-11.
 
     jobs: list of dicts with keys field (FieldStore), params, center, normal,

@@ -11,6 +11,8 @@
 //   k_qcut          — Q of each compacted pixel from its four pseudo-lines
 //                     (demo/Q_RKF45CuPy.ipynb cell 10).
 //   k_qmerge        — writes the pseudo-line Q into the map (cell 11).
+//   k_*_jobs        — the same kernels over a table of plane jobs, one
+//                     launch each for a whole batch (QPostJob).
 //
 // Compiled with -fmad=false so the FP32 form rounds exactly as the
 // reference's array expressions do.
@@ -33,14 +35,14 @@ __device__ __forceinline__ void face_xy(float x, float y, float z, int flag, T& 
 }
 
 
+// Q of the interior pixels first, first + stride, ... of one job.
 template <bool F64>
-__global__ void k_qcalc_plane(const QPlaneArgs a) {
+__device__ __forceinline__ void qcalc_range(const QPlaneArgs& a, long long first, long long stride) {
     typedef typename std::conditional<F64, double, float>::type T;
     const long long m0 = a.n0 - 2, m1 = a.n1 - 2;
     const long long per = m0 * m1;
     const long long total = per * a.nplanes;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
+    for (long long t = first; t < total; t += stride) {
         const long long pl = t / per;
         const long long r = t - pl * per;
         const int i = (int)(r / m1) + 1, j = (int)(r % m1) + 1;
@@ -88,6 +90,11 @@ __global__ void k_qcalc_plane(const QPlaneArgs a) {
     }
 }
 
+template <bool F64>
+__global__ void k_qcalc_plane(const QPlaneArgs a) {
+    qcalc_range<F64>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
 // ---- ordered compaction of flagged pixels (tile = 1024 pixels) ----
 constexpr int kTile = 1024;
 
@@ -100,9 +107,10 @@ __device__ __forceinline__ bool pixel_selected(const int* bflag, long long p, in
     return i >= 1 && i <= n0 - 2 && j >= 1 && j <= n1 - 2;
 }
 
-__global__ void __launch_bounds__(256) k_flag_count(const int* bflag, long long n, int n0, int n1, int interior_only,
-                                                    int* tile_count) {
-    const long long t0 = (long long)blockIdx.x * kTile;
+// Selected pixels of one tile, counted by a block of 256 threads.
+__device__ __forceinline__ void flag_count_tile(const int* bflag, long long n, int n0, int n1, int interior_only,
+                                                long long tile, int* tile_count) {
+    const long long t0 = tile * kTile;
     int cnt = 0;
     for (int k = threadIdx.x; k < kTile; k += blockDim.x) {
         const long long p = t0 + k;
@@ -115,13 +123,18 @@ __global__ void __launch_bounds__(256) k_flag_count(const int* bflag, long long 
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) tile_count[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) tile_count[tile] = red[0];
+}
+
+__global__ void __launch_bounds__(256) k_flag_count(const int* bflag, long long n, int n0, int n1, int interior_only,
+                                                    int* tile_count) {
+    flag_count_tile(bflag, n, n0, n1, interior_only, blockIdx.x, tile_count);
 }
 
 // Exclusive scan of the tile counts by one block; writes the grand total
 // (total[0]) and the number of pseudo-line seeds (total[1] = 4 * total[0]).
-__global__ void __launch_bounds__(1024) k_tile_scan(const int* tile_count, long long ntiles, long long* tile_off,
-                                                     unsigned long long* total) {
+__device__ __forceinline__ void tile_scan_block(const int* tile_count, long long ntiles, long long* tile_off,
+                                                unsigned long long* total) {
     __shared__ long long carry;
     __shared__ long long warp_sum[32];
     if (threadIdx.x == 0) carry = 0;
@@ -158,9 +171,16 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const int* tile_count, long 
     }
 }
 
+__global__ void __launch_bounds__(1024) k_tile_scan(const int* tile_count, long long ntiles, long long* tile_off,
+                                                     unsigned long long* total) {
+    tile_scan_block(tile_count, ntiles, tile_off, total);
+}
 
-__global__ void __launch_bounds__(kTile) k_cook_write(const CookArgs a) {
-    const long long p = (long long)blockIdx.x * kTile + threadIdx.x;
+
+// The selected pixels of one tile and their pseudo-line seeds, written in
+// pixel order by a block of kTile threads.
+__device__ __forceinline__ void cook_write_tile(const CookArgs& a, long long tile) {
+    const long long p = tile * kTile + threadIdx.x;
     const bool sel = p < a.n && pixel_selected(a.bflag, p, a.n0, a.n1, a.interior_only);
     __shared__ int wcount[kTile / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -172,7 +192,7 @@ __global__ void __launch_bounds__(kTile) k_cook_write(const CookArgs a) {
     for (int w = 0; w < warp; ++w) before += wcount[w];
     unsigned lt;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-    const long long k = a.tile_off[blockIdx.x] + before + __popc(m & lt);
+    const long long k = a.tile_off[tile] + before + __popc(m & lt);
     const float x = a.xs[p], y = a.ys[p], z = a.zs[p];
     const int f = a.fs[p];
     const int d = (f >= 1 && f <= 6) ? (f - 1) / 2 : -1;
@@ -192,13 +212,14 @@ __global__ void __launch_bounds__(kTile) k_cook_write(const CookArgs a) {
     if (a.pix) a.pix[k] = p;
 }
 
+__global__ void __launch_bounds__(kTile) k_cook_write(const CookArgs a) { cook_write_tile(a, blockIdx.x); }
+
 
 template <bool F64>
-__global__ void k_qcut(const QcutArgs a) {
+__device__ __forceinline__ void qcut_range(const QcutArgs& a, long long first, long long stride) {
     typedef typename std::conditional<F64, double, float>::type T;
     const long long cnt = a.count_dev ? (long long)*a.count_dev : a.count;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < cnt;
-         k += (long long)gridDim.x * blockDim.x) {
+    for (long long k = first; k < cnt; k += stride) {
         T X1[4], Y1[4], X2[4], Y2[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -224,20 +245,92 @@ __global__ void k_qcut(const QcutArgs a) {
     }
 }
 
+template <bool F64>
+__global__ void k_qcut(const QcutArgs a) {
+    qcut_range<F64>(a, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
 // Q_final[plane, i-1, j-1] = Qcut[k] for each compacted interior pixel.
 template <class TQ, class TC>
-__global__ void k_qmerge(const long long* pix, const TC* qcut, const unsigned long long* count_dev, long long count,
-                         int n0, int n1, TQ* qfinal) {
-    const long long cnt = count_dev ? (long long)*count_dev : count;
+__device__ __forceinline__ void qmerge_range(const long long* pix, const TC* qcut, long long cnt, int n0, int n1,
+                                             TQ* qfinal, long long first, long long stride) {
     const long long per = (long long)n0 * n1, per2 = (long long)(n0 - 2) * (n1 - 2);
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < cnt;
-         k += (long long)gridDim.x * blockDim.x) {
+    for (long long k = first; k < cnt; k += stride) {
         const long long p = pix[k];
         const long long pl = p / per, r = p % per;
         const int i = (int)(r / n1), j = (int)(r % n1);
         if (i >= 1 && i <= n0 - 2 && j >= 1 && j <= n1 - 2)
             qfinal[pl * per2 + (long long)(i - 1) * (n1 - 2) + (j - 1)] = (TQ)qcut[k];
     }
+}
+
+template <class TQ, class TC>
+__global__ void k_qmerge(const long long* pix, const TC* qcut, const unsigned long long* count_dev, long long count,
+                         int n0, int n1, TQ* qfinal) {
+    const long long cnt = count_dev ? (long long)*count_dev : count;
+    qmerge_range(pix, qcut, cnt, n0, n1, qfinal, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
+}
+
+// ---- batched forms: one launch per kernel for every job of a table ----
+// The job of block b of a grid whose begin column is `begin` (njobs + 1
+// nondecreasing entries): the last j with begin[j] <= b.
+__device__ __forceinline__ int post_job(const long long* begin, int njobs, long long b) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (begin[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_qcalc_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long b = blockIdx.x;
+    const int j = post_job(begin, njobs, b);
+    const QPlaneArgs a = jobs[j].q;
+    qcalc_range<true>(a, (b - begin[j]) * blockDim.x + threadIdx.x, jobs[j].qblocks * blockDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_flag_count_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long* tb = begin + (njobs + 1);
+    const long long b = blockIdx.x;
+    const int j = post_job(tb, njobs, b);
+    const CookArgs& c = jobs[j].c;
+    flag_count_tile(c.bflag, c.n, c.n0, c.n1, c.interior_only, b - tb[j], jobs[j].tile_count);
+}
+
+// one block per job
+__global__ void __launch_bounds__(1024) k_tile_scan_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long* tb = begin + (njobs + 1);
+    const int j = blockIdx.x;
+    tile_scan_block(jobs[j].tile_count, tb[j + 1] - tb[j], jobs[j].tile_off, jobs[j].total);
+}
+
+__global__ void __launch_bounds__(kTile) k_cook_write_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long* tb = begin + (njobs + 1);
+    const long long b = blockIdx.x;
+    const int j = post_job(tb, njobs, b);
+    const CookArgs a = jobs[j].c;
+    cook_write_tile(a, b - tb[j]);
+}
+
+__global__ void __launch_bounds__(256) k_qcut_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long* cb = begin + 2 * (njobs + 1);
+    const long long b = blockIdx.x;
+    const int j = post_job(cb, njobs, b);
+    const QcutArgs a = jobs[j].k;
+    qcut_range<true>(a, (b - cb[j]) * blockDim.x + threadIdx.x, jobs[j].cblocks * blockDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_qmerge_jobs(const QPostJob* jobs, const long long* begin, int njobs) {
+    const long long* cb = begin + 2 * (njobs + 1);
+    const long long b = blockIdx.x;
+    const int j = post_job(cb, njobs, b);
+    const QPostJob& J = jobs[j];
+    const long long cnt = (long long)*J.total;
+    qmerge_range(J.c.pix, (const double*)J.k.q64, cnt, J.c.n0, J.c.n1, J.q.q64, (b - cb[j]) * blockDim.x + threadIdx.x,
+                 J.cblocks * blockDim.x);
 }
 
 // ---- host launchers ----
@@ -292,6 +385,29 @@ cudaError_t launch_qmerge_f64(const long long* pix, const double* qcut, const un
                               long long count, long long max_count, int n0, int n1, double* qfinal, cudaStream_t st) {
     if (max_count <= 0) return cudaSuccess;
     k_qmerge<double, double><<<grid_for(max_count, 256), 256, 0, st>>>(pix, qcut, count_dev, count, n0, n1, qfinal);
+    return cudaGetLastError();
+}
+
+long long qcalc_blocks(long long pixels) { return pixels > 0 ? (long long)grid_for(pixels, 256) : 0; }
+
+cudaError_t launch_qpost_assemble(const QPostJob* jobs, const long long* begin, int njobs, const long long grid[3],
+                                  cudaStream_t st) {
+    if (njobs < 1) return cudaSuccess;
+    for (int g = 0; g < 3; ++g)
+        if (grid[g] < 1 || grid[g] > 0x7fffffffLL) return cudaErrorInvalidValue;
+    k_qcalc_jobs<<<(unsigned)grid[0], 256, 0, st>>>(jobs, begin, njobs);
+    k_flag_count_jobs<<<(unsigned)grid[1], 256, 0, st>>>(jobs, begin, njobs);
+    k_tile_scan_jobs<<<(unsigned)njobs, 1024, 0, st>>>(jobs, begin, njobs);
+    k_cook_write_jobs<<<(unsigned)grid[1], kTile, 0, st>>>(jobs, begin, njobs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_qpost_pseudo(const QPostJob* jobs, const long long* begin, int njobs, const long long grid[3],
+                                cudaStream_t st) {
+    if (njobs < 1) return cudaSuccess;
+    if (grid[2] < 1 || grid[2] > 0x7fffffffLL) return cudaErrorInvalidValue;
+    k_qcut_jobs<<<(unsigned)grid[2], 256, 0, st>>>(jobs, begin, njobs);
+    k_qmerge_jobs<<<(unsigned)grid[2], 256, 0, st>>>(jobs, begin, njobs);
     return cudaGetLastError();
 }
 

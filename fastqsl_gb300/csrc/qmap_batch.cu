@@ -2,10 +2,12 @@
 // many requests laid out in one caller-provided workspace and queued from C++
 // (seed grids, tile orders, the batched main trace or a window of it, Q
 // assembly, pseudo-line compaction, the batched pseudo-line trace, pseudo Q
-// and merge).  The same entry points, kernels and order as the Python
-// QBatch, so the Q maps are the same bit for bit; the host does per request
-// a few launches instead of building ~40 arrays and job records in Python.
-// No device allocation and no synchronisation.
+// and merge).  The trace kernels are the Python QBatch's; the Q assembly,
+// compaction, pseudo Q and merge run as one launch each for the whole batch
+// over a job table (QPostJob) with the per-job kernels' arithmetic, so the
+// Q maps are the same bit for bit.  The host does two launches per request
+// (seed grid, tile order) and one table copy instead of building ~40 arrays
+// and job records in Python.  No device allocation and no synchronisation.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -14,6 +16,7 @@
 #include <vector>
 
 #include "../../include/fastqsl_gb300.h"
+#include "qassembly.h"
 
 namespace qsl {
 int set_error(int code, const char* msg);
@@ -109,8 +112,10 @@ struct qsl_qmap_batch {
     std::vector<qsl_qmap_job> jobs;
     std::vector<JobLayout> lay;
     char* ws;
-    int64_t main_table, sub_table;  // workspace offsets of the two job tables
+    int64_t main_table, sub_table;  // workspace offsets of the two trace job tables
+    int64_t post_table;             // and of the Q-assembly table (QPostJob[njobs], then the begin columns)
     qsl_batch_info main_info, sub_info;
+    long long post_grid[qsl::kPostGrids];
 };
 
 namespace {
@@ -139,6 +144,78 @@ void job_lists(const qsl_qmap_batch& B, std::vector<qsl_batch_job>& mj, std::vec
         mj[k] = a;
         sj[k] = s;
     }
+}
+
+// Bytes of the Q-assembly table of njobs jobs.
+int64_t post_bytes(int njobs) {
+    return up((int64_t)njobs * (int64_t)sizeof(qsl::QPostJob) + qsl::kPostGrids * (int64_t)(njobs + 1) * 8);
+}
+
+// The Q-assembly table of a laid-out batch, written to dst (post_bytes), and
+// the three grid sizes.  Each job's arguments are those the per-job entries
+// (qsl_qcalc_plane, qsl_cook_pseudo_line, qsl_qcut, qsl_qmerge) build from
+// the same arrays.
+int post_table(const qsl_qmap_batch& B, char* dst, long long grid[qsl::kPostGrids]) {
+    using qsl::QPostJob;
+    const int nj = B.njobs;
+    QPostJob* T = reinterpret_cast<QPostJob*>(dst);
+    long long* begin = reinterpret_cast<long long*>(dst + (size_t)nj * sizeof(QPostJob));
+    for (int g = 0; g < qsl::kPostGrids; ++g) grid[g] = 0;
+    char* w = B.ws;
+    for (int k = 0; k < nj; ++k) {
+        const qsl_qmap_job& j = B.jobs[k];
+        const JobLayout& L = B.lay[k];
+        const double jac = pow(1.0 / (2.0 * j.spacing), 4.0);
+        auto F = [&](const int64_t* o, int i) { return (const float*)(w + o[i]); };
+        auto I = [&](const int64_t* o, int i) { return (const int*)(w + o[i]); };
+        QPostJob P;
+        memset(&P, 0, sizeof(P));
+        // qsl_qcalc_plane(end xyz flag, start xyz flag, B_start z, B_end z, B_this xyz, ..., Q64)
+        qsl::QPlaneArgs& q = P.q;
+        q.xe = F(L.main, 4); q.ye = F(L.main, 5); q.ze = F(L.main, 6); q.fe = I(L.main, 7);
+        q.xs = F(L.main, 0); q.ys = F(L.main, 1); q.zs = F(L.main, 2); q.fs = I(L.main, 3);
+        q.bz_in = F(L.main, 14); q.bz_out = F(L.main, 17);
+        q.bx0 = F(L.main, 8); q.by0 = F(L.main, 9); q.bz0 = F(L.main, 10);
+        q.cx = (float)j.normal[0]; q.cy = (float)j.normal[1]; q.cz = (float)j.normal[2];
+        q.n0 = j.n0; q.n1 = j.n1; q.nplanes = j.nplanes;
+        q.k32 = (float)jac; q.k64 = jac;
+        q.q32 = nullptr; q.q64 = (double*)(w + L.q);
+        // qsl_cook_pseudo_line(B_flag, start xyz flag, B_start z, B_end z, n, n0, n1, interior_only = 1, ...)
+        P.tile_off = (long long*)(w + L.work);
+        P.tile_count = (int*)(P.tile_off + qsl::cook_tiles(L.n));
+        P.total = (unsigned long long*)(w + L.count);
+        qsl::CookArgs& c = P.c;
+        c.bflag = I(L.main, 11);
+        c.xs = F(L.main, 0); c.ys = F(L.main, 1); c.zs = F(L.main, 2); c.fs = I(L.main, 3);
+        c.bz_in = F(L.main, 14); c.bz_out = F(L.main, 17);
+        c.n = L.n; c.n0 = j.n0; c.n1 = j.n1; c.interior_only = 1;
+        c.stride = (float)j.spacing;
+        c.tile_off = P.tile_off;
+        c.cx = (float*)(w + L.cut[0]); c.cy = (float*)(w + L.cut[1]); c.cz = (float*)(w + L.cut[2]);
+        c.bz0s = (float*)(w + L.bz0s); c.bz0e = (float*)(w + L.bz0e);
+        c.pix = (long long*)(w + L.pix);
+        // qsl_qcut(pseudo-line start xyz flag, end xyz flag, Bz0 start / end, count on the device, ...)
+        qsl::QcutArgs& kc = P.k;
+        kc.xs = F(L.sub, 0); kc.ys = F(L.sub, 1); kc.zs = F(L.sub, 2); kc.fs = I(L.sub, 3);
+        kc.xe = F(L.sub, 4); kc.ye = F(L.sub, 5); kc.ze = F(L.sub, 6); kc.fe = I(L.sub, 7);
+        kc.bz0s = c.bz0s; kc.bz0e = c.bz0e;
+        kc.count_dev = P.total; kc.count = 0;
+        kc.k32 = (float)jac; kc.k64 = jac;
+        kc.q32 = nullptr; kc.q64 = (double*)(w + L.qcut);
+        P.qblocks = qsl::qcalc_blocks(L.m);
+        P.cblocks = qsl::qcalc_blocks(L.m);
+        const long long sizes[qsl::kPostGrids] = {P.qblocks, qsl::cook_tiles(L.n), P.cblocks};
+        for (int g = 0; g < qsl::kPostGrids; ++g) {
+            begin[g * (nj + 1) + k] = grid[g];
+            grid[g] += sizes[g];
+        }
+        memcpy(T + k, &P, sizeof(P));
+    }
+    for (int g = 0; g < qsl::kPostGrids; ++g) {
+        begin[g * (nj + 1) + nj] = grid[g];
+        if (grid[g] > 0x7fffffffLL) return qsl::set_error(QSL_ERR_TOO_LARGE, "batch too large for one Q-assembly grid");
+    }
+    return QSL_OK;
 }
 
 int sizes(const qsl_qmap_job* jobs, int njobs, std::vector<JobLayout>* lay, int64_t* arrays_bytes,
@@ -185,8 +262,8 @@ int qsl_qmap_batch_size(const qsl_qmap_job* jobs, int njobs, int64_t* device_byt
     qsl_batch_info mi, si;
     const int rc = sizes(jobs, njobs, nullptr, &arrays, &mt, &st, &mi, &si);
     if (rc != QSL_OK) return rc;
-    *device_bytes = arrays + mt + st;
-    *host_bytes = mt + st;
+    *device_bytes = arrays + mt + st + post_bytes(njobs);
+    *host_bytes = mt + st + post_bytes(njobs);
     return QSL_OK;
 }
 
@@ -201,8 +278,9 @@ int qsl_qmap_batch_create(const qsl_qmap_job* jobs, int njobs, void* workspace, 
     qsl_batch_info mi, si;
     int rc = sizes(jobs, njobs, &lay, &arrays, &mt, &st, &mi, &si);
     if (rc != QSL_OK) return rc;
-    if (workspace_bytes < arrays + mt + st) return qsl::set_error(QSL_ERR_INVALID, "workspace too small");
-    if (host_bytes < mt + st) return qsl::set_error(QSL_ERR_INVALID, "host staging buffer too small");
+    const int64_t pt = post_bytes(njobs);
+    if (workspace_bytes < arrays + mt + st + pt) return qsl::set_error(QSL_ERR_INVALID, "workspace too small");
+    if (host_bytes < mt + st + pt) return qsl::set_error(QSL_ERR_INVALID, "host staging buffer too small");
     qsl_qmap_batch* B = new (std::nothrow) qsl_qmap_batch();
     if (!B) return qsl::set_error(QSL_ERR_NOMEM, "host allocation failed");
     B->njobs = njobs;
@@ -211,6 +289,7 @@ int qsl_qmap_batch_create(const qsl_qmap_job* jobs, int njobs, void* workspace, 
     B->ws = (char*)workspace;
     B->main_table = arrays;
     B->sub_table = arrays + mt;
+    B->post_table = arrays + mt + st;
     cudaStream_t s = (cudaStream_t)stream;
     // seed grids and tile orders, one launch each per job
     for (int k = 0; k < njobs && rc == QSL_OK; ++k) {
@@ -222,15 +301,16 @@ int qsl_qmap_batch_create(const qsl_qmap_job* jobs, int njobs, void* workspace, 
             rc = qsl_tile_order(j.nplanes, j.n0, j.n1, j.tile_y, j.tile_x, j.nplanes, (uint32_t*)(B->ws + L.order),
                                 stream);
     }
-    // the two job tables, serialised into the staging buffer and copied
+    // the three job tables, serialised into the staging buffer and copied
     std::vector<qsl_batch_job> mj, sj;
     if (rc == QSL_OK) {
         job_lists(*B, mj, sj);
         rc = qsl_batch_pack(mj.data(), njobs, host_staging, mt, &B->main_info);
     }
     if (rc == QSL_OK) rc = qsl_batch_pack(sj.data(), njobs, (char*)host_staging + mt, st, &B->sub_info);
+    if (rc == QSL_OK) rc = post_table(*B, (char*)host_staging + mt + st, B->post_grid);
     if (rc == QSL_OK) {
-        const cudaError_t e = cudaMemcpyAsync(B->ws + B->main_table, host_staging, (size_t)(mt + st),
+        const cudaError_t e = cudaMemcpyAsync(B->ws + B->main_table, host_staging, (size_t)(mt + st + pt),
                                               cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) rc = cuda_err(e);
     }
@@ -258,42 +338,19 @@ int qsl_qmap_batch_run_main(const qsl_qmap_batch_t* B, int64_t line_lo, int64_t 
 
 int qsl_qmap_batch_run_post(const qsl_qmap_batch_t* B, int max_blocks, int occupancy, qsl_stream_t stream) {
     if (!B) return qsl::set_error(QSL_ERR_INVALID, "null batch");
-    char* w = B->ws;
-    int rc = QSL_OK;
-    for (int k = 0; k < B->njobs && rc == QSL_OK; ++k) {
-        const qsl_qmap_job& j = B->jobs[k];
-        const JobLayout& L = B->lay[k];
-        const int64_t* o = L.main;
-        const double jac = pow(1.0 / (2.0 * j.spacing), 4.0);
-        const float cd[3] = {(float)j.normal[0], (float)j.normal[1], (float)j.normal[2]};
-        auto F = [&](int i) { return (const float*)(w + o[i]); };
-        auto I = [&](int i) { return (const int*)(w + o[i]); };
-        rc = qsl_qcalc_plane(F(4), F(5), F(6), I(7), F(0), F(1), F(2), I(3), F(14), F(17), F(8), F(9), F(10), j.n0,
-                             j.n1, j.nplanes, jac, cd, nullptr, (double*)(w + L.q), stream);
-        if (rc == QSL_OK)
-            rc = qsl_cook_pseudo_line(I(11), F(0), F(1), F(2), I(3), F(14), F(17), L.n, j.n0, j.n1, 1,
-                                      (float)j.spacing, (float*)(w + L.cut[0]), (float*)(w + L.cut[1]),
-                                      (float*)(w + L.cut[2]), (float*)(w + L.bz0s), (float*)(w + L.bz0e),
-                                      (int64_t*)(w + L.pix), (unsigned long long*)(w + L.count), w + L.work,
-                                      L.work_bytes, stream);
-    }
-    if (rc == QSL_OK)
-        rc = qsl_batch_run_window(w + B->sub_table, &B->sub_info, nullptr, 0, -1, max_blocks, occupancy, stream);
-    for (int k = 0; k < B->njobs && rc == QSL_OK; ++k) {
-        const qsl_qmap_job& j = B->jobs[k];
-        const JobLayout& L = B->lay[k];
-        const int64_t* o = L.sub;
-        const double jac = pow(1.0 / (2.0 * j.spacing), 4.0);
-        auto F = [&](int i) { return (const float*)(w + o[i]); };
-        auto I = [&](int i) { return (const int*)(w + o[i]); };
-        const unsigned long long* cnt = (const unsigned long long*)(w + L.count);
-        rc = qsl_qcut(F(0), F(1), F(2), I(3), F(4), F(5), F(6), I(7), (const float*)(w + L.bz0s),
-                      (const float*)(w + L.bz0e), 0, cnt, L.m, jac, nullptr, (double*)(w + L.qcut), stream);
-        if (rc == QSL_OK)
-            rc = qsl_qmerge((const int64_t*)(w + L.pix), nullptr, (const double*)(w + L.qcut), 0, cnt, L.m, j.n0,
-                            j.n1, nullptr, (double*)(w + L.q), stream);
-    }
-    return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const qsl::QPostJob* T = (const qsl::QPostJob*)(B->ws + B->post_table);
+    const long long* begin = (const long long*)(B->ws + B->post_table + (int64_t)B->njobs * sizeof(qsl::QPostJob));
+    // Q of every job, then the compaction of its flagged pixels into
+    // pseudo-line seeds
+    cudaError_t e = qsl::launch_qpost_assemble(T, begin, B->njobs, B->post_grid, s);
+    if (e != cudaSuccess) return cuda_err(e);
+    const int rc = qsl_batch_run_window(B->ws + B->sub_table, &B->sub_info, nullptr, 0, -1, max_blocks, occupancy,
+                                        stream);
+    if (rc != QSL_OK) return rc;
+    // Q of the pseudo-lines, merged into each map
+    e = qsl::launch_qpost_pseudo(T, begin, B->njobs, B->post_grid, s);
+    return e == cudaSuccess ? QSL_OK : cuda_err(e);
 }
 
 double* qsl_qmap_batch_q(const qsl_qmap_batch_t* B, int job) {

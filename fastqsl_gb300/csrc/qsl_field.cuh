@@ -69,7 +69,6 @@ __device__ __forceinline__ float div_fast(float x, float y) {
     return __fmul_rn(x, r);
 }
 __device__ __forceinline__ float comp(float3 a, int d) { return d == 0 ? a.x : (d == 1 ? a.y : a.z); }
-__device__ __forceinline__ float fcomp(const float* a, int d) { return a[d]; }
 
 struct Dims {
     int nx, ny, nz;

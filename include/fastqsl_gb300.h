@@ -581,7 +581,9 @@ int64_t qsl_qmap_batch_lines(const qsl_qmap_batch_t *batch);
  * end), max_blocks / occupancy as in qsl_batch_run_window. */
 int qsl_qmap_batch_run_main(const qsl_qmap_batch_t *batch, int64_t line_lo, int64_t line_hi, int max_blocks,
                             int occupancy, qsl_stream_t stream);
-/* Everything after the main trace: Q, pseudo-lines and merge of every job. */
+/* Everything after the main trace: Q, pseudo-lines and merge of every job
+ * (the Q assembly, compaction, pseudo Q and merge as one launch each for
+ * the whole batch, the pseudo-line trace as one batched trace). */
 int qsl_qmap_batch_run_post(const qsl_qmap_batch_t *batch, int max_blocks, int occupancy, qsl_stream_t stream);
 /* Device address of job k's Q, float64 (nplanes, n0 - 2, n1 - 2) inside the workspace. */
 double *qsl_qmap_batch_q(const qsl_qmap_batch_t *batch, int job);

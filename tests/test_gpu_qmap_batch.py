@@ -1,8 +1,10 @@
 """The native Q-map batch (qsl_qmap_batch_*) against the Python-built batch
 of the same jobs (QBatch over qsl_plane_seeds / qsl_tile_order seeds): the
-same kernels in the same order, so every Q map must be equal bit for bit,
-whole and run as windows of the main trace, for planes of any orientation,
-several fields, tolerances and sub-boxes of stacked planes."""
+same trace kernels, and the Q assembly, compaction, pseudo Q and merge as
+one launch each over a job table with the per-job kernels' arithmetic, so
+every Q map must be equal bit for bit, whole and run as windows of the main
+trace, for planes of any orientation, several fields, tolerances and
+sub-boxes of stacked planes."""
 import numpy as np
 import pytest
 import torch
@@ -64,6 +66,32 @@ def test_native_batch_equals_python_batch(fields, tile):
     for a, b in zip(ref, got):
         _same(a, b)
     assert sum(int(torch.isfinite(q).sum()) for q in got) > 0.9 * sum(q.numel() for q in got)
+    nb.close()
+
+
+def test_native_batch_many_jobs(fields):
+    """Eleven jobs, several with more than one compaction tile (1024 pixels)
+    and Q grid block per plane, so that the batched Q-assembly launches map
+    blocks to jobs across uneven block ranges."""
+    from fastqsl_gb300 import serving
+    geo = [((24.0, 22.0, 8.0), (0.0, 0.0, 1.0), 0.3, 64, 50, 1), ((24.0, 22.0, 12.0), (0.2, 0.1, 0.97), 0.25, 41, 37, 2),
+           ((23.0, 21.0, 15.0), (1.0, 0.0, 0.0), 0.4, 33, 61, 1), ((22.0, 22.0, 9.0), (0.0, 1.0, 0.0), 0.5, 5, 4, 1),
+           ((25.0, 20.0, 20.0), (0.0, 0.0, 1.0), 0.6, 3, 3, 2), ((24.0, 24.0, 6.0), (0.5, -0.5, 0.7), 0.2, 70, 70, 1),
+           ((21.0, 23.0, 10.0), (0.0, 0.0, 1.0), 0.35, 17, 90, 3), ((20.0, 22.0, 18.0), (0.0, 1.0, 0.0), 0.3, 48, 48, 1),
+           ((26.0, 21.0, 7.0), (0.0, 0.0, 1.0), 0.8, 9, 11, 4), ((24.0, 22.0, 14.0), (1.0, 0.0, 0.0), 0.25, 65, 33, 1),
+           ((22.0, 20.0, 11.0), (0.3, 0.3, 0.9), 0.45, 29, 31, 2)]
+    jobs = []
+    for k, (c, nrm, sp, n0, n1, npl) in enumerate(geo):
+        n, u, v = serving.plane_axes(nrm)
+        jobs.append(dict(field=fields["f%d" % (k % 2)], params=P.absolute_rkf45(tol=(1e-4, 1e-3)[k % 2]), center=c,
+                         normal=n, u=u, v=v, spacing=sp, n0=n0, n1=n1, nplanes=npl, s_len=0.25, tol_coef=1.0))
+    ref = [q.clone() for q in _qbatch(jobs, (8, 8)).run()]
+    nb = api.PlaneQBatch(jobs, tile=(8, 8))
+    got = nb.run()
+    torch.cuda.synchronize()
+    for a, b in zip(ref, got):
+        _same(a, b)
+    assert sum(int(torch.isfinite(q).sum()) for q in got) > 0.8 * sum(q.numel() for q in got)
     nb.close()
 
 
