@@ -57,20 +57,29 @@ __device__ __forceinline__ float3 along(float3 u, const float3 g[3]) {
 }
 
 // Unit field and its gradient by central differences of the unit field at
-// p +- 1e-3 e_j (the offset applied in double and narrowed, as `x -= 0.001`
-// on a float does).
+// p +- 1e-3 e_j.  Exact arithmetic: the offset applied in double and
+// narrowed, as `x -= 0.001` on a float does, and the difference divided by
+// 0.002f.  Fast arithmetic: the offset 0.001f added in float and the
+// difference multiplied by 500 (rounding-level differences; no FP64 add or
+// IEEE divide, nine of each per right-hand side otherwise).
 template <bool EXACT, class F>
 __device__ __forceinline__ float3 unit_and_grad_fd(const F& f, float3 p, float3 g[3], unsigned& ns) {
     const float3 b = sample<EXACT>(f, p, true);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         float3 lo = p, hi = p;
-        if (j == 0) { lo.x = (float)((double)lo.x - 0.001); hi.x = (float)((double)hi.x + 0.001); }
-        if (j == 1) { lo.y = (float)((double)lo.y - 0.001); hi.y = (float)((double)hi.y + 0.001); }
-        if (j == 2) { lo.z = (float)((double)lo.z - 0.001); hi.z = (float)((double)hi.z + 0.001); }
+        if (EXACT) {
+            if (j == 0) { lo.x = (float)((double)lo.x - 0.001); hi.x = (float)((double)hi.x + 0.001); }
+            if (j == 1) { lo.y = (float)((double)lo.y - 0.001); hi.y = (float)((double)hi.y + 0.001); }
+            if (j == 2) { lo.z = (float)((double)lo.z - 0.001); hi.z = (float)((double)hi.z + 0.001); }
+        } else {
+            if (j == 0) { lo.x = lo.x - 0.001f; hi.x = hi.x + 0.001f; }
+            if (j == 1) { lo.y = lo.y - 0.001f; hi.y = hi.y + 0.001f; }
+            if (j == 2) { lo.z = lo.z - 0.001f; hi.z = hi.z + 0.001f; }
+        }
         const float3 b1 = sample<EXACT>(f, lo, true);
         const float3 b2 = sample<EXACT>(f, hi, true);
-        g[j] = (b2 - b1) / 0.002f;
+        g[j] = EXACT ? (b2 - b1) / 0.002f : 500.f * (b2 - b1);
     }
     ns += 7;
     return b;
