@@ -253,7 +253,9 @@ static void stretch_constants_host(FieldStretchT<M>& f, const float* ax, const f
         clo[k] = (float)((double)lo[k] + 1e-6);
         chi[k] = (float)((double)hi[k] - 1e-6);
         us[k] = (hi[k] - lo[k]) / (float)n[k];
-        binv[k] = (float)(STRETCH_BINS_PER_CELL * (n[k] - 1)) / (hi[k] - lo[k]);
+        // tables: bins per unit coordinate; uniform formula: 1 / us (as
+        // store_prepare forms them on the device)
+        binv[k] = (M == 2 || M == 4) ? 1.0f / us[k] : (float)(STRETCH_BINS_PER_CELL * (n[k] - 1)) / (hi[k] - lo[k]);
     }
     f.lo = make_float3(lo[0], lo[1], lo[2]);
     f.hi = make_float3(hi[0], hi[1], hi[2]);

@@ -246,7 +246,8 @@ struct FieldStretchT {
     //            them, else the range (k_stretch_tables)
     const float4* srec;
     const float4* sbin;
-    float3 sbinv;         // bins per unit coordinate (set at kernel start)
+    float3 sbinv;         // search tables (M = 1, 3): bins per unit coordinate; uniform formula
+                          // (M = 2, 4): 1 / us, the fast arithmetic's reciprocal (set at kernel start)
     __device__ __forceinline__ float corners(int ix, int iy, int iz, float3 c[8]) const {
         if constexpr (M == 1 || M == 2) {
 #pragma unroll
@@ -714,6 +715,15 @@ __device__ __forceinline__ int stretch_uni(float c, int n, float a0, float du) {
     r = r < 0 ? 0 : r;
     return r > n - 2 ? n - 2 : r;
 }
+// Fast form: the quotient as a product with inv = 1 / du (formed once per
+// kernel); it can differ from the divide's only where (c - a0) / du lies
+// within an ulp or two of an integer, which moves the formula's switch point
+// between two cells by that much.
+__device__ __forceinline__ int stretch_uni_fast(float c, int n, float a0, float inv) {
+    int r = __float2int_rd((c - a0) * inv);
+    r = r < 0 ? 0 : r;
+    return r > n - 2 ? n - 2 : r;
+}
 
 // The reference search's cell for c through the tables of a packed store
 // (FieldStretchP): srec[j] is the cell the reference's search returns for
@@ -780,7 +790,8 @@ __device__ __forceinline__ void stretch_locate(const FieldStretchT<M>& f, int k,
     if constexpr (stretch_search_mode<M>() == 1) {
         i = stretch_table<M, WIDE>(f, k, c, a0, binv, ai, di);
     } else {
-        if constexpr (stretch_search_mode<M>() == 2) i = stretch_uni(c, n, a0, du);
+        if constexpr (stretch_search_mode<M>() == 2)
+            i = EXACT ? stretch_uni(c, n, a0, du) : stretch_uni_fast(c, n, a0, binv);
         else i = stretch_bisect(c, n, a);
         ai = __ldg(a + i);
         di = __ldg(a + i + 1) - ai;

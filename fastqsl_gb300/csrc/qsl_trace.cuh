@@ -375,6 +375,9 @@ __device__ __forceinline__ void store_prepare(FieldStretchT<M>& f) {
         f.sbinv = v3((float)(STRETCH_BINS_PER_CELL * (f.d.nx - 1)) / (f.hi.x - f.lo.x),
                      (float)(STRETCH_BINS_PER_CELL * (f.d.ny - 1)) / (f.hi.y - f.lo.y),
                      (float)(STRETCH_BINS_PER_CELL * (f.d.nz - 1)) / (f.hi.z - f.lo.z));
+    } else if constexpr (M == 4) {
+        // the uniform formula's reciprocal spacing (fast arithmetic)
+        f.sbinv = v3(1.f / f.us.x, 1.f / f.us.y, 1.f / f.us.z);
     }
 }
 // The current density is always the caller's arrays: a view of them on the

@@ -94,10 +94,14 @@ def test_dropin_stretch_exact_matches_reference(cuda, oracle_port, name):
         assert close[live].mean() >= 0.99, close[live].mean()
 
 
-def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
+@pytest.mark.parametrize("uni", [False, True])
+def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port, uni):
+    """The native entry in fast arithmetic (cell search through the tables,
+    or the uniform-spacing formula as a reciprocal product) against the FP64
+    oracle of the same search."""
     from fastqsl_gb300 import api, synthetic as S
     spec = S.bipole4_stretch(5)
-    coords = S.stretched_axes(spec.shape, z_ratio=1.05)
+    coords = S.stretched_axes(spec.shape, z_ratio=1.0 if uni else 1.05)
     Bx, By, Bz = S.make_field_coords(spec, *coords)
     xs, ys, zs, _ = S.plane_seeds((-5, 5), (-4, 4), 48, 40, 0.3)
     # tight tolerance: at 1e-5 the FP32 rounding alone already moves 13 % of
@@ -105,11 +109,11 @@ def test_native_stretch_fast_vs_fp64_oracle(cuda, oracle_port):
     # the reference-rounding FP32 oracle tracks FP64 to 1e-3 on > 99.8 %
     prm = P.reference_stretch(arith=P.ARITH_FAST).copy(tol_law=P.TOL_ABSOLUTE, tol=1e-7, h_min=1e-4, h_max=0.25)
     ref = oracle_port.trace_all("port64", Bx, By, Bz, xs, ys, zs, s_len=0.01, params=prm.copy(arith=P.ARITH_EXACT),
-                                coords=coords)
+                                coords=coords, uni=uni)
     samples = torch.zeros(1, dtype=torch.int64, device="cuda")
     out = api.trace_stretch(*[torch.from_numpy(np.asfortranarray(b)) for b in (Bx, By, Bz)],
                             [torch.from_numpy(c).cuda() for c in coords], _dev(xs), _dev(ys), _dev(zs), prm,
-                            s_len=0.01, samples=samples)
+                            s_len=0.01, samples=samples, uni=uni)
     torch.cuda.synchronize()
     got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
     flags = ((got["flag_start"] == ref["flag_start"]) & (got["flag_end"] == ref["flag_end"])).mean()
