@@ -308,13 +308,16 @@ __device__ void scott_line(const F& f, const ScottJob<F>& J, long long i, float 
                 const float3 j1 = sample<EXACT>(current_view(f, J.cur), b.p, false);
                 bp1 = sample<EXACT>(f, b.p, false);
                 ns += 2;
-                td = dot(j1, bp1) / dot(bp1, bp1);
-                tw = tw + (double)td / 4.0 / kRefPi * (double)dl;
+                // fast arithmetic: the main tracer's integrand and one
+                // float product (no FP64 divide per step)
+                td = twist_density<EXACT>(j1, bp1);
+                tw = tw + (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
             }
             flag = box_flag(f.d, b.p);
             if (flag > 0) {
                 len_add(-(double)dl, -dl);
-                if (TWIST && tw_on) tw = tw - (double)td / 4.0 / kRefPi * (double)dl;
+                if (TWIST && tw_on)
+                    tw = tw - (EXACT ? (double)td / 4.0 / kRefPi * (double)dl : (double)(td * dl * kInv4PiF));
                 if (flag <= 6) {
                     const int d = (flag - 1) / 2;
                     const float q1 = comp(a.p, d), q2 = comp(b.p, d);

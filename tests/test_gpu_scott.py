@@ -13,7 +13,9 @@ TraceBlineScott.cu:334-595).
   rounded power: identical flags, footpoints within 1e-3 cell on >= 99.5 %,
   q_perp within 1e-3 relative on >= 99 %;
 * fast arithmetic, both gradients, fp16 bricks included: flags >= 99 %;
-  log10 q_perp within 1e-2 of the FP64 oracle (median).
+  log10 q_perp within 1e-2 of the FP64 oracle (median); with a current
+  density, the twist no further from the FP64 oracle than the reference's
+  own FP32 rounding is (within a factor 1.5, median and 90th percentile).
 """
 import numpy as np
 import pytest
@@ -141,3 +143,44 @@ def test_fast_scott_vs_fp64_oracle(cuda, oracle_port, layout, grad):
          (got["flag_start"] == ref["flag_start"]) & (ref["flag_start"] != 0) & (ref["flag_end"] != 0)
     d = np.abs(np.log10(got["q_perp"][ok]) - np.log10(ref["q_perp"][ok]))
     assert np.median(d) <= 1e-2, np.median(d)
+
+
+@pytest.mark.parametrize("layout,grad", [("soa", "fd"), ("h4b", "analytic")])
+def test_fast_scott_twist_vs_fp64_oracle(cuda, oracle_port, layout, grad):
+    """The twist integral of the fast Scott tracer (the main tracer's fast
+    integrand and 1 / (4 pi) product per step) against the FP64 oracle, on
+    lines whose exit faces agree, measured against the reference's own FP32
+    rounding (the oracle restatement pinned to it, port32cr): on these Scott
+    lines the reference's FP32 twist is itself 7-17 % (median) off FP64 (the
+    line lengths move with the step sequence), so the fast kernel must be
+    no further off than that, within a factor 1.5."""
+    import golden_util as G
+    from fastqsl_gb300 import api
+    Bx, By, Bz, xs, ys, zs = _case()
+    cur = G.twist_current(Bx, By, Bz)
+    prm = P.reference_scott(arith=P.ARITH_FAST)
+    prm.tol = 1e-5
+    prm.h_min = 1e-3
+    prm.h_max = 1.0
+    ex = prm.copy(arith=P.ARITH_EXACT)
+    ref = oracle_port.scott_all("port64", Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=ex, curB=cur)
+    r32 = oracle_port.scott_all("port32cr", Bx, By, Bz, xs, ys, zs, s_len=0.25, tol_coef=1.0, params=ex, curB=cur)
+    fs = api.FieldStore(*[torch.from_numpy(b) for b in (Bx, By, Bz)], layout=layout)
+    curd = [api.as_xfast(torch.from_numpy(np.asfortranarray(c))) for c in cur]  # x-fastest, as the field
+    out = api.trace_scott(fs, _dev(xs), _dev(ys), _dev(zs), prm, s_len=0.25, grad=grad, curB=curd)
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in out.items() if v is not None}
+
+    def err(o):
+        # seeds on the bottom plane trace one direction (flag_start 0, as
+        # the reference); lines whose flags agree and which carry a twist
+        same = (o["flag_start"] == ref["flag_start"]) & (o["flag_end"] == ref["flag_end"]) & (np.abs(ref["twist"]) > 0)
+        rel = np.abs(o["twist"][same] - ref["twist"][same]) / np.maximum(np.abs(ref["twist"][same]), 1e-3)
+        return same.mean(), np.median(rel), np.quantile(rel, 0.9)
+
+    lines, med, p90 = err(got)
+    _, med32, p90_32 = err(r32)
+    print(layout, grad, "scott twist lines %.3f rel err median %.2e p90 %.2e (reference FP32: %.2e / %.2e)" % (
+        lines, med, p90, med32, p90_32))
+    assert lines > 0.5
+    assert med <= 1.5 * med32 and p90 <= 1.5 * p90_32, (med, p90, med32, p90_32)
